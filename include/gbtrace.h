@@ -1,0 +1,159 @@
+/*
+ * gbtrace.h -- C ABI of the GB300 (sm_103a) backend for ChSchmidt99/trace's
+ * pkg/pt hot path: Morton LBVH build, PHR refinement, closest-hit tracing and
+ * the path-tracing render loop.
+ *
+ * Conventions
+ *  - Every call returns GBT_OK (0) or a negative GBT_E* code; the message of
+ *    the last failure on a context is gbt_last_error(ctx).  The Go reference
+ *    panics instead (obj.go:13); a binding turns non-zero codes into panics.
+ *  - Handles are opaque; the library owns all device memory.  Host buffers
+ *    passed in are copied; host output buffers are written before return.
+ *  - All work of a context runs on its own CUDA stream (gbt_ctx_stream).
+ *    Calls without the _async suffix return after the stream is idle; _async
+ *    calls only enqueue, on device buffers, and never allocate.
+ *  - Primitive index space: triangles [0, n_tri), then spheres
+ *    [n_tri, n_tri + n_sph), the order pkg/pt/scene.go:100-114 collects
+ *    tracables in.
+ *  - One context per host thread; no callbacks.
+ */
+#ifndef GBTRACE_H
+#define GBTRACE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBT_OK 0
+#define GBT_EINVAL -1      /* bad argument (null handle, size out of range) */
+#define GBT_ECUDA -2       /* CUDA runtime error */
+#define GBT_ENOMEM -3      /* device or host allocation failed */
+#define GBT_ETIMEOUT -4    /* a bounded device-side wait ran out */
+#define GBT_EDEVICE -5     /* a kernel reported an internal error */
+#define GBT_EUNSUPPORTED -6
+
+typedef struct gbt_ctx gbt_ctx;
+typedef struct gbt_scene gbt_scene;
+typedef struct gbt_bvh gbt_bvh;
+
+typedef struct {
+    float center[3];
+    float radius;
+} gbt_sphere; /* pkg/pt/primitive.go:25-40 Sphere */
+
+#define GBT_MAT_DIFFUSE 0 /* pkg/pt/material.go:25-42 Diffuse{Albedo} */
+#define GBT_MAT_LIGHT 1   /* pkg/pt/material.go:13-23 Light{Color} */
+typedef struct {
+    int32_t type;
+    float color[3];
+} gbt_material;
+
+typedef struct {
+    float origin[3];
+    float tmin;
+    float dir[3]; /* not normalised, as pkg/pt/camera.go:95-97 casts it */
+    float tmax;
+} gbt_ray;
+
+typedef struct {
+    int32_t prim; /* primitive index, -1 on a miss */
+    float t, u, v;
+} gbt_hit;
+
+typedef struct {
+    double look_from[3], look_at[3], up[3]; /* pkg/pt/camera.go:7-11 CameraTransformation */
+    double aspect, fov_deg;                 /* pkg/pt/camera.go:53-59 NewCamera */
+} gbt_camera;
+
+#define GBT_MISS_BLACK 0    /* render.go:228 DefaultMissShader */
+#define GBT_MISS_WHITE 1    /* render.go:232 WhiteMissShader */
+#define GBT_MISS_SKY 2      /* render.go:236 SkyMissShader */
+#define GBT_MISS_CONSTANT 3 /* constant colour (render.go:244 SunMissShader is one) */
+typedef struct {
+    int32_t width, height, spp, max_depth; /* render.go:20-30 ImageRenderer fields */
+    int32_t miss_mode;
+    float miss_color[3];
+    uint64_t seed;
+} gbt_render_params;
+
+typedef struct {
+    uint64_t rays_traced;  /* every traced segment: primary + bounces */
+    uint64_t paths;
+    double ms_total;       /* device time of the render, CUDA events */
+    double ms_traverse;    /* device time inside traversal launches */
+} gbt_render_stats;
+
+/* ---- context -------------------------------------------------------- */
+int gbt_ctx_create(int device, gbt_ctx **out);
+int gbt_ctx_destroy(gbt_ctx *ctx);
+const char *gbt_last_error(const gbt_ctx *ctx);
+void *gbt_ctx_stream(gbt_ctx *ctx); /* the context's cudaStream_t */
+int gbt_ctx_sync(gbt_ctx *ctx);
+
+/* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */
+/* verts: n_tri*9 floats (v0 v1 v2); normals: n_tri*9 per-vertex normals or
+ * NULL for face normals (NewTriangleWithoutNormals, primitive.go:116-132);
+ * prim_mat: n_tri+n_sph material indices into mats. */
+int gbt_scene_upload(gbt_ctx *ctx, const float *verts, const float *normals, uint32_t n_tri,
+                     const gbt_sphere *spheres, uint32_t n_sph, const uint32_t *prim_mat,
+                     const gbt_material *mats, uint32_t n_mat, gbt_scene **out);
+int gbt_scene_destroy(gbt_scene *scene);
+
+/* OBJ loader: pkg/pt/obj.go:10-140 ParseFromPath (fan triangulation,
+ * negative indices, v/vn/f).  Two calls: first with verts == NULL to get
+ * *n_tri and *has_normals, then with buffers of n_tri*9 floats. */
+int gbt_obj_parse(const char *path, float *verts, float *normals, uint32_t *n_tri, int32_t *has_normals);
+
+/* ---- BVH builders --------------------------------------------------- */
+/* pkg/pt/lbvh.go:13-25 DefaultLBVH: Morton codes, LSD radix sort, Karras-style
+ * hierarchy emission and bottom-up refit, all on the device. */
+int gbt_lbvh_build(gbt_ctx *ctx, gbt_scene *scene, gbt_bvh **out);
+/* Rebuild an LBVH in place over the scene it was built from (after the scene's
+ * vertices changed through gbt_scene_update_async).  Enqueue only. */
+int gbt_lbvh_rebuild_async(gbt_ctx *ctx, gbt_bvh *bvh);
+int gbt_scene_update_async(gbt_ctx *ctx, gbt_scene *scene, const float *d_verts);
+
+/* pkg/pt/phr.go:47-84 PhrBuilder.BuildFromAuxilary over an LBVH from
+ * gbt_lbvh_build; alpha/delta/branching as NewPHRBuilder (phr.go:30-40). */
+int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out);
+int gbt_bvh_destroy(gbt_bvh *bvh);
+
+int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost); /* bvh.go:46-48 BVH.Cost */
+int gbt_bvh_size(gbt_ctx *ctx, gbt_bvh *bvh, int64_t *size); /* bvh.go:50-52 BVH.Size */
+/* counts[0] nodes, [1] leaves, [2] primitive references, [3] root is a leaf */
+int gbt_bvh_counts(gbt_ctx *ctx, gbt_bvh *bvh, int64_t counts[4]);
+/* Depth-first pre-order export, children in stored order: kind (1 leaf),
+ * count (children or primitives), box (lo.xyz, hi.xyz), leaf primitives. */
+int gbt_bvh_export(gbt_ctx *ctx, gbt_bvh *bvh, int8_t *kind, int32_t *count, double *box, int32_t *prims);
+/* LBVH only: the sorted (Morton code, primitive index) pairs (lbvh.go:216-219). */
+int gbt_lbvh_sorted(gbt_ctx *ctx, gbt_bvh *bvh, uint64_t *codes, int32_t *idx);
+
+/* ---- queries -------------------------------------------------------- */
+/* Closest hit per ray (bvh.go:74-77 BVH.intersected over primitive.go:56-86
+ * and :172-208), host buffers. */
+int gbt_trace(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_ray *rays, uint32_t n, gbt_hit *hits);
+/* Same on device buffers; enqueue only. */
+int gbt_trace_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits);
+
+/* ---- renderer (render.go:91-129 ImageRenderer.RenderToBuffer) -------- */
+/* rgb: width*height*3 floats, row y=0 is the bottom row (buffer.go:47-49
+ * order); each pixel is the mean of spp samples. */
+int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+               float *rgb, gbt_render_stats *stats);
+/* Same into a device buffer; enqueue only; stats are read by gbt_render_last_stats. */
+int gbt_render_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+                     float *d_rgb);
+int gbt_render_last_stats(gbt_ctx *ctx, gbt_render_stats *stats);
+
+/* ---- device memory helpers for callers without a CUDA runtime ------- */
+int gbt_device_alloc(gbt_ctx *ctx, size_t bytes, void **d_ptr);
+int gbt_device_free(gbt_ctx *ctx, void *d_ptr);
+int gbt_copy_h2d_async(gbt_ctx *ctx, void *d_dst, const void *h_src, size_t bytes);
+int gbt_copy_d2h_async(gbt_ctx *ctx, void *h_dst, const void *d_src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

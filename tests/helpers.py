@@ -1,0 +1,59 @@
+"""Comparison helpers shared by the parity tests."""
+import numpy as np
+
+
+def classify_disagreements(orc_bvh, rays, gpu_prim, gpu_t, orc_prim, orc_t, rel_tie=1e-5, edge=1e-4):
+    """Split hit-ID disagreements into near-ties and hard mismatches.
+
+    near-tie: both primitives are hit in float64 at distances within rel_tie
+    (an equal-distance tie whose winner depends on traversal order), or the
+    primitive one side reports lies within `edge` of a barycentric or
+    distance boundary in float64 (float32 rounding decides it).
+    """
+    bad = np.nonzero(gpu_prim != orc_prim)[0]
+    near, hard = [], []
+    for i in bad:
+        r = rays[i]
+        gp, op = int(gpu_prim[i]), int(orc_prim[i])
+        tie = False
+        if gp >= 0 and op >= 0:
+            ok, t, u, v, det = orc_bvh.prim_intersect(gp, r)
+            if ok and abs(t - orc_t[i]) <= rel_tie * max(1.0, abs(orc_t[i])):
+                tie = True
+        for p in (gp, op):
+            if tie or p < 0:
+                continue
+            ok, t, u, v, det = orc_bvh.prim_intersect(p, r)
+            margin = min(abs(u), abs(1 - u), abs(v), abs(1 - u - v))
+            if margin <= edge or abs(abs(det) - 1e-7) <= 1e-7 * 0.5 or abs(t - r[3]) <= edge * max(1.0, abs(t)):
+                tie = True
+            if p == gp and op >= 0 and not ok:
+                # the GPU's primitive is not hit in float64 but the closest is: compare distances
+                ok2, t2, *_ = orc_bvh.prim_intersect(op, r)
+                if ok2 and np.isfinite(t) and abs(t - t2) <= 1e-4 * max(1.0, abs(t2)):
+                    tie = True
+        (near if tie else hard).append(int(i))
+    return np.asarray(near, np.int64), np.asarray(hard, np.int64)
+
+
+def canonical_equal(a, b):
+    """Exact equality of two pre-order exports (kind, count, box, prims)."""
+    ka, ca, ba, pa = a
+    kb, cb, bb, pb = b
+    return (ka.shape == kb.shape and np.array_equal(ka, kb) and np.array_equal(ca, cb)
+            and np.array_equal(pa, pb) and np.array_equal(ba, bb))
+
+
+def first_mismatch(a, b):
+    ka, ca, ba, pa = a
+    kb, cb, bb, pb = b
+    n = min(len(ka), len(kb))
+    for i in range(n):
+        if ka[i] != kb[i] or ca[i] != cb[i]:
+            return "node %d kind/count %s/%s vs %s/%s" % (i, ka[i], ca[i], kb[i], cb[i])
+        if not np.array_equal(ba[i], bb[i]):
+            return "node %d box %s vs %s" % (i, ba[i], bb[i])
+    if len(ka) != len(kb):
+        return "node count %d vs %d" % (len(ka), len(kb))
+    m = np.nonzero(pa != pb)[0]
+    return "prims differ at %s" % m[:5] if len(m) else "equal"

@@ -1,0 +1,78 @@
+"""GPU wavefront path tracer vs the oracle's path tracer (statistical parity).
+
+Both sides sample with their own random numbers (the reference seeds from the
+clock), so images are compared through their error against a converged
+oracle image: at equal spp the GPU image's per-channel RMSE must be within
+RMSE_RATIO of the oracle's own, and the converged means must agree.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from trace_gb300 import pt, scenes
+
+pytestmark = pytest.mark.gpu
+
+RMSE_RATIO = 1.15   # GPU RMSE / oracle RMSE at equal spp, per channel
+MEAN_REL = 0.01     # relative difference of the image means at high spp
+BLOCK_REL = 0.03    # relative RMSE of 8x8 block means at high spp
+
+
+def rmse(a, b):
+    return np.sqrt(np.mean((a - b) ** 2, axis=(0, 1)))
+
+
+def blocks(img, k=8):
+    h, w, _ = img.shape
+    return img[: h // k * k, : w // k * k].reshape(h // k, k, w // k, k, 3).mean(axis=(1, 3))
+
+
+def run(ctx, s, w, h, spp_eq, spp_conv, spp_hi, max_depth=None):
+    rd = s["render"]
+    md = rd["max_depth"] if max_depth is None else max_depth
+    cam = dict(s["camera"], aspect=w / h)
+    s2 = dict(s, camera=cam)
+    o = O.lbvh(s["verts"], s.get("spheres"))
+    conv = o.render(s2, width=w, height=h, spp=spp_conv, max_depth=md, seed=101)
+    orc = o.render(s2, width=w, height=h, spp=spp_eq, max_depth=md, seed=202)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    gpu, st = g.render(cam, w, h, spp_eq, md, rd["miss_mode"], rd["miss_color"], seed=303)
+    gpu_hi, st_hi = g.render(cam, w, h, spp_hi, md, rd["miss_mode"], rd["miss_color"], seed=404)
+    r_g, r_o = rmse(gpu, conv), rmse(orc, conv)
+    print("rmse gpu", r_g, "oracle", r_o, "means", gpu_hi.mean(axis=(0, 1)), conv.mean(axis=(0, 1)),
+          "rays", st["rays_traced"])
+    assert np.all(r_g <= RMSE_RATIO * r_o + 1e-6), (r_g, r_o)
+    m_g, m_c = gpu_hi.mean(axis=(0, 1)), conv.mean(axis=(0, 1))
+    assert np.all(np.abs(m_g - m_c) <= MEAN_REL * np.maximum(m_c, 1e-3)), (m_g, m_c)
+    bg, bc = blocks(gpu_hi), blocks(conv)
+    brel = np.sqrt(np.mean((bg - bc) ** 2)) / max(bc.mean(), 1e-3)
+    assert brel <= BLOCK_REL, brel
+    return st
+
+
+def test_render_cornell(ctx):
+    st = run(ctx, scenes.cornell(), 96, 96, spp_eq=16, spp_conv=512, spp_hi=1024)
+    assert st["rays_traced"] >= 96 * 96 * 16
+
+
+def test_render_soup_primary_plus_bounce(ctx):
+    s = scenes.soup(200_000, seed=1)
+    st = run(ctx, s, 160, 90, spp_eq=4, spp_conv=256, spp_hi=512)
+    # MaxDepth 0: one primary ray per path plus one bounce per primary hit
+    assert 160 * 90 * 4 <= st["rays_traced"] <= 2 * 160 * 90 * 4
+
+
+def test_render_terrain_sun_constant_sky(ctx):
+    s = scenes.terrain(g=129)
+    run(ctx, s, 96, 54, spp_eq=16, spp_conv=512, spp_hi=1024)
+
+
+def test_render_emitter_exact(ctx):
+    """Looking straight at a Light quad with MaxDepth 0 gives exactly its colour."""
+    quad = np.array([[-1, -1, 0, 1, -1, 0, 1, 1, 0], [-1, -1, 0, 1, 1, 0, -1, 1, 0]], np.float32)
+    ds = pt.DeviceScene(ctx, quad, prim_mat=np.array([0, 0]), mat_type=[1], mat_color=[[10.0, 10.0, 10.0]])
+    g = pt.DefaultLBVH(ds)
+    cam = dict(look_from=(0, 0, 2), look_at=(0, 0, 0), up=(0, 1, 0), fov=20.0, aspect=1.0)
+    img, st = g.render(cam, 8, 8, 2, 0)
+    np.testing.assert_allclose(img, 10.0)

@@ -1,0 +1,109 @@
+"""GPU closest-hit traversal vs the float64 oracle on fixed deterministic ray sets.
+
+Bar: >= 99.99% hit-ID agreement; every disagreement classified, near-ties
+(equal-distance ties and float32 edge cases) counted and bounded; hit
+distance within 1e-5 relative of float64 Moeller-Trumbore.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import classify_disagreements
+from trace_gb300 import pt, scenes
+
+pytestmark = pytest.mark.gpu
+
+T_REL = 1e-5  # relative hit-distance tolerance vs the float64 oracle
+
+
+def bounce_rays(ds_verts, rays, prim, t, seed=9):
+    """One cosine-weighted bounce from each primary hit (deterministic)."""
+    v = ds_verts.astype(np.float64).reshape(-1, 3, 3)
+    hit = prim >= 0
+    o = rays[hit, 0:3].astype(np.float64) + rays[hit, 4:7].astype(np.float64) * t[hit, None]
+    tri = v[prim[hit]]
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    d = rays[hit, 4:7].astype(np.float64)
+    n = np.where((np.einsum("ij,ij->i", n, d) < 0)[:, None], n, -n)
+    rng = np.random.default_rng(seed)
+    z = 1 - 2 * rng.random(len(n))
+    phi = 2 * np.pi * rng.random(len(n))
+    r = np.sqrt(1 - z * z)
+    sd = n + np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    out = np.empty((len(n), 8), np.float32)
+    out[:, 0:3] = o
+    out[:, 3] = 1e-4
+    out[:, 4:7] = sd
+    out[:, 7] = np.inf
+    return out
+
+
+def check(ctx, bvh_gpu, bvh_orc, rays, label):
+    gp, gt, gu, gv = bvh_gpu.trace(rays)
+    op, ot, ou, ov = bvh_orc.trace(rays)
+    agree = (gp == op).mean()
+    near, hard = classify_disagreements(bvh_orc, rays, gp, gt, op, ot)
+    both = (gp == op) & (op >= 0)
+    rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
+    print("%s: rays=%d hit=%.4f agree=%.6f near=%d hard=%d t_rel_max=%.2e t_rel_p999=%.2e" % (
+        label, len(rays), (op >= 0).mean(), agree, len(near), len(hard), rel.max() if rel.size else 0,
+        np.quantile(rel, 0.999) if rel.size else 0))
+    assert len(hard) == 0, "hard hit-ID mismatches at rays %s" % hard[:10]
+    assert agree >= 0.9999 or len(near) <= 1e-4 * len(rays) + 2
+    assert len(near) <= 1e-3 * len(rays) + 2
+    assert (rel <= T_REL).mean() >= 0.9999
+    return gp, gt
+
+
+def test_trace_cornell(ctx):
+    s = scenes.cornell()
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    o = O.lbvh(s["verts"])
+    rays = scenes.camera_rays(s["camera"], 256, 256, jitter_seed=1)
+    gp, gt = check(ctx, g, o, rays, "cornell primary")
+    b = bounce_rays(s["verts"], rays, gp, gt)
+    check(ctx, g, o, b, "cornell bounce")
+
+
+@pytest.mark.parametrize("n,w,h", [(100_000, 480, 270), (1_000_000, 960, 540)])
+def test_trace_soup(ctx, n, w, h):
+    s = scenes.soup(n, seed=1)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    o = O.lbvh(s["verts"])
+    rays = scenes.camera_rays(s["camera"], w, h, jitter_seed=2)
+    gp, gt = check(ctx, g, o, rays, "soup%d primary" % n)
+    b = bounce_rays(s["verts"], rays, gp, gt)
+    check(ctx, g, o, b, "soup%d bounce" % n)
+
+
+def test_trace_terrain_with_sphere(ctx):
+    s = scenes.terrain(g=513, width=320, height=180)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    o = O.lbvh(s["verts"], s["spheres"])
+    rays = scenes.camera_rays(s["camera"], 320, 180, jitter_seed=3)
+    gp, gt = check(ctx, g, o, rays, "terrain primary")
+    # rays aimed at the sphere light
+    c = s["spheres"][0, :3].astype(np.float64)
+    org = np.array(s["camera"]["look_from"], np.float64)
+    rr = np.zeros((64, 8), np.float32)
+    rr[:, 0:3] = org
+    rr[:, 3] = 1e-3
+    rng = np.random.default_rng(4)
+    rr[:, 4:7] = (c - org) + rng.normal(scale=0.05, size=(64, 3))
+    rr[:, 7] = np.inf
+    check(ctx, g, o, rr, "terrain sphere rays")
+
+
+def test_trace_empty_and_miss(ctx):
+    s = scenes.soup(1000, seed=3)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    p, t, u, v = g.trace(np.zeros((0, 8), np.float32))
+    assert p.shape == (0,)
+    away = np.array([[0.5, 0.5, 3.0, 0.0, 0.0, 0.0, 1.0, np.inf]], np.float32)
+    p, t, u, v = g.trace(away)
+    assert p[0] == -1 and np.isinf(t[0])

@@ -1,0 +1,116 @@
+// Internal declarations shared by the CUDA translation units of libgbtrace.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gbtrace.h"
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+#define GBT_DEVERR_SPIN 1u       // a bounded spin-wait ran out
+#define GBT_DEVERR_BOUNDS 2u     // an index check failed and the access was skipped
+#define GBT_DEVERR_STACK 4u      // traversal stack overflow (deepest entries dropped)
+#define GBT_DEVERR_CAPACITY 8u   // a device work list was full
+
+// Iteration limit of every device-side spin-wait.  With the 64 ns back-off it
+// bounds one wait at roughly a quarter of a second.
+#define GBT_SPIN_LIMIT (1u << 22)
+
+struct gbt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    unsigned int *d_error = nullptr;  // device error word (GBT_DEVERR_*)
+    int num_sms = 0;
+    // grow-only scratch, reused by every build on this context
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // render state (grow-only)
+    void *rstate = nullptr;
+    size_t rstate_bytes = 0;
+    gbt_render_stats last_stats{};
+    unsigned long long *d_ray_total = nullptr;  // rays traced by the last render (device)
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+struct gbt_scene {
+    gbt_ctx *ctx = nullptr;
+    uint32_t n_tri = 0, n_sph = 0, n_mat = 0;
+    float *d_verts = nullptr;      // n_tri*9, input order
+    float *d_normals = nullptr;    // n_tri*9 or null
+    float4 *d_sph = nullptr;       // n_sph (center, radius)
+    uint32_t *d_prim_mat = nullptr;
+    float4 *d_mats = nullptr;      // (color.rgb, type)
+    std::vector<gbt_material> mats;
+};
+
+// Device-resident header of a BVH: the root entry (a node or a leaf) and sizes.
+struct BvhHeader {
+    int32_t root_ref;  // node index, or first primitive record when root_cnt > 0
+    int32_t root_cnt;  // > 0: the root is a leaf of root_cnt primitives
+    uint32_t n_unique; // LBVH: distinct Morton codes (= leaves)
+    uint32_t n_nodes;  // inner nodes in use
+    uint32_t sorted_sel; // LBVH: which half of d_codes/d_idx holds the sorted pairs
+    uint32_t pad[3];
+    float root_lo[4];
+    float root_hi[4];
+};
+
+#define GBT_BVH_LBVH 0
+#define GBT_BVH_PHR 1
+
+struct gbt_bvh {
+    gbt_ctx *ctx = nullptr;
+    gbt_scene *scene = nullptr;
+    int kind = GBT_BVH_LBVH;
+    int arity = 2;              // 2: 64-byte nodes; 4: 128-byte nodes
+    uint32_t n_prim = 0;        // primitive records
+    uint32_t node_cap = 0;      // allocated inner nodes
+    float4 *d_nodes = nullptr;  // arity 2: 4 float4 per node; arity 4: 8 float4 per node
+    float4 *d_prims = nullptr;  // 3 float4 per primitive record, in leaf order
+    BvhHeader *d_hdr = nullptr;
+    // LBVH products kept for parity checks and PHR
+    uint64_t *d_codes = nullptr;    // sorted Morton codes
+    uint32_t *d_idx = nullptr;      // sorted primitive indices
+    uint32_t *d_run = nullptr;      // start of each distinct-code run, n_unique+1 entries
+    uint64_t *d_ukey = nullptr;     // distinct codes
+    int32_t *d_parent = nullptr;    // per inner node: parent node (-1 root) -- LBVH only
+    uint32_t *d_size = nullptr;     // per inner node: subtree size (bvh.go:159-167)
+    int32_t *d_other = nullptr;     // emission hand-off words
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+int gbt_fail(gbt_ctx *ctx, int code, const std::string &msg);
+int gbt_cuda_fail(gbt_ctx *ctx, cudaError_t e, const char *what);
+int gbt_check_device_error(gbt_ctx *ctx, const char *what);
+int gbt_scratch(gbt_ctx *ctx, size_t bytes, void **out);
+
+#define GBT_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return gbt_cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+static inline size_t gbt_align(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// entry points between translation units
+// ---------------------------------------------------------------------------
+// lbvh.cu
+int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh);
+size_t gbt_lbvh_scratch_bytes(uint32_t n);
+// traverse.cu
+int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits);
+void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
+                         const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s);
+// render.cu
+int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
+                       float *d_rgb);
+// phr.cu
+int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, gbt_bvh *out);

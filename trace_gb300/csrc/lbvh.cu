@@ -1,0 +1,676 @@
+// Morton-code LBVH construction on the device.
+//
+// Restates pkg/pt/lbvh.go:13-25 (DefaultLBVH) as a chain of kernels on one
+// stream, with no host synchronisation:
+//   k_bounds     scene box, fp64 min/max fold            (bounding.go:19-25)
+//   k_morton     fp64 quantisation + bit interleave       (lbvh.go:64-73, morton.go:6-20)
+//   k_hist, k_sort_plan, k_onesweep x8
+//                stable LSD radix sort of (code, index)   (lbvh.go:216-301 bucket sort)
+//   k_rle_*      runs of equal codes -> leaves            (lbvh.go:134-145, 179-181)
+//   k_gather     primitive records in leaf order
+//   k_emit       binary radix tree over the distinct codes with the
+//                bottom-up box refit fused in             (lbvh.go:76-203, bvh.go:104-126,201-222)
+#include <cuda_runtime.h>
+
+#include "gbt_internal.cuh"
+
+namespace {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 16;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+constexpr uint32_t ST_AGG = 1u << 30;
+constexpr uint32_t ST_PREFIX = 2u << 30;
+constexpr uint32_t ST_FLAGS = 3u << 30;
+constexpr uint32_t ST_VALUE = (1u << 30) - 1;
+
+// ---------------------------------------------------------------------------
+// small device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Order-preserving map of a double onto uint64 (for atomicMin/atomicMax).
+__device__ __forceinline__ unsigned long long dbl_to_ord(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double ord_to_dbl(unsigned long long o) {
+    unsigned long long b = (o >> 63) ? (o & 0x7fffffffffffffffULL) : ~o;
+    return __longlong_as_double((long long)b);
+}
+
+// Primitive box in float64: triangle min/max of three widened floats
+// (primitive.go:102-114), sphere centre -/+ radius (primitive.go:31-40).
+__device__ __forceinline__ void prim_box_f64(const float *__restrict__ verts, const float4 *__restrict__ sph,
+                                             uint32_t n_tri, uint32_t i, double lo[3], double hi[3]) {
+    if (i < n_tri) {
+        const float *t = verts + (size_t)i * 9;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float a = t[k], b = t[3 + k], c = t[6 + k];
+            lo[k] = (double)fminf(fminf(a, b), c);
+            hi[k] = (double)fmaxf(fmaxf(a, b), c);
+        }
+    } else {
+        float4 s = sph[i - n_tri];
+        double r = (double)s.w;
+        lo[0] = __dsub_rn((double)s.x, r);
+        lo[1] = __dsub_rn((double)s.y, r);
+        lo[2] = __dsub_rn((double)s.z, r);
+        hi[0] = __dadd_rn((double)s.x, r);
+        hi[1] = __dadd_rn((double)s.y, r);
+        hi[2] = __dadd_rn((double)s.z, r);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// scene bounds
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_bounds(const float *__restrict__ verts, const float4 *__restrict__ sph,
+                                                uint32_t n_tri, uint32_t n, unsigned long long *acc) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double a[3], b[3];
+        prim_box_f64(verts, sph, n_tri, i, a, b);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            lo[k] = fmin(lo[k], a[k]);
+            hi[k] = fmax(hi[k], b[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fmin(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmax(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    __shared__ double s[8][6];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+        for (int k = 0; k < 3; k++) { s[w][k] = lo[k]; s[w][3 + k] = hi[k]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int k = threadIdx.x;
+        double v = s[0][k];
+        for (int j = 1; j < (int)(blockDim.x >> 5); j++) v = k < 3 ? fmin(v, s[j][k]) : fmax(v, s[j][k]);
+        if (k < 3) atomicMin(&acc[k], dbl_to_ord(v));
+        else atomicMax(&acc[k], dbl_to_ord(v));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Morton codes
+// ---------------------------------------------------------------------------
+// Interleave: bit k of a moves to bit 3k (the standard shift-and-mask spread
+// of 21 bits over 63).
+__device__ __forceinline__ uint64_t spread3(uint64_t a) {
+    uint64_t x = a & 0x1fffffULL;
+    x = (x | (x << 32)) & 0x001f00000000ffffULL;
+    x = (x | (x << 16)) & 0x001f0000ff0000ffULL;
+    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+    x = (x | (x << 2)) & 0x1249249249249249ULL;
+    return x;
+}
+
+// uint64(dx / step) exactly as the reference computes it: a correctly rounded
+// float64 division, truncated.  The product with the rounded reciprocal is
+// within a few ulp of the quotient, so its integer part is the answer unless
+// the quotient lies within 2^-26 of an integer; only then is the division done.
+__device__ __forceinline__ uint64_t quantise(double dx, double step, double rstep) {
+    double qa = __dmul_rn(dx, rstep);
+    if (qa >= 0.0 && qa < 4194304.0) {
+        double f = floor(qa);
+        double fr = qa - f;
+        if (fr > 0x1p-26 && fr < 1.0 - 0x1p-26) return (uint64_t)f;
+    }
+    double q = __ddiv_rn(dx, step);
+    if (!(q < 9223372036854775808.0) || q < 0.0) return 0;  // NaN (zero-extent axis) or out of domain
+    return (uint64_t)__double2ull_rz(q);
+}
+
+__global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts, const float4 *__restrict__ sph,
+                                                uint32_t n_tri, uint32_t n, const unsigned long long *__restrict__ acc,
+                                                uint64_t *__restrict__ codes) {
+    __shared__ double s_e[9];  // lo.xyz, step.xyz, 1/step.xyz
+    if (threadIdx.x < 3) {
+        int k = threadIdx.x;
+        double lo = ord_to_dbl(acc[k]), hi = ord_to_dbl(acc[3 + k]);
+        double ext = __dsub_rn(hi, lo);                 // aabb.update width/height/depth
+        double step = __ddiv_rn(ext, 2097151.0);        // extent / (MORTON_SIZE-1)
+        s_e[k] = lo;
+        s_e[3 + k] = step;
+        s_e[6 + k] = __drcp_rn(step);
+    }
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double lo[3], hi[3];
+        prim_box_f64(verts, sph, n_tri, i, lo, hi);
+        uint64_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            double c = __dmul_rn(__dadd_rn(lo[k], hi[k]), 0.5);  // aabb barycenter
+            double dx = fabs(__dsub_rn(s_e[k], c));
+            q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
+        }
+        codes[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// LSD radix sort: 8 passes of 8 bits, one-sweep with decoupled look-back
+// ---------------------------------------------------------------------------
+struct SortPlan {
+    const uint64_t *in_k[8];
+    uint64_t *out_k[8];
+    const uint32_t *in_v[8];
+    uint32_t *out_v[8];
+    uint32_t active[8];
+    uint32_t identity[8];
+    uint64_t *final_k;
+    uint32_t *final_v;
+    uint32_t final_sel;
+    uint32_t pad;
+    uint32_t digit_base[8][256];
+};
+
+struct SortScratch {  // byte offsets inside one scratch allocation
+    size_t plan, hist, ctr, status, total;
+    uint32_t n_tiles;
+};
+
+SortScratch sort_layout(uint32_t n, size_t base) {
+    SortScratch s;
+    s.n_tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    s.plan = gbt_align(base);
+    s.hist = gbt_align(s.plan + sizeof(SortPlan));
+    s.ctr = gbt_align(s.hist + 8 * 256 * sizeof(uint32_t));
+    s.status = gbt_align(s.ctr + 8 * sizeof(uint32_t));
+    s.total = gbt_align(s.status + (size_t)8 * s.n_tiles * 256 * sizeof(uint32_t));
+    return s;
+}
+
+// One read of the keys builds the digit histograms of all eight passes.
+__global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ ghist) {
+    __shared__ uint32_t h[8 * 256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < 8; p++) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&ghist[i], h[i]);
+}
+
+// Exclusive scan of 256 values held one per thread (blockDim == 256).
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_tmp /*8*/, uint32_t *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[w] = x;
+    __syncthreads();
+    uint32_t off = 0, tot = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        uint32_t c = s_tmp[j];
+        off += (j < w) ? c : 0u;
+        tot += c;
+    }
+    __syncthreads();
+    if (total) *total = tot;
+    return off + x - v;
+}
+
+// Decide which passes are needed (a pass whose digit is equal for every key
+// leaves the order unchanged) and chain the ping-pong buffers through them.
+__global__ void __launch_bounds__(256) k_sort_plan(SortPlan *plan, const uint32_t *__restrict__ ghist, uint32_t n,
+                                                   uint64_t *kA, uint32_t *vA, uint64_t *kB, uint32_t *vB,
+                                                   int identity_vals, BvhHeader *hdr) {
+    __shared__ uint32_t s_tmp[8];
+    __shared__ uint32_t s_active[8];
+    const int t = threadIdx.x;
+    for (int p = 0; p < 8; p++) {
+        uint32_t c = ghist[p * 256 + t];
+        int full = __syncthreads_or(c == n);
+        plan->digit_base[p][t] = block_excl_scan256(c, s_tmp, nullptr);
+        if (t == 0) s_active[p] = full ? 0u : 1u;
+    }
+    __syncthreads();
+    if (t == 0) {
+        int any = 0;
+        for (int p = 0; p < 8; p++) any |= s_active[p];
+        if (!any) s_active[0] = 1;  // one pass still has to move the pairs (and write the values)
+        uint64_t *ck = kA;
+        uint32_t *cv = vA;
+        int first = 1;
+        for (int p = 0; p < 8; p++) {
+            plan->active[p] = s_active[p];
+            plan->identity[p] = 0;
+            if (!s_active[p]) continue;
+            uint64_t *ok = (ck == kA) ? kB : kA;
+            uint32_t *ov = (cv == vA) ? vB : vA;
+            plan->in_k[p] = ck;
+            plan->in_v[p] = cv;
+            plan->out_k[p] = ok;
+            plan->out_v[p] = ov;
+            plan->identity[p] = (first && identity_vals) ? 1u : 0u;
+            first = 0;
+            ck = ok;
+            cv = ov;
+        }
+        plan->final_k = ck;
+        plan->final_v = cv;
+        plan->final_sel = (ck == kA) ? 0u : 1u;
+        if (hdr) hdr->sorted_sel = plan->final_sel;
+    }
+}
+
+__device__ __forceinline__ uint32_t lookback_wait(const uint32_t *p, unsigned int *err) {
+    for (uint32_t it = 0;; ++it) {
+        uint32_t s = ld_relaxed(p);
+        if (s & ST_FLAGS) return s;
+        if (it >= GBT_SPIN_LIMIT) {
+            atomicOr(err, GBT_DEVERR_SPIN);
+            return ST_PREFIX;  // give up: the result is wrong but the kernel ends; the host sees the flag
+        }
+        if (it > 64) __nanosleep(64);
+    }
+}
+
+// One pass: rank each key within its warp by digit (match_any + ballot
+// counts into warp-private shared histograms), publish the tile's digit
+// counts, look back over earlier tiles for the global offsets, stage the tile
+// in shared memory in digit order and write it out in runs.
+__global__ void __launch_bounds__(SORT_THREADS, 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
+                                                              uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
+                                                              unsigned int *err) {
+    if (!plan->active[pass]) return;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *s_wh = reinterpret_cast<uint32_t *>(smem);  // [8][256]
+    uint32_t *s_tstart = s_wh + 8 * 256;                    // [256]
+    uint32_t *s_gbase = s_tstart + 256;                      // [256]
+    uint32_t *s_misc = s_gbase + 256;                        // [32]
+    uint64_t *s_keys = reinterpret_cast<uint64_t *>(s_misc + 32);
+    uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + SORT_TILE);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_misc[16] = atomicAdd(&tile_ctr[pass], 1u);
+    for (int i = tid; i < 8 * 256; i += SORT_THREADS) s_wh[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_misc[16];
+    const uint32_t shift = 8u * pass;
+    const uint64_t *__restrict__ kin = plan->in_k[pass];
+    const uint32_t *__restrict__ vin = plan->in_v[pass];
+    const bool ident = plan->identity[pass] != 0;
+    const uint32_t wbase = tile * SORT_TILE + warp * 32 * SORT_ITEMS;
+
+    uint64_t k[SORT_ITEMS];
+    uint32_t v[SORT_ITEMS];
+    uint32_t rk[SORT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; i++) {
+        uint32_t idx = wbase + i * 32 + lane;
+        bool ok = idx < n;
+        k[i] = ok ? __ldcs(kin + idx) : 0ull;
+        v[i] = ident ? idx : (ok ? __ldcs(vin + idx) : 0u);
+    }
+    uint32_t *wh = s_wh + warp * 256;
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; i++) {
+        uint32_t idx = wbase + i * 32 + lane;
+        bool ok = idx < n;
+        uint32_t d = ok ? (uint32_t)((k[i] >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t base = ok ? wh[d] : 0u;
+        __syncwarp();
+        if (ok && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = base + __popc(peers);
+        __syncwarp();
+        rk[i] = base + __popc(peers & lt);
+    }
+    __syncthreads();
+
+    {
+        const uint32_t t = tid;  // one thread per digit
+        uint32_t sum = 0;
+#pragma unroll
+        for (int w = 0; w < 8; w++) {
+            uint32_t c = s_wh[w * 256 + t];
+            s_wh[w * 256 + t] = sum;
+            sum += c;
+        }
+        uint32_t *st = status + (size_t)tile * 256;
+        st_relaxed(&st[t], (tile == 0 ? ST_PREFIX : ST_AGG) | sum);
+        s_tstart[t] = block_excl_scan256(sum, s_misc, nullptr);
+        uint32_t prefix = 0;
+        if (tile > 0) {
+            for (int j = (int)tile - 1; j >= 0; --j) {
+                uint32_t s = lookback_wait(&status[(size_t)j * 256 + t], err);
+                prefix += s & ST_VALUE;
+                if ((s & ST_FLAGS) == ST_PREFIX) break;
+            }
+            st_relaxed(&st[t], ST_PREFIX | (prefix + sum));
+        }
+        s_gbase[t] = plan->digit_base[pass][t] + prefix;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; i++) {
+        uint32_t idx = wbase + i * 32 + lane;
+        if (idx < n) {
+            uint32_t d = (uint32_t)((k[i] >> shift) & 255u);
+            uint32_t pos = s_tstart[d] + wh[d] + rk[i];
+            s_keys[pos] = k[i];
+            s_vals[pos] = v[i];
+        }
+    }
+    __syncthreads();
+    uint64_t *__restrict__ kout = plan->out_k[pass];
+    uint32_t *__restrict__ vout = plan->out_v[pass];
+    const uint32_t tile0 = tile * SORT_TILE;
+    const uint32_t valid = (n - tile0) < (uint32_t)SORT_TILE ? (n - tile0) : (uint32_t)SORT_TILE;
+    for (uint32_t j = tid; j < valid; j += SORT_THREADS) {
+        uint64_t kk = s_keys[j];
+        uint32_t d = (uint32_t)((kk >> shift) & 255u);
+        uint32_t g = s_gbase[d] + (j - s_tstart[d]);
+        kout[g] = kk;
+        vout[g] = s_vals[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// runs of equal codes
+// ---------------------------------------------------------------------------
+constexpr int RLE_THREADS = 256, RLE_ITEMS = 16, RLE_TILE = RLE_THREADS * RLE_ITEMS;
+
+__device__ __forceinline__ bool run_start_at(const uint64_t *__restrict__ k, uint32_t i, uint32_t n) {
+    return i < n && (i == 0 || k[i] != k[i - 1]);
+}
+
+__global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__restrict__ plan, uint32_t n,
+                                                           uint32_t *__restrict__ tile_cnt) {
+    const uint64_t *k = plan->final_k;
+    uint32_t base = blockIdx.x * RLE_TILE, c = 0;
+#pragma unroll
+    for (int i = 0; i < RLE_ITEMS; i++) c += run_start_at(k, base + i * RLE_THREADS + threadIdx.x, n);
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ uint32_t s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int j = 0; j < 8; j++) t += s[j];
+        tile_cnt[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t n_tiles, BvhHeader *hdr) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t b = 0; b < n_tiles; b += 1024) {
+        uint32_t i = b + threadIdx.x;
+        uint32_t v = i < n_tiles ? tile_cnt[i] : 0u, x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[w] = x;
+        __syncthreads();
+        uint32_t off = s_carry, tot = 0;
+        for (int j = 0; j < 32; j++) {
+            off += (j < w) ? s_w[j] : 0u;
+            tot += s_w[j];
+        }
+        if (i < n_tiles) tile_cnt[i] = off + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        hdr->n_unique = s_carry;
+        hdr->n_nodes = s_carry > 0 ? s_carry - 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(RLE_THREADS) k_rle_write(const SortPlan *__restrict__ plan, uint32_t n,
+                                                           const uint32_t *__restrict__ tile_off,
+                                                           uint32_t *__restrict__ run, uint64_t *__restrict__ ukey) {
+    const uint64_t *k = plan->final_k;
+    __shared__ uint32_t s_w[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    uint32_t base = blockIdx.x * RLE_TILE, carry = tile_off[blockIdx.x];
+    for (int i = 0; i < RLE_ITEMS; i++) {
+        uint32_t idx = base + i * RLE_THREADS + threadIdx.x;
+        bool f = run_start_at(k, idx, n);
+        uint32_t b = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_w[w] = __popc(b);
+        __syncthreads();
+        uint32_t off = carry, tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            off += (j < w) ? s_w[j] : 0u;
+            tot += s_w[j];
+        }
+        if (f) {
+            uint32_t u = off + __popc(b & lt);
+            run[u] = idx;
+            ukey[u] = k[idx];
+        }
+        if (idx == n - 1) run[off + __popc(b & lt) + (f ? 1u : 0u)] = n;
+        carry += tot;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// primitive records in sorted order: r0 = (v0, id), r1 = (v1 | centre r, kind), r2 = v2
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gather(const SortPlan *__restrict__ plan, const float *__restrict__ verts,
+                                                const float4 *__restrict__ sph, uint32_t n_tri, uint32_t n,
+                                                float4 *__restrict__ recs) {
+    const uint32_t *idx = plan->final_v;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        uint32_t o = idx[s];
+        float4 r0, r1, r2;
+        if (o < n_tri) {
+            const float *t = verts + (size_t)o * 9;
+            r0 = make_float4(t[0], t[1], t[2], __int_as_float((int)o));
+            r1 = make_float4(t[3], t[4], t[5], __int_as_float(0));
+            r2 = make_float4(t[6], t[7], t[8], 0.f);
+        } else {
+            float4 c = sph[o - n_tri];
+            r0 = make_float4(c.x, c.y, c.z, __int_as_float((int)o));
+            r1 = make_float4(c.w, 0.f, 0.f, __int_as_float(1));
+            r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        recs[3 * (size_t)s + 0] = r0;
+        recs[3 * (size_t)s + 1] = r1;
+        recs[3 * (size_t)s + 2] = r2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// hierarchy emission + refit
+// ---------------------------------------------------------------------------
+// Box of one stored primitive record, in float32.  Triangle boxes are exact;
+// a sphere box (float64 centre -/+ radius in the reference) is rounded outward.
+__device__ __forceinline__ void record_box(const float4 *__restrict__ recs, uint32_t s, float3 &lo, float3 &hi) {
+    float4 r0 = recs[3 * (size_t)s], r1 = recs[3 * (size_t)s + 1];
+    if (__float_as_int(r1.w) == 0) {
+        float4 r2 = recs[3 * (size_t)s + 2];
+        lo = make_float3(fminf(fminf(r0.x, r1.x), r2.x), fminf(fminf(r0.y, r1.y), r2.y), fminf(fminf(r0.z, r1.z), r2.z));
+        hi = make_float3(fmaxf(fmaxf(r0.x, r1.x), r2.x), fmaxf(fmaxf(r0.y, r1.y), r2.y), fmaxf(fmaxf(r0.z, r1.z), r2.z));
+    } else {
+        double r = r1.x;
+        lo = make_float3(__double2float_rd((double)r0.x - r), __double2float_rd((double)r0.y - r),
+                         __double2float_rd((double)r0.z - r));
+        hi = make_float3(__double2float_ru((double)r0.x + r), __double2float_ru((double)r0.y + r),
+                         __double2float_ru((double)r0.z + r));
+    }
+}
+
+__device__ __forceinline__ int prefix_len(const uint64_t *__restrict__ ukey, uint32_t i, uint32_t j) {
+    return __clzll((long long)(ukey[i] ^ ukey[j]));
+}
+
+// One thread per leaf walks up the binary radix tree.  A node covering the
+// distinct-code range [l, r] is the left child of the split r|r+1 or the right
+// child of the split l-1|l, whichever boundary shares the longer common prefix
+// (the reference splits a range at the highest differing bit, lbvh.go:147-176,
+// so that boundary is its parent's split).  Inner node k is the split k|k+1.
+// The second child to arrive at a node folds both boxes and carries on.
+__global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
+                                              const uint32_t *__restrict__ run, const uint64_t *__restrict__ ukey,
+                                              const float4 *__restrict__ recs, float4 *nodes, int32_t *other,
+                                              uint32_t *subtree, int32_t *parent_of, uint32_t n) {
+    const uint32_t U = hdr_in->n_unique;
+    uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= U || u >= n) return;
+    uint32_t first = run[u], last = run[u + 1];
+    float3 lo, hi;
+    record_box(recs, first, lo, hi);
+    for (uint32_t s = first + 1; s < last; s++) {
+        float3 a, b;
+        record_box(recs, s, a, b);
+        lo = make_float3(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z));
+        hi = make_float3(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z));
+    }
+    int32_t ref = (int32_t)first, cnt = (int32_t)(last - first);
+    uint32_t size = 1;
+    uint32_t l = u, r = u;
+    for (;;) {
+        if (l == 0 && r == U - 1) {
+            hdr->root_ref = ref;
+            hdr->root_cnt = cnt;
+            hdr->root_lo[0] = lo.x; hdr->root_lo[1] = lo.y; hdr->root_lo[2] = lo.z; hdr->root_lo[3] = 0.f;
+            hdr->root_hi[0] = hi.x; hdr->root_hi[1] = hi.y; hdr->root_hi[2] = hi.z; hdr->root_hi[3] = 0.f;
+            if (cnt == 0) parent_of[ref] = -1;
+            return;
+        }
+        bool left = (l == 0) || (r != U - 1 && prefix_len(ukey, r, r + 1) > prefix_len(ukey, l - 1, l));
+        uint32_t p = left ? r : l - 1;
+        int slot = left ? 0 : 1;
+        float4 *nd = nodes + 4 * (size_t)p;
+        nd[slot] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        reinterpret_cast<float2 *>(nd + 2)[slot] = make_float2(lo.z, hi.z);
+        reinterpret_cast<int2 *>(nd + 3)[slot] = make_int2(ref, cnt);
+        if (cnt == 0) parent_of[ref] = (int32_t)p;
+        __threadfence();
+        int32_t o = atomicExch(&other[p], (int32_t)(left ? l : r));
+        if (o < 0) return;  // first child here: the sibling finishes the node
+        __threadfence();
+        float4 sb = __ldcg(nd + (slot ^ 1));
+        float2 sz = __ldcg(reinterpret_cast<const float2 *>(nd + 2) + (slot ^ 1));
+        int2 sr = __ldcg(reinterpret_cast<const int2 *>(nd + 3) + (slot ^ 1));
+        lo = make_float3(fminf(lo.x, sb.x), fminf(lo.y, sb.z), fminf(lo.z, sz.x));
+        hi = make_float3(fmaxf(hi.x, sb.y), fmaxf(hi.y, sb.w), fmaxf(hi.z, sz.y));
+        uint32_t sib = sr.y > 0 ? 1u : __ldcg(subtree + sr.x);
+        size = 1 + size + sib;
+        subtree[p] = size;
+        if (left) r = (uint32_t)o;
+        else l = (uint32_t)o;
+        ref = (int32_t)p;
+        cnt = 0;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t lbvh_scratch_layout(uint32_t n, size_t *acc_off, SortScratch *ss, size_t *rle_off) {
+    *acc_off = 0;
+    *ss = sort_layout(n, gbt_align(6 * sizeof(unsigned long long)));
+    *rle_off = ss->total;
+    uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
+    return gbt_align(*rle_off + (size_t)(rt + 1) * sizeof(uint32_t));
+}
+
+size_t gbt_lbvh_scratch_bytes(uint32_t n) {
+    size_t a, r;
+    SortScratch s;
+    return lbvh_scratch_layout(n, &a, &s, &r);
+}
+
+static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &ss, uint64_t *kA, uint32_t *vA,
+                        uint64_t *kB, uint32_t *vB, uint32_t n, int identity_vals, BvhHeader *hdr) {
+    cudaStream_t st = ctx->stream;
+    SortPlan *plan = reinterpret_cast<SortPlan *>(sbase + ss.plan);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(sbase + ss.hist);
+    uint32_t *ctr = reinterpret_cast<uint32_t *>(sbase + ss.ctr);
+    uint32_t *status = reinterpret_cast<uint32_t *>(sbase + ss.status);
+    GBT_CUDA(ctx, cudaMemsetAsync(sbase + ss.hist, 0, ss.total - ss.hist, st));
+    int hb = ctx->num_sms * 2;
+    k_hist<<<hb, 256, 0, st>>>(kA, n, hist);
+    k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
+    size_t smem = (8 * 256 + 256 + 256 + 32) * sizeof(uint32_t) + (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+    GBT_CUDA(ctx, cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (int p = 0; p < 8; p++)
+        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr,
+                                                            ctx->d_error);
+    GBT_CUDA(ctx, cudaGetLastError());
+    return GBT_OK;
+}
+
+int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
+    gbt_scene *sc = bvh->scene;
+    const uint32_t n_tri = sc->n_tri, n = sc->n_tri + sc->n_sph;
+    if (n == 0) return gbt_fail(ctx, GBT_EINVAL, "empty scene");
+    if (n >= (1u << 30)) return gbt_fail(ctx, GBT_EINVAL, "scene larger than 2^30 primitives");
+    size_t acc_off, rle_off;
+    SortScratch ss;
+    size_t need = lbvh_scratch_layout(n, &acc_off, &ss, &rle_off);
+    void *scr = nullptr;
+    int rc = gbt_scratch(ctx, need, &scr);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(scr);
+    cudaStream_t st = ctx->stream;
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(sb + acc_off);
+    GBT_CUDA(ctx, cudaMemsetAsync(acc, 0xff, 3 * sizeof(unsigned long long), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(acc + 3, 0x00, 3 * sizeof(unsigned long long), st));
+    int grid = ctx->num_sms * 8;
+    int g2 = (int)((n + 255) / 256);
+    if (g2 < grid) grid = g2;
+    k_bounds<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc);
+    k_morton<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes);
+    rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr);
+    if (rc) return rc;
+    const SortPlan *plan = reinterpret_cast<const SortPlan *>(sb + ss.plan);
+    uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
+    uint32_t *tcnt = reinterpret_cast<uint32_t *>(sb + rle_off);
+    k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt);
+    k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr);
+    k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey);
+    k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims);
+    GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
+    k_emit<<<(n + 255) / 256, 256, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
+                                            bvh->d_other, bvh->d_size, bvh->d_parent, n);
+    GBT_CUDA(ctx, cudaGetLastError());
+    return GBT_OK;
+}

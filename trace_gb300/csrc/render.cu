@@ -1,0 +1,316 @@
+// Wavefront path tracer: pkg/pt/render.go:91-129 (ImageRenderer.RenderToBuffer)
+// with DefaultClosestHitShader (render.go:209-224), Diffuse/Light materials
+// (material.go:13-42) and the miss shaders (render.go:228-246).
+//
+// A wave is a range of path indices g in [0, W*H*spp); path g samples pixel
+// g % (W*H).  Per bounce level b the kernels are
+//   k_raygen (b = 0)   camera rays                          camera.go:95-97, render.go:201-205
+//   traversal          closest hit of every live ray        traverse.cu
+//   k_shade            miss / emission / Lambertian scatter render.go:209-224
+//                      and compaction of the live paths into the next level
+// and k_resolve divides the accumulated radiance by spp.  The recursion of the
+// reference, L = Le + albedo * L(next), becomes a throughput T carried along
+// the path: L += T * Le, T *= albedo.  A surface at depth > MaxDepth returns
+// black (render.go:210-212); a ray that misses returns the miss colour.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "gbt_internal.cuh"
+#include "traverse.cuh"
+
+using namespace gbt_dev;
+
+namespace {
+
+struct CamF {
+    float3 origin, llc, hor, ver;
+};
+
+struct ShadeParams {
+    uint32_t npix, width, height, spp;
+    int32_t max_depth;
+    int32_t miss_mode;
+    float3 miss_color;
+    uint32_t seed_lo, seed_hi;
+    uint32_t n_tri;
+};
+
+// Philox-2x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2,
+// 3", SC'11): counter (path, stream) and key from the seed.
+__device__ __forceinline__ uint2 philox2x32(uint32_t c0, uint32_t c1, uint32_t key) {
+#pragma unroll
+    for (int i = 0; i < 10; i++) {
+        uint32_t hi = __umulhi(0xD256D193u, c0);
+        uint32_t lo = 0xD256D193u * c0;
+        c0 = hi ^ key ^ c1;
+        c1 = lo;
+        key += 0x9E3779B9u;
+    }
+    return make_uint2(c0, c1);
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+__global__ void __launch_bounds__(256) k_raygen(CamF cam, ShadeParams sp, uint32_t g0, uint32_t count,
+                                                float4 *__restrict__ rays, float4 *__restrict__ aux, uint32_t *counts) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) counts[0] = count;
+    if (i >= count) return;
+    uint32_t g = g0 + i;
+    uint32_t pix = g % sp.npix;
+    uint32_t x = pix % sp.width, y = pix / sp.width;
+    uint2 rnd = philox2x32(g, 0xFFFFu, sp.seed_lo ^ sp.seed_hi);
+    float s = ((float)x + u01(rnd.x)) / (float)(sp.width - 1);   // RandomSampling: /(w-1)
+    float t = ((float)y + u01(rnd.y)) / (float)(sp.height - 1);
+    float3 d = sub3(add3(add3(cam.llc, mul3(cam.hor, s)), mul3(cam.ver, t)), cam.origin);
+    rays[2 * (size_t)i] = make_float4(cam.origin.x, cam.origin.y, cam.origin.z, 0.001f);
+    rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    aux[2 * (size_t)i] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)g));
+    aux[2 * (size_t)i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__device__ __forceinline__ float3 miss_colour(const ShadeParams &sp, float3 d) {
+    switch (sp.miss_mode) {
+    case GBT_MISS_WHITE: return f3(1.f, 1.f, 1.f);
+    case GBT_MISS_SKY: {
+        float inv = rsqrtf(dot3(d, d));
+        float t = 0.5f * (d.y * inv + 1.f);
+        return f3(0.8f * (1.f - t) + 0.25f * t, 0.8f * (1.f - t) + 0.35f * t, 0.8f * (1.f - t) + 0.5f * t);
+    }
+    case GBT_MISS_CONSTANT: return sp.miss_color;
+    default: return f3(0.f, 0.f, 0.f);
+    }
+}
+
+__device__ __forceinline__ void deposit(float *__restrict__ acc, uint32_t pix, float3 L) {
+    if (L.x != 0.f) atomicAdd(acc + 3 * (size_t)pix, L.x);
+    if (L.y != 0.f) atomicAdd(acc + 3 * (size_t)pix + 1, L.y);
+    if (L.z != 0.f) atomicAdd(acc + 3 * (size_t)pix + 2, L.z);
+}
+
+__global__ void __launch_bounds__(256) k_shade(ShadeParams sp, int level, const float4 *__restrict__ rays_in,
+                                               const float4 *__restrict__ aux_in, const float4 *__restrict__ hits,
+                                               const uint32_t *__restrict__ count_in, float4 *__restrict__ rays_out,
+                                               float4 *__restrict__ aux_out, uint32_t *count_out,
+                                               const float4 *__restrict__ recs, const uint32_t *__restrict__ prim_mat,
+                                               const float4 *__restrict__ mats, const float *__restrict__ normals,
+                                               float *__restrict__ acc, uint32_t cap) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n = *count_in;
+    bool alive = false;
+    float4 out_r0, out_r1, out_a0, out_a1;
+    if (i < n) {
+        float4 a0 = aux_in[2 * (size_t)i], a1 = aux_in[2 * (size_t)i + 1];
+        float3 T = f3(a0.x, a0.y, a0.z), L = f3(a1.x, a1.y, a1.z);
+        uint32_t g = (uint32_t)__float_as_int(a0.w);
+        uint32_t pix = g % sp.npix;
+        float4 h = hits[i];
+        int rec = __float_as_int(h.w);
+        float4 ro = rays_in[2 * (size_t)i], rd = rays_in[2 * (size_t)i + 1];
+        float3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
+        if (rec < 0) {
+            L = add3(L, emul3(T, miss_colour(sp, d)));
+            deposit(acc, pix, L);
+        } else if (level > sp.max_depth) {
+            deposit(acc, pix, L);  // render.go:210-212: beyond MaxDepth the surface returns black
+        } else {
+            const float4 *pr = recs + 3 * (size_t)rec;
+            float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+            uint32_t id = (uint32_t)__float_as_int(r0.w);
+            float4 m = __ldg(mats + __ldg(prim_mat + id));
+            float3 col = f3(m.x, m.y, m.z);
+            if (__float_as_int(m.w) == GBT_MAT_LIGHT) {
+                L = add3(L, emul3(T, col));
+                deposit(acc, pix, L);
+            } else {
+                float3 p = add3(o, mul3(d, h.x));  // ray.position(t)
+                float3 nrm;
+                if (__float_as_int(r1.w) == 0) {
+                    float4 r2 = __ldg(pr + 2);
+                    float3 e1 = f3(r1.x - r0.x, r1.y - r0.y, r1.z - r0.z), e2 = f3(r2.x - r0.x, r2.y - r0.y, r2.z - r0.z);
+                    float3 ng = cross3(e1, e2);
+                    bool front = dot3(d, ng) < 0.f;  // det > 0 (primitive.go:201)
+                    if (normals) {                   // interpolated vertex normals (primitive.go:144-150)
+                        const float *nv = normals + 9 * (size_t)id;
+                        float w = 1.f - h.y - h.z;
+                        nrm = f3(nv[3] * h.y + nv[6] * h.z + nv[0] * w, nv[4] * h.y + nv[7] * h.z + nv[1] * w,
+                                 nv[5] * h.y + nv[8] * h.z + nv[2] * w);
+                    } else {
+                        nrm = mul3(ng, rsqrtf(dot3(ng, ng)));
+                    }
+                    if (!front) nrm = mul3(nrm, -1.f);
+                } else {
+                    nrm = mul3(sub3(p, f3(r0.x, r0.y, r0.z)), 1.f / r1.x);
+                    if (!(dot3(d, nrm) < 0.f)) nrm = mul3(nrm, -1.f);
+                }
+                // Diffuse.scatter: normal + RandomUnitVector (uniform on the sphere)
+                uint2 rnd = philox2x32(g, (uint32_t)level, sp.seed_lo ^ sp.seed_hi);
+                float z = 1.f - 2.f * u01(rnd.x);
+                float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+                float sphi, cphi;
+                sincospif(2.f * u01(rnd.y), &sphi, &cphi);
+                float3 sd = f3(nrm.x + rr * cphi, nrm.y + rr * sphi, nrm.z + z);
+                if (fabsf(sd.x) <= 1e-7f && fabsf(sd.y) <= 1e-7f && fabsf(sd.z) <= 1e-7f) sd = nrm;
+                T = emul3(T, col);
+                alive = true;
+                out_r0 = make_float4(p.x, p.y, p.z, 0.0001f);
+                out_r1 = make_float4(sd.x, sd.y, sd.z, __int_as_float(0x7f800000));
+                out_a0 = make_float4(T.x, T.y, T.z, a0.w);
+                out_a1 = make_float4(L.x, L.y, L.z, 0.f);
+            }
+        }
+    }
+    // compaction: one atomic per warp
+    uint32_t ball = __ballot_sync(0xffffffffu, alive);
+    if (ball == 0) return;
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == (uint32_t)(__ffs(ball) - 1)) base = atomicAdd(count_out, (uint32_t)__popc(ball));
+    base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
+    if (alive) {
+        uint32_t lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        uint32_t slot = base + __popc(ball & lt);
+        if (slot < cap) {
+            rays_out[2 * (size_t)slot] = out_r0;
+            rays_out[2 * (size_t)slot + 1] = out_r1;
+            aux_out[2 * (size_t)slot] = out_a0;
+            aux_out[2 * (size_t)slot + 1] = out_a1;
+        }
+    }
+}
+
+__global__ void k_resolve(const float *__restrict__ acc, float *__restrict__ out, uint32_t n, float inv_spp) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = acc[i] * inv_spp;
+}
+
+__global__ void k_sum_counts(const uint32_t *counts, int levels, unsigned long long *total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int i = 0; i < levels; i++) s += counts[i];
+        *total += s;
+    }
+}
+
+CamF make_cam(const gbt_camera *c) {
+    // camera.go:53-66 in float64, then rounded
+    auto sub = [](const double *a, const double *b, double *o) { for (int k = 0; k < 3; k++) o[k] = a[k] - b[k]; };
+    auto unit = [](double *v) { double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); for (int k = 0; k < 3; k++) v[k] /= l; };
+    auto cross = [](const double *a, const double *b, double *o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    double vh = 2.0 * std::tan((c->fov_deg * (M_PI / 180)) / 2), vw = c->aspect * vh;
+    double w[3], u[3], v[3];
+    sub(c->look_from, c->look_at, w);
+    unit(w);
+    cross(c->up, w, u);
+    unit(u);
+    cross(w, u, v);
+    double hor[3], ver[3], llc[3];
+    for (int k = 0; k < 3; k++) {
+        hor[k] = u[k] * vw;
+        ver[k] = v[k] * vh;
+        llc[k] = c->look_from[k] - hor[k] * 0.5 - ver[k] * 0.5 - w[k];
+    }
+    CamF f;
+    f.origin = make_float3((float)c->look_from[0], (float)c->look_from[1], (float)c->look_from[2]);
+    f.llc = make_float3((float)llc[0], (float)llc[1], (float)llc[2]);
+    f.hor = make_float3((float)hor[0], (float)hor[1], (float)hor[2]);
+    f.ver = make_float3((float)ver[0], (float)ver[1], (float)ver[2]);
+    return f;
+}
+
+}  // namespace
+
+// Per-context render state: ping-pong path buffers, hits, counters, accumulator.
+struct RenderState {
+    size_t cap;           // paths per wave
+    float4 *rays[2], *aux[2];
+    float4 *hits;
+    uint32_t *counts;     // per level
+    unsigned long long *total;
+    float *acc;
+};
+
+static size_t render_layout(size_t cap, size_t npix, size_t *off) {
+    size_t o = 0;
+    off[0] = o; o = gbt_align(o + cap * 32);  // rays[0]
+    off[1] = o; o = gbt_align(o + cap * 32);  // rays[1]
+    off[2] = o; o = gbt_align(o + cap * 32);  // aux[0]
+    off[3] = o; o = gbt_align(o + cap * 32);  // aux[1]
+    off[4] = o; o = gbt_align(o + cap * 16);  // hits
+    off[5] = o; o = gbt_align(o + 64 * sizeof(uint32_t));
+    off[6] = o; o = gbt_align(o + sizeof(unsigned long long));
+    off[7] = o; o = gbt_align(o + npix * 3 * sizeof(float));
+    return o;
+}
+
+int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p, float *d_rgb) {
+    if (p->width < 2 || p->height < 2 || p->spp < 1 || p->max_depth < 0 || p->max_depth > 60)
+        return gbt_fail(ctx, GBT_EINVAL, "render: width/height >= 2, spp >= 1, 0 <= max_depth <= 60");
+    const size_t npix = (size_t)p->width * p->height;
+    const size_t total = npix * (size_t)p->spp;
+    if (total >= (1ull << 32)) return gbt_fail(ctx, GBT_EINVAL, "render: width*height*spp must be < 2^32");
+    size_t cap = total < (size_t)(1u << 23) ? total : (size_t)(1u << 23);
+    size_t off[8];
+    size_t need = render_layout(cap, npix, off);
+    if (ctx->rstate_bytes < need) {
+        if (ctx->rstate) cudaFree(ctx->rstate);
+        ctx->rstate = nullptr;
+        ctx->rstate_bytes = 0;
+        if (cudaMalloc(&ctx->rstate, need) != cudaSuccess) return gbt_fail(ctx, GBT_ENOMEM, "render: state allocation");
+        ctx->rstate_bytes = need;
+    }
+    unsigned char *b = static_cast<unsigned char *>(ctx->rstate);
+    RenderState rs;
+    rs.cap = cap;
+    rs.rays[0] = reinterpret_cast<float4 *>(b + off[0]);
+    rs.rays[1] = reinterpret_cast<float4 *>(b + off[1]);
+    rs.aux[0] = reinterpret_cast<float4 *>(b + off[2]);
+    rs.aux[1] = reinterpret_cast<float4 *>(b + off[3]);
+    rs.hits = reinterpret_cast<float4 *>(b + off[4]);
+    rs.counts = reinterpret_cast<uint32_t *>(b + off[5]);
+    rs.total = reinterpret_cast<unsigned long long *>(b + off[6]);
+    rs.acc = reinterpret_cast<float *>(b + off[7]);
+
+    cudaStream_t st = ctx->stream;
+    gbt_scene *sc = bvh->scene;
+    CamF cf = make_cam(cam);
+    ShadeParams sp;
+    sp.npix = (uint32_t)npix;
+    sp.width = (uint32_t)p->width;
+    sp.height = (uint32_t)p->height;
+    sp.spp = (uint32_t)p->spp;
+    sp.max_depth = p->max_depth;
+    sp.miss_mode = p->miss_mode;
+    sp.miss_color = make_float3(p->miss_color[0], p->miss_color[1], p->miss_color[2]);
+    sp.seed_lo = (uint32_t)p->seed;
+    sp.seed_hi = (uint32_t)(p->seed >> 32);
+    sp.n_tri = sc->n_tri;
+    const int levels = p->max_depth + 2;  // surfaces at depth 0..MaxDepth+1 are traced
+
+    GBT_CUDA(ctx, cudaMemsetAsync(rs.acc, 0, npix * 3 * sizeof(float), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(rs.total, 0, sizeof(unsigned long long), st));
+    for (size_t g0 = 0; g0 < total; g0 += cap) {
+        uint32_t count = (uint32_t)((total - g0) < cap ? (total - g0) : cap);
+        GBT_CUDA(ctx, cudaMemsetAsync(rs.counts, 0, 64 * sizeof(uint32_t), st));
+        uint32_t blocks = (count + 255) / 256;
+        k_raygen<<<blocks, 256, 0, st>>>(cf, sp, (uint32_t)g0, count, rs.rays[0], rs.aux[0], rs.counts);
+        for (int lv = 0; lv < levels; lv++) {
+            int a = lv & 1;
+            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st);
+            k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],
+                                            rs.aux[a ^ 1], rs.counts + lv + 1, bvh->d_prims, sc->d_prim_mat, sc->d_mats,
+                                            sc->d_normals, rs.acc, (uint32_t)cap);
+        }
+        k_sum_counts<<<1, 32, 0, st>>>(rs.counts, levels, rs.total);
+    }
+    k_resolve<<<(uint32_t)((npix * 3 + 255) / 256), 256, 0, st>>>(rs.acc, d_rgb, (uint32_t)(npix * 3), 1.0f / p->spp);
+    GBT_CUDA(ctx, cudaGetLastError());
+    ctx->last_stats.paths = total;
+    ctx->d_ray_total = rs.total;
+    return GBT_OK;
+}

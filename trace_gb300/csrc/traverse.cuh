@@ -1,0 +1,257 @@
+// Device-side ray/BVH queries shared by the trace and render kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbt_internal.cuh"
+
+namespace gbt_dev {
+
+struct Ray {
+    float3 o, d, inv, oi;
+    float tmin, tmax;
+};
+
+struct Hit {
+    float t, u, v;
+    int rec;  // primitive record index, -1 for a miss
+};
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 emul3(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Reciprocal direction for the slab test.  A zero component is replaced by a
+// tiny one of the same sign, so the slab test stays finite (the box test only
+// culls; the primitive tests use the exact direction).
+__device__ __forceinline__ void finish_ray(Ray &r) {
+    const float eps = 1e-20f;
+    float dx = fabsf(r.d.x) > eps ? r.d.x : copysignf(eps, r.d.x);
+    float dy = fabsf(r.d.y) > eps ? r.d.y : copysignf(eps, r.d.y);
+    float dz = fabsf(r.d.z) > eps ? r.d.z : copysignf(eps, r.d.z);
+    r.inv = f3(1.0f / dx, 1.0f / dy, 1.0f / dz);
+    r.oi = f3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
+}
+
+__device__ __forceinline__ Ray load_ray(const float4 *__restrict__ rays, uint32_t i) {
+    float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+    Ray r;
+    r.o = f3(a.x, a.y, a.z);
+    r.tmin = a.w;
+    r.d = f3(b.x, b.y, b.z);
+    r.tmax = b.w;
+    finish_ray(r);
+    return r;
+}
+
+// Slab test against [tmin, tmax]; returns the entry distance.  The far
+// distance is widened by a few ulp so that a primitive lying on the box
+// boundary is never culled by float32 rounding.
+__device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy, float hz, const Ray &r,
+                                     float tmax, float &tenter) {
+    float tx0 = fmaf(lx, r.inv.x, -r.oi.x), tx1 = fmaf(hx, r.inv.x, -r.oi.x);
+    float ty0 = fmaf(ly, r.inv.y, -r.oi.y), ty1 = fmaf(hy, r.inv.y, -r.oi.y);
+    float tz0 = fmaf(lz, r.inv.z, -r.oi.z), tz1 = fmaf(hz, r.inv.z, -r.oi.z);
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), r.tmin));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    tenter = tn;
+    return tn <= tf * 1.0000005f;
+}
+
+// Moeller-Trumbore (primitive.go:172-208) on record s; narrows h on a hit.
+__device__ __forceinline__ void test_record(const float4 *__restrict__ recs, int s, const Ray &r, Hit &h) {
+    const float4 *p = recs + 3 * (size_t)s;
+    float4 r0 = __ldg(p), r1 = __ldg(p + 1);
+    if (__float_as_int(r1.w) == 0) {
+        float4 r2 = __ldg(p + 2);
+        float3 v0 = f3(r0.x, r0.y, r0.z);
+        float3 e1 = f3(r1.x - r0.x, r1.y - r0.y, r1.z - r0.z);
+        float3 e2 = f3(r2.x - r0.x, r2.y - r0.y, r2.z - r0.z);
+        float3 pv = cross3(r.d, e2);
+        float det = dot3(e1, pv);
+        if (fabsf(det) <= 1e-7f) return;
+        float inv = 1.0f / det;
+        float3 tv = sub3(r.o, v0);
+        float u = dot3(tv, pv) * inv;
+        if (u < 0.f || u > 1.f) return;
+        float3 qv = cross3(tv, e1);
+        float v = dot3(r.d, qv) * inv;
+        if (v < 0.f || u + v > 1.f) return;
+        float t = dot3(e2, qv) * inv;
+        if (t < r.tmin || t > h.t) return;
+        h.t = t;
+        h.u = u;
+        h.v = v;
+        h.rec = s;
+    } else {  // Sphere.intersected (primitive.go:56-86)
+        float3 c = f3(r0.x, r0.y, r0.z);
+        float rad = r1.x;
+        float3 oc = sub3(r.o, c);
+        float dn = sqrtf(dot3(r.d, r.d));
+        float a = dn * dn;
+        float hb = dot3(oc, r.d);
+        float ocn = sqrtf(dot3(oc, oc));
+        float cc = ocn * ocn - rad * rad;
+        float disc = hb * hb - a * cc;
+        if (disc < 0.f) return;
+        float sq = sqrtf(disc);
+        float t = (-hb - sq) / a;
+        if (t <= r.tmin || t >= h.t) {
+            t = (-hb + sq) / a;
+            if (t <= r.tmin || t >= h.t) return;
+        }
+        h.t = t;
+        h.u = 0.f;
+        h.v = 0.f;
+        h.rec = s;
+    }
+}
+
+__device__ __forceinline__ void leaf(const float4 *__restrict__ recs, int first, int cnt, const Ray &r, Hit &h) {
+    for (int s = first; s < first + cnt; ++s) test_record(recs, s, r, h);
+}
+
+template <int STACK>
+__device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *__restrict__ nodes,
+                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err) {
+    Hit h;
+    h.t = r.tmax;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    float te;
+    if (!slab(hdr.root_lo[0], hdr.root_lo[1], hdr.root_lo[2], hdr.root_hi[0], hdr.root_hi[1], hdr.root_hi[2], r, h.t, te))
+        return h;
+    int2 stack[STACK];
+    float stack_t[STACK];
+    int sp = 0;
+    int2 cur = make_int2(hdr.root_ref, hdr.root_cnt);
+    for (;;) {
+        if (cur.y == 0) {
+            const float4 *nd = nodes + 4 * (size_t)cur.x;
+            float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+            int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+            float t0, t1;
+            bool h0 = n3.y >= 0 && slab(n0.x, n0.z, n2.x, n0.y, n0.w, n2.y, r, h.t, t0);
+            bool h1 = n3.w >= 0 && slab(n1.x, n1.z, n2.z, n1.y, n1.w, n2.w, r, h.t, t1);
+            if (h0 && h1) {
+                int2 a = make_int2(n3.x, n3.y), b = make_int2(n3.z, n3.w);
+                float tb = t1;
+                if (t1 < t0) {
+                    int2 tmp = a;
+                    a = b;
+                    b = tmp;
+                    tb = t0;
+                }
+                if (sp < STACK) {
+                    stack[sp] = b;
+                    stack_t[sp] = tb;
+                    ++sp;
+                } else {
+                    atomicOr(err, GBT_DEVERR_STACK);
+                }
+                cur = a;
+                continue;
+            }
+            if (h0) { cur = make_int2(n3.x, n3.y); continue; }
+            if (h1) { cur = make_int2(n3.z, n3.w); continue; }
+        } else if (cur.y > 0) {
+            leaf(recs, cur.x, cur.y, r, h);
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= h.t * 1.0000005f) {
+                cur = stack[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return h;
+}
+
+template <int STACK>
+__device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *__restrict__ nodes,
+                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err) {
+    Hit h;
+    h.t = r.tmax;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    float te;
+    if (!slab(hdr.root_lo[0], hdr.root_lo[1], hdr.root_lo[2], hdr.root_hi[0], hdr.root_hi[1], hdr.root_hi[2], r, h.t, te))
+        return h;
+    int2 stack[STACK];
+    float stack_t[STACK];
+    int sp = 0;
+    int2 cur = make_int2(hdr.root_ref, hdr.root_cnt);
+    for (;;) {
+        if (cur.y == 0) {
+            const float4 *nd = nodes + 8 * (size_t)cur.x;
+            float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+            float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+            int4 rf = __ldg(reinterpret_cast<const int4 *>(nd + 6));
+            int4 cn = __ldg(reinterpret_cast<const int4 *>(nd + 7));
+            float tc[4];
+            int2 ch[4];
+            int k = 0;
+            float t;
+            if (cn.x >= 0 && slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.x, cn.x); }
+            if (cn.y >= 0 && slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.y, cn.y); }
+            if (cn.z >= 0 && slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.z, cn.z); }
+            if (cn.w >= 0 && slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.w, cn.w); }
+            if (k > 0) {
+                // order by entry distance, far first onto the stack
+                for (int a = 1; a < k; ++a)
+                    for (int b = a; b > 0 && tc[b] > tc[b - 1]; --b) {
+                        float tt = tc[b]; tc[b] = tc[b - 1]; tc[b - 1] = tt;
+                        int2 cc = ch[b]; ch[b] = ch[b - 1]; ch[b - 1] = cc;
+                    }
+                for (int a = 0; a < k - 1; ++a) {
+                    if (sp < STACK) {
+                        stack[sp] = ch[a];
+                        stack_t[sp] = tc[a];
+                        ++sp;
+                    } else {
+                        atomicOr(err, GBT_DEVERR_STACK);
+                    }
+                }
+                cur = ch[k - 1];
+                continue;
+            }
+        } else if (cur.y > 0) {
+            leaf(recs, cur.x, cur.y, r, h);
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= h.t * 1.0000005f) {
+                cur = stack[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return h;
+}
+
+// out_mode 0: gbt_hit (primitive id, t, u, v); 1: (t, u, v, record) for the renderer
+__device__ __forceinline__ void store_hit(float4 *__restrict__ hits, uint32_t i, const Hit &h,
+                                          const float4 *__restrict__ recs, int out_mode) {
+    if (out_mode == 0) {
+        int id = h.rec >= 0 ? __float_as_int(__ldg(recs + 3 * (size_t)h.rec).w) : -1;
+        float t = h.rec >= 0 ? h.t : __int_as_float(0x7f800000);
+        hits[i] = make_float4(__int_as_float(id), t, h.u, h.v);
+    } else {
+        hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.rec));
+    }
+}
+
+}  // namespace gbt_dev

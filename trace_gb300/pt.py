@@ -1,0 +1,343 @@
+"""Host-side mirror of ChSchmidt99/trace pkg/pt over the C ABI (include/gbtrace.h).
+
+The names follow the Go package so a caller of the reference finds the same
+entry points:
+
+  Go (pkg/pt)                                   here
+  ------------------------------------------    -----------------------------------------
+  ParseFromPath (obj.go:10-17)                  ParseFromPath(path) -> Geometry
+  Scene.CompileLBVH (scene.go:27-30)            Scene.CompileLBVH(ctx) / DefaultLBVH(scene)
+  Scene.Compile / CompilePHR (scene.go:21-36)   Scene.Compile(ctx) / Scene.CompilePHR(ctx, a, d, bf)
+  NewPHRBuilder + BuildFromAuxilary (phr.go)    NewPHRBuilder(alpha, delta, bf).BuildFromAuxilary(aux)
+  BVH.Cost / BVH.Size (bvh.go:46-52)            BVH.Cost() / BVH.Size()
+  NewCamera (camera.go:53-59)                   NewCamera(aspect, fov, CameraTransformation)
+  ImageRenderer.RenderToBuffer (render.go:91)   ImageRenderer(...).RenderToBuffer(buffer)
+  NewPxlBuffer / NewFrameBuffer (buffer.go)     NewPxlBuffer(w, h) / NewFrameBuffer(w, h)
+
+Errors: the Go code panics; here every failing call raises GbtError with the
+library's message.  Everything runs on the GPU through libgbtrace.so; there
+is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import GbtError
+
+DIFFUSE, LIGHT = 0, 1
+MISS_BLACK, MISS_WHITE, MISS_SKY, MISS_CONSTANT = 0, 1, 2, 3
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """A CUDA stream plus grow-only device scratch on one GPU (gbt_ctx)."""
+
+    def __init__(self, device=0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.gbt_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise GbtError(rc, "gbt_ctx_create(device=%d) failed" % device)
+        self.h = h
+
+    def check(self, rc, what=""):
+        if rc != 0:
+            msg = self.L.gbt_last_error(self.h)
+            raise GbtError(rc, (what + ": " if what else "") + (msg.decode() if msg else ""))
+
+    @property
+    def stream(self):
+        return self.L.gbt_ctx_stream(self.h)
+
+    def sync(self):
+        self.check(self.L.gbt_ctx_sync(self.h), "sync")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gbt_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # raw device buffers for callers without a CUDA runtime of their own
+    def alloc(self, nbytes):
+        p = C.c_void_p()
+        self.check(self.L.gbt_device_alloc(self.h, nbytes, C.byref(p)), "device_alloc")
+        return p.value
+
+    def free(self, ptr):
+        self.check(self.L.gbt_device_free(self.h, C.c_void_p(ptr)), "device_free")
+
+    def h2d(self, dptr, arr):
+        arr = np.ascontiguousarray(arr)
+        self.check(self.L.gbt_copy_h2d_async(self.h, C.c_void_p(dptr), _p(arr), arr.nbytes), "h2d")
+
+    def d2h(self, arr, dptr):
+        self.check(self.L.gbt_copy_d2h_async(self.h, _p(arr), C.c_void_p(dptr), arr.nbytes), "d2h")
+
+
+class DeviceScene:
+    """Flattened primitives resident on the device (gbt_scene)."""
+
+    def __init__(self, ctx, verts, normals=None, spheres=None, prim_mat=None, mat_type=None, mat_color=None):
+        self.ctx = ctx
+        self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+        sph = np.zeros((0, 4), np.float32) if spheres is None else np.ascontiguousarray(spheres, np.float32).reshape(-1, 4)
+        self.spheres = sph
+        n = self.verts.shape[0] + sph.shape[0]
+        pm = np.zeros(n, np.uint32) if prim_mat is None else np.ascontiguousarray(prim_mat, np.uint32)
+        mt = np.array([DIFFUSE], np.int32) if mat_type is None else np.asarray(mat_type, np.int32)
+        mc = np.array([[0.5, 0.5, 0.5]]) if mat_color is None else np.asarray(mat_color, np.float64).reshape(-1, 3)
+        mats = (_lib.Material * len(mt))()
+        for i in range(len(mt)):
+            mats[i].type = int(mt[i])
+            mats[i].color[:] = [float(x) for x in mc[i]]
+        sarr = (_lib.Sphere * max(1, sph.shape[0]))()
+        for i in range(sph.shape[0]):
+            sarr[i].center[:] = [float(x) for x in sph[i, :3]]
+            sarr[i].radius = float(sph[i, 3])
+        h = C.c_void_p()
+        ctx.check(ctx.L.gbt_scene_upload(ctx.h, _p(self.verts), _p(self.normals), self.verts.shape[0],
+                                         C.cast(sarr, C.c_void_p), sph.shape[0], _p(pm), C.cast(mats, C.c_void_p),
+                                         len(mt), C.byref(h)), "scene_upload")
+        self.h = h
+        self.n_prim = n
+
+    @classmethod
+    def from_dict(cls, ctx, s):
+        return cls(ctx, s["verts"], s.get("normals"), s.get("spheres"), s.get("prim_mat"), s.get("mat_type"),
+                   s.get("mat_color"))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.gbt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BVH:
+    """A device BVH (gbt_bvh) with the queries of pkg/pt/bvh.go."""
+
+    def __init__(self, ctx, h, scene, kind):
+        self.ctx, self.h, self.scene, self.kind = ctx, h, scene, kind
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.gbt_bvh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def Cost(self):
+        c = C.c_double()
+        self.ctx.check(self.ctx.L.gbt_bvh_cost(self.ctx.h, self.h, C.byref(c)), "bvh_cost")
+        return c.value
+
+    def Size(self):
+        c = C.c_int64()
+        self.ctx.check(self.ctx.L.gbt_bvh_size(self.ctx.h, self.h, C.byref(c)), "bvh_size")
+        return c.value
+
+    def counts(self):
+        out = np.zeros(4, np.int64)
+        self.ctx.check(self.ctx.L.gbt_bvh_counts(self.ctx.h, self.h, _p(out)), "bvh_counts")
+        return out
+
+    def export(self):
+        n_nodes, _, n_refs, _ = self.counts()
+        kind = np.empty(n_nodes, np.int8)
+        count = np.empty(n_nodes, np.int32)
+        box = np.empty((n_nodes, 6), np.float64)
+        prims = np.empty(max(1, n_refs), np.int32)
+        self.ctx.check(self.ctx.L.gbt_bvh_export(self.ctx.h, self.h, _p(kind), _p(count), _p(box), _p(prims)), "export")
+        return kind, count, box, prims[:n_refs]
+
+    def sorted_pairs(self):
+        n = self.scene.n_prim
+        codes = np.empty(n, np.uint64)
+        idx = np.empty(n, np.int32)
+        self.ctx.check(self.ctx.L.gbt_lbvh_sorted(self.ctx.h, self.h, _p(codes), _p(idx)), "lbvh_sorted")
+        return codes, idx
+
+    def trace(self, rays):
+        """rays: (n, 8) float32 (origin, tmin, dir, tmax) -> (prim, t, u, v)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        hits = np.empty((n, 4), np.float32)
+        self.ctx.check(self.ctx.L.gbt_trace(self.ctx.h, self.h, _p(rays), n, _p(hits)), "trace")
+        return hits[:, 0].view(np.int32).copy(), hits[:, 1].copy(), hits[:, 2].copy(), hits[:, 3].copy()
+
+    def render(self, camera, width, height, spp, max_depth, miss_mode=MISS_BLACK, miss_color=(0, 0, 0), seed=1):
+        cam = camera if isinstance(camera, _lib.Camera) else make_camera(camera)
+        p = _lib.RenderParams(width, height, spp, max_depth, miss_mode, (C.c_float * 3)(*miss_color), seed)
+        img = np.empty((height, width, 3), np.float32)
+        st = _lib.RenderStats()
+        self.ctx.check(self.ctx.L.gbt_render(self.ctx.h, self.h, C.byref(cam), C.byref(p), _p(img), C.byref(st)),
+                       "render")
+        return img, dict(rays_traced=st.rays_traced, paths=st.paths, ms=st.ms_total)
+
+
+def make_camera(cam):
+    c = _lib.Camera()
+    c.look_from[:] = [float(x) for x in cam["look_from"]]
+    c.look_at[:] = [float(x) for x in cam["look_at"]]
+    c.up[:] = [float(x) for x in cam["up"]]
+    c.aspect = float(cam["aspect"])
+    c.fov_deg = float(cam["fov"])
+    return c
+
+
+# ---------------------------------------------------------------------------
+# Go-named entry points
+# ---------------------------------------------------------------------------
+def DefaultLBVH(scene: DeviceScene) -> BVH:
+    """pkg/pt/lbvh.go:13-15."""
+    ctx = scene.ctx
+    h = C.c_void_p()
+    ctx.check(ctx.L.gbt_lbvh_build(ctx.h, scene.h, C.byref(h)), "lbvh_build")
+    return BVH(ctx, h, scene, "lbvh")
+
+
+@dataclass
+class PhrBuilder:
+    """pkg/pt/phr.go:13-24 (Threshold = DefaultThreshold, Split = SweepSAH)."""
+    Alpha: float = 0.5
+    Delta: float = 6.0
+    BranchingFactor: int = 2
+
+    def BuildFromAuxilary(self, aux: BVH) -> BVH:
+        ctx = aux.ctx
+        h = C.c_void_p()
+        ctx.check(ctx.L.gbt_phr_build(ctx.h, aux.h, float(self.Alpha), float(self.Delta), int(self.BranchingFactor),
+                                      C.byref(h)), "phr_build")
+        return BVH(ctx, h, aux.scene, "phr")
+
+    def Build(self, scene: DeviceScene) -> BVH:
+        aux = DefaultLBVH(scene)
+        out = self.BuildFromAuxilary(aux)
+        out.aux = aux
+        return out
+
+
+def NewPHRBuilder(alpha, delta, branching_factor):
+    return PhrBuilder(alpha, delta, branching_factor)
+
+
+def NewDefaultBuilder():
+    return PhrBuilder(0.5, 6.0, 2)  # phr.go:26-28
+
+
+@dataclass
+class CameraTransformation:
+    LookFrom: tuple
+    LookAt: tuple
+    Up: tuple = (0.0, 1.0, 0.0)
+
+
+@dataclass
+class Camera:
+    aspect: float
+    fov: float
+    transform: CameraTransformation
+
+    def SetTransformation(self, t):
+        self.transform = t
+
+    def desc(self):
+        return dict(look_from=self.transform.LookFrom, look_at=self.transform.LookAt, up=self.transform.Up,
+                    aspect=self.aspect, fov=self.fov)
+
+
+def NewCamera(aspect, fov, transform):
+    return Camera(aspect, fov, transform)
+
+
+def NewDefaultCamera(aspect, fov):
+    return Camera(aspect, fov, CameraTransformation((0, 0, 0), (1, 0, 0), (0, 1, 0)))
+
+
+@dataclass
+class PixelBuffer:
+    width: int
+    height: int
+    data: np.ndarray = field(default=None, repr=False)
+
+    def Width(self):
+        return self.width
+
+    def Height(self):
+        return self.height
+
+
+def NewPxlBuffer(width, height):
+    return PixelBuffer(width, height, np.zeros((height, width, 3), np.float32))
+
+
+def NewFrameBuffer(width, height):
+    return PixelBuffer(width, height, np.zeros((height, width, 3), np.float32))
+
+
+@dataclass
+class ImageRenderer:
+    """pkg/pt/render.go:20-30; only the built-in shaders run on the device."""
+    Bvh: BVH
+    Camera: Camera
+    MaxDepth: int = 5
+    Spp: int = 300
+    Miss: int = MISS_BLACK
+    MissColor: tuple = (0.0, 0.0, 0.0)
+    Seed: int = 1
+    Verbose: bool = False
+    last_stats: dict = None
+
+    def RenderToBuffer(self, buff: PixelBuffer):
+        img, st = self.Bvh.render(self.Camera.desc(), buff.width, buff.height, self.Spp, self.MaxDepth, self.Miss,
+                                  self.MissColor, self.Seed)
+        buff.data[...] = img
+        self.last_stats = st
+        return buff
+
+
+def NewDefaultRenderer(bvh, camera):
+    return ImageRenderer(bvh, camera, MaxDepth=5, Spp=300, Miss=MISS_BLACK)  # render.go:32-44
+
+
+def NewBenchmarkRenderer(bvh, camera):
+    return ImageRenderer(bvh, camera, MaxDepth=5, Spp=1, Miss=MISS_WHITE)  # render.go:60-72
+
+
+def ParseFromPath(path):
+    """pkg/pt/obj.go:10-17 -> (verts (n,9) float32, normals (n,9) float32 or None)."""
+    L = _lib.load()
+    n = C.c_uint32(0)
+    hn = C.c_int32(0)
+    rc = L.gbt_obj_parse(str(path).encode(), None, None, C.byref(n), C.byref(hn))
+    if rc != 0:
+        raise GbtError(rc, "ParseFromPath(%s)" % path)
+    verts = np.empty((n.value, 9), np.float32)
+    normals = np.empty((n.value, 9), np.float32)
+    rc = L.gbt_obj_parse(str(path).encode(), _p(verts), _p(normals), C.byref(n), C.byref(hn))
+    if rc != 0:
+        raise GbtError(rc, "ParseFromPath(%s)" % path)
+    return verts, (normals if hn.value else None)
