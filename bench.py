@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Headline benchmark: Mrays/s on the 1M-triangle soup.
+
+Workload: 1,000,000 random triangles (centroids U[0,1]^3, seed 1, vertex
+offsets U[-0.005, 0.005]), LBVH built then PHR-refined (alpha 0.5, delta 6,
+branching 2), rendered at 1920x1080 with one primary ray and one
+cosine-weighted diffuse bounce per pixel (spp 1, MaxDepth 0, white miss,
+albedo 0.7) -- the reference's benchmark renderer (render.go:60-72) on this
+scene.  A step is one frame.  Inputs (scene, BVH) are resident in HBM; L2 is
+flushed (a 256 MiB write) before every timed step.
+
+Reported:
+  value        rays traced / device time of the K timed frames (CUDA events
+               on the library's stream), summed over ranks / max over ranks
+  e2e          the same through the C ABI's gbt_render with a pinned host
+               image (the image's device->host copy is inside the timed region)
+  roofline     traversal kernels: counted bytes (64 B per inner node fetched,
+               48 B per primitive record tested, 32 B ray + 16 B hit per ray)
+               per second against the measured HBM copy bandwidth
+  cpu_baseline the C restatement of the reference (oracle/) on the host cores,
+               on a bounded sample of the same frame
+  lbvh         LBVH build Mtri/s on the same scene, with its own roofline
+
+--impl reference times the reference's CPU path (the C restatement in
+oracle/, since the Go reference cannot be built here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, SPP, MAX_DEPTH = 1920, 1080, 1, 0
+N_TRI = 1_000_000
+PHR = (0.5, 6.0, 2)
+WORKLOAD = "soup1M_1920x1080_primary+1bounce_spp1"
+
+# Algorithmic bytes of one LBVH build per triangle, by kernel:
+#   bounds 36 (read vertices) + morton 44 (read 36, write 8-byte key)
+#   + histogram 8 + 8 sort passes x 24 (read+write 8-byte key and 4-byte index)
+#   + runs 28 (two key reads, 12 bytes written per run)
+#   + gather 88 (index 4 + vertices 36 read, 48-byte record written)
+#   + emission/refit 48 (record) + 64 (node) + 8 (runs) + 8 (codes for prefix tests)
+LBVH_BYTES_PER_TRI = 36 + 44 + 8 + 8 * 24 + 28 + 88 + 48 + 64 + 8 + 8
+SORT_BYTES_PER_KEY = 8 * 24
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, backend):
+        self.ws = ws
+        self.torch = None
+        if ws > 1:
+            import torch
+            import torch.distributed as dist
+
+            self.torch = torch
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def reduce(self, x, op="max"):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64)
+        if self.dist.get_backend() == "nccl":
+            t = t.cuda()
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else "/tmp/gbt_clocks.csv"
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, seconds=8.0, threads=None):
+    """The oracle's renderer (a C restatement of render.go:91-129) on a bounded
+    sample of the frame: 480x270 frames of the same view, repeated for about
+    `seconds`, all host threads."""
+    from oracle import oracle as O
+
+    threads = threads or (os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    o = O.lbvh(scene["verts"], threads=threads)
+    ph = o.phr(*PHR)
+    build_s = time.perf_counter() - t0
+    rays, el, frames, seed = 0, 0.0, 0, 1
+    sw, sh = 480, 270
+    while el < seconds or frames == 0:
+        t = time.perf_counter()
+        ph.render(scene, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=seed, threads=threads)
+        el += time.perf_counter() - t
+        rays += ph.last_rays
+        frames += 1
+        seed += 1
+    return {"value": rays / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": "%d frames of %dx%d (same camera, spp %d, MaxDepth %d) on the PHR tree; %d rays in %.2f s; "
+                      "CPU LBVH+PHR build %.2f s untimed" % (frames, sw, sh, SPP, MAX_DEPTH, rays, el, build_s)}
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the reference's CPU path on the host cores."""
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    from trace_gb300 import scenes
+
+    O.build()
+    s = scenes.soup(N_TRI, seed=1, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH)
+    threads = os.cpu_count() or 1
+    o = O.lbvh(s["verts"], threads=threads)
+    ph = o.phr(*PHR)
+    sw, sh = 480, 270
+    for i in range(args.warmup):
+        ph.render(s, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=1000 + i, threads=threads)
+    rays, el = 0, 0.0
+    for i in range(args.steps):
+        t = time.perf_counter()
+        ph.render(s, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=1 + i, threads=threads)
+        el += time.perf_counter() - t
+        rays += ph.last_rays
+    val = rays / el / 1e6
+    line = {"impl": "reference", "metric": "Mrays/s", "value": val, "unit": "Mrays/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
+                       "max_depth": MAX_DEPTH, "bvh": "phr(alpha=0.5,delta=6,bf=2)",
+                       "step_sample": "%dx%d frame of the same view per step" % (sw, sh)},
+            "cpu_baseline": {"value": val, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": "%dx%d frame per step, %d steps, %d rays" % (sw, sh, args.steps, rays)},
+            "e2e": {"value": val, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "C restatement of pkg/pt (oracle/); the Go reference cannot be built on this image"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbt", choices=["gbt", "reference"])
+    ap.add_argument("--bvh", default="phr", choices=["phr", "lbvh"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+
+    from trace_gb300 import _lib, pt, scenes
+
+    torch.cuda.set_device(local)
+    dist = Dist(ws, "nccl")
+    ctx = pt.Context(local)
+    s = scenes.soup(N_TRI, seed=1, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    aux = pt.DefaultLBVH(ds)
+    bvh_name = "lbvh"
+    bvh = aux
+    if args.bvh == "phr":
+        try:
+            bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux)
+            bvh_name = "phr(alpha=0.5,delta=6,bf=2)"
+        except _lib.GbtError as e:
+            if e.code != -6:
+                raise
+    L, h = ctx.L, ctx.h
+    cam = pt.make_camera(s["camera"])
+    rp = _lib.RenderParams(W, H, SPP, MAX_DEPTH, pt.MISS_WHITE, (C.c_float * 3)(1, 1, 1), 7)
+    d_img = ctx.alloc(W * H * 3 * 4)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    st = _lib.RenderStats()
+    # warm-up
+    for i in range(args.warmup):
+        ctx.check(L.gbt_render_async(h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+    ctx.sync()
+    # roofline counters: one counting frame (not timed)
+    ctx.check(L.gbt_ctx_set_profiling(h, 2))
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    ctx.check(L.gbt_render_async(h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    count_stats = st.as_dict()
+    # timed region: per-step events, L2 flushed before each step
+    ctx.check(L.gbt_ctx_set_profiling(h, 1))
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    ctx.sync()
+    for k in range(args.steps):
+        flush_l2()
+        ev[k][0].record(stream)
+        ctx.check(L.gbt_render_async(h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+        ev[k][1].record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    timed = st.as_dict()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms_max = dist.reduce(ms, "max")
+    rays_all = dist.reduce(timed["rays_traced"], "sum")
+    value = rays_all / ms_max / 1e3  # Mrays/s
+    # roofline of the traversal kernels
+    hbm, peak_kind = peaks()
+    rays_per_frame = count_stats["rays_traced"]
+    bytes_frame = 64 * count_stats["nodes_visited"] + 48 * count_stats["prims_tested"] + 48 * rays_per_frame
+    trav_ms_frame = timed["ms_traverse"] / args.steps
+    achieved = bytes_frame / (trav_ms_frame * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": TRAVERSAL_TRAFFIC.get(bvh_name.split("(")[0]), "kernel": "k_trace2 (closest hit)",
+            "peak_source": peak_kind, "bytes_per_frame": bytes_frame,
+            "traversal_ms_per_frame": trav_ms_frame, "traversal_share": timed["ms_traverse"] / ms,
+            "nodes_per_ray": count_stats["nodes_visited"] / rays_per_frame,
+            "prims_per_ray": count_stats["prims_tested"] / rays_per_frame,
+            "note": "bytes counted at the node/record level; most are L1/L2 hits, so frac can exceed 1"}
+    ctx.check(L.gbt_ctx_set_profiling(h, 0))
+
+    # e2e: the C-ABI call with a pinned host image, device->host copy inside the timed region
+    hp = C.c_void_p()
+    ctx.check(L.gbt_host_alloc(h, W * H * 3 * 4, C.byref(hp)), "host_alloc")
+    img = np.ctypeslib.as_array(C.cast(hp, C.POINTER(C.c_float)), shape=(H, W, 3))
+    for i in range(2):
+        ctx.check(L.gbt_render(h, bvh.h, C.byref(cam), C.byref(rp), hp, None), "render")
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ctx.check(L.gbt_render(h, bvh.h, C.byref(cam), C.byref(rp), hp, None), "render")
+    e2e_s = time.perf_counter() - t0
+    dist.barrier()
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    e2e_rays = dist.reduce(st.rays_traced, "sum")
+    e2e_s = dist.reduce(e2e_s, "max")
+    assert np.isfinite(img).all()
+    L.gbt_host_free(h, hp)
+
+    # LBVH rebuild throughput on the same scene
+    lb_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.warmup):
+        ctx.check(L.gbt_lbvh_rebuild_async(h, aux.h), "rebuild")
+    ctx.sync()
+    for k in range(args.steps):
+        flush_l2()
+        lb_ev[k][0].record(stream)
+        ctx.check(L.gbt_lbvh_rebuild_async(h, aux.h), "rebuild")
+        lb_ev[k][1].record(stream)
+    ctx.sync()
+    lb_ms = sum(a.elapsed_time(b) for a, b in lb_ev) / args.steps
+    lb_ms = dist.reduce(lb_ms, "max")
+    lb_bw = N_TRI * LBVH_BYTES_PER_TRI / (lb_ms * 1e-3) / 1e9
+    lbvh = {"mtri_s": N_TRI / lb_ms / 1e3 * ws, "ms": lb_ms,
+            "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
+                         "bytes_per_tri": LBVH_BYTES_PER_TRI, "traffic": None, "kernel": "whole build (15 launches)"}}
+
+    line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
+                       "max_depth": MAX_DEPTH, "miss": "white", "bvh": bvh_name,
+                       "rays_per_step": timed["rays_traced"] / args.steps,
+                       "l2": "flushed before every timed step (256 MiB write)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roof,
+            "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s",
+                    "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(rp), "d2h_bytes_per_step": W * H * 3 * 4,
+                    "api": "gbt_render (C ABI), pinned host image"},
+            "gpu_launches": int(timed["kernel_launches"]),
+            "clocks": clk,
+            "lbvh": lbvh}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s, seconds=args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.free(d_img)
+    dist.close()
+    return 0
+
+
+# DRAM bytes per traversal launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum),
+# filled in from the capture summarised in profiles/; None until captured.
+TRAVERSAL_TRAFFIC = {"lbvh": None, "phr": None}
+
+if __name__ == "__main__":
+    sys.exit(main())

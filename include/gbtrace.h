@@ -79,10 +79,14 @@ typedef struct {
 } gbt_render_params;
 
 typedef struct {
-    uint64_t rays_traced;  /* every traced segment: primary + bounces */
+    uint64_t rays_traced;       /* every traced segment: primary + bounces */
     uint64_t paths;
-    double ms_total;       /* device time of the render, CUDA events */
-    double ms_traverse;    /* device time inside traversal launches */
+    double ms_total;            /* device time of the render (CUDA events; gbt_render only) */
+    double ms_traverse;         /* device time inside traversal launches (profiling >= 1) */
+    uint64_t traverse_launches; /* traversal kernels launched */
+    uint64_t kernel_launches;   /* all kernels this library launched for the render */
+    uint64_t nodes_visited;     /* inner nodes fetched by traversal (profiling 2) */
+    uint64_t prims_tested;      /* primitive records tested (profiling 2) */
 } gbt_render_stats;
 
 /* ---- context -------------------------------------------------------- */
@@ -91,6 +95,10 @@ int gbt_ctx_destroy(gbt_ctx *ctx);
 const char *gbt_last_error(const gbt_ctx *ctx);
 void *gbt_ctx_stream(gbt_ctx *ctx); /* the context's cudaStream_t */
 int gbt_ctx_sync(gbt_ctx *ctx);
+/* Profiling level of later calls: 0 off; 1 CUDA events around every traversal
+ * launch (ms_traverse); 2 also counts inner nodes and primitive tests (a
+ * slower counting traversal).  No counterpart in the reference. */
+int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */
 /* verts: n_tri*9 floats (v0 v1 v2); normals: n_tri*9 per-vertex normals or
@@ -150,6 +158,8 @@ int gbt_render_last_stats(gbt_ctx *ctx, gbt_render_stats *stats);
 /* ---- device memory helpers for callers without a CUDA runtime ------- */
 int gbt_device_alloc(gbt_ctx *ctx, size_t bytes, void **d_ptr);
 int gbt_device_free(gbt_ctx *ctx, void *d_ptr);
+int gbt_host_alloc(gbt_ctx *ctx, size_t bytes, void **h_ptr); /* page-locked host memory */
+int gbt_host_free(gbt_ctx *ctx, void *h_ptr);
 int gbt_copy_h2d_async(gbt_ctx *ctx, void *d_dst, const void *h_src, size_t bytes);
 int gbt_copy_d2h_async(gbt_ctx *ctx, void *h_dst, const void *d_src, size_t bytes);
 

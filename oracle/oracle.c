@@ -948,7 +948,10 @@ typedef struct {
     ocam cam;
     double *acc; /* running mean per pixel (PixelBuffer) */
     int32_t *samples;
+    atomic_llong rays;
 } render_ctx;
+
+static _Thread_local int64_t tl_rays; /* rays traced by this thread's current row */
 
 static v3 miss_color(const render_ctx *x, const oray *r) { /* render.go:228-246 */
     switch (x->rd->miss_mode) {
@@ -979,6 +982,7 @@ static v3 shade(const render_ctx *x, oray r, ohit h, int depth, xrng *g) {
     ohit h2;
     memset(&h2, 0, sizeof(h2));
     (void)r;
+    tl_rays++;
     if (bvh_hit(x->b, &r2, 0.0001, INFINITY, &h2, 1))
         return vadd(light, vemul(shade(x, r2, h2, depth, g), col));
     return vadd(light, vemul(miss_color(x, &r2), col));
@@ -990,6 +994,7 @@ static void render_row(void *c, int64_t job) {
     int64_t pass = job / hgt, y = job % hgt;
     xrng g;
     xseed(&g, x->rd->seed, (uint64_t)pass + 1, (uint64_t)y + 1);
+    tl_rays = w; /* one primary ray per pixel */
     for (int32_t px = 0; px < w; px++) {
         double s = ((double)px + xf64(&g)) / (double)(w - 1); /* RandomSampling render.go:201-205 */
         double t = ((double)y + xf64(&g)) / (double)(hgt - 1);
@@ -1012,6 +1017,7 @@ static void render_row(void *c, int64_t job) {
             a[2] = a[2] + (col.z - a[2]) / n;
         }
     }
+    atomic_fetch_add(&x->rays, tl_rays);
 }
 
 typedef struct { render_ctx *x; int64_t pass; } pass_ctx;
@@ -1021,7 +1027,7 @@ static void pass_row(void *c, int64_t y) {
 }
 
 int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_type, const double *mat_color,
-               const orc_camera_desc *cam, const orc_render_desc *rd, double *rgb) {
+               const orc_camera_desc *cam, orc_render_desc *rd, double *rgb) {
     if (rd->width < 2 || rd->height < 2) return ORC_E_ARG;
     render_ctx x;
     x.b = b;
@@ -1031,6 +1037,7 @@ int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_typ
     x.rd = rd;
     x.cam = make_camera(cam);
     x.acc = rgb;
+    atomic_init(&x.rays, 0);
     int64_t np = (int64_t)rd->width * rd->height;
     x.samples = (int32_t *)calloc((size_t)np, sizeof(int32_t));
     if (!x.samples) return ORC_E_NOMEM;
@@ -1041,6 +1048,7 @@ int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_typ
         pass_ctx pc = {&x, pass};
         orc_parallel(rd->threads, rd->height, pass_row, &pc);
     }
+    rd->rays_traced = atomic_load(&x.rays);
     free(x.samples);
     return ORC_OK;
 }

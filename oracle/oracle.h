@@ -78,11 +78,12 @@ typedef struct {
     double miss_color[3];
     uint64_t seed;
     int32_t threads;
+    int64_t rays_traced; /* out: every traced segment (primary + bounces) */
 } orc_render_desc;
 
 /* materials: mat_type[m] 0 = Diffuse(albedo), 1 = Light(color); mat_color[m*3] */
 int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_type, const double *mat_color,
-               const orc_camera_desc *cam, const orc_render_desc *rd, double *rgb);
+               const orc_camera_desc *cam, orc_render_desc *rd, double *rgb);
 void orc_camera_rays(const orc_camera_desc *cam, int32_t width, int32_t height,
                      const double *su, const double *sv, int64_t n, double *dirs, double origin[3]);
 

@@ -77,7 +77,7 @@ class CameraDesc(C.Structure):
 class RenderDesc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("miss_mode", C.c_int32), ("miss_color", C.c_double * 3), ("seed", C.c_uint64),
-                ("threads", C.c_int32)]
+                ("threads", C.c_int32), ("rays_traced", C.c_int64)]
 
 
 def split_by3(a):
@@ -198,6 +198,7 @@ class BVH:
         rc = lib().orc_render(self.h, _p(pm), _p(mt), _p(mc), C.byref(cd), C.byref(r), _p(img))
         if rc != 0:
             raise RuntimeError("oracle render failed: %d" % rc)
+        self.last_rays = int(r.rays_traced)
         return img
 
     def phr(self, alpha=0.5, delta=6.0, bf=2):

@@ -79,3 +79,16 @@ def test_rebuild_in_place_is_identical(ctx):
     ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, g.h), "rebuild")
     ctx.sync()
     assert canonical_equal(e1, g.export())
+
+
+def test_context_closed_before_its_objects():
+    """Closing a context first destroys its scenes and BVHs; later deletes are no-ops."""
+    c = pt.Context(0)
+    s = scenes.soup(1000, seed=2)
+    ds = pt.DeviceScene.from_dict(c, s)
+    g = pt.DefaultLBVH(ds)
+    c.close()
+    del g, ds
+    import gc
+
+    gc.collect()

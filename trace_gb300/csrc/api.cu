@@ -94,7 +94,9 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
     cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&c->d_error, sizeof(unsigned int)) != cudaSuccess ||
-        cudaMemset(c->d_error, 0, sizeof(unsigned int)) != cudaSuccess) {
+        cudaMemset(c->d_error, 0, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc(&c->d_counters, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(c->d_counters, 0, 4 * sizeof(unsigned long long)) != cudaSuccess) {
         delete c;
         return GBT_ECUDA;
     }
@@ -110,6 +112,9 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->rstate) cudaFree(ctx->rstate);
     if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_out) cudaFree(ctx->d_out);
+    for (auto &e : ctx->prof_ev) cudaEventDestroy(e);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -119,6 +124,27 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
 
 extern "C" const char *gbt_last_error(const gbt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 extern "C" void *gbt_ctx_stream(gbt_ctx *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
+extern "C" int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level) {
+    if (!ctx || level < 0 || level > 2) return GBT_EINVAL;
+    if (level >= 1 && ctx->prof_ev.empty()) {
+        ctx->prof_ev.resize(1024);
+        for (auto &e : ctx->prof_ev) GBT_CUDA(ctx, cudaEventCreate(&e));
+    }
+    ctx->profiling = level;
+    ctx->n_prof_ev = 0;
+    return GBT_OK;
+}
+
+void gbt_prof_begin(gbt_ctx *ctx) {
+    if (ctx->profiling >= 1 && ctx->n_prof_ev + 2 <= (int)ctx->prof_ev.size())
+        cudaEventRecord(ctx->prof_ev[ctx->n_prof_ev++], ctx->stream);
+}
+
+void gbt_prof_end(gbt_ctx *ctx) {
+    if (ctx->profiling >= 1 && (ctx->n_prof_ev & 1))
+        cudaEventRecord(ctx->prof_ev[ctx->n_prof_ev++], ctx->stream);
+}
 
 extern "C" int gbt_ctx_sync(gbt_ctx *ctx) {
     if (!ctx) return GBT_EINVAL;
@@ -224,6 +250,7 @@ extern "C" int gbt_bvh_destroy(gbt_bvh *b) {
     cudaFree(b->d_parent);
     cudaFree(b->d_size);
     cudaFree(b->d_other);
+    cudaFree(b->d_range);
     delete b;
     return GBT_OK;
 }
@@ -248,6 +275,7 @@ static int lbvh_alloc(gbt_ctx *ctx, gbt_scene *sc, gbt_bvh **out) {
     if (!rc) rc = dalloc(ctx, &b->d_parent, n);
     if (!rc) rc = dalloc(ctx, &b->d_size, n);
     if (!rc) rc = dalloc(ctx, &b->d_other, n);
+    if (!rc) rc = dalloc(ctx, &b->d_range, n);
     if (rc) { gbt_bvh_destroy(b); return rc; }
     *out = b;
     return GBT_OK;
@@ -496,13 +524,23 @@ extern "C" int gbt_render_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *ca
 
 extern "C" int gbt_render_last_stats(gbt_ctx *ctx, gbt_render_stats *stats) {
     if (!ctx || !stats) return GBT_EINVAL;
-    unsigned long long total = 0;
-    if (ctx->d_ray_total) {
-        GBT_CUDA(ctx, cudaMemcpyAsync(&total, ctx->d_ray_total, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
-        GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned long long c[4] = {0, 0, 0, 0};
+    GBT_CUDA(ctx, cudaMemcpyAsync(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+    GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double ms = 0.0;
+    for (int i = 0; i + 1 < ctx->n_prof_ev; i += 2) {
+        float m = 0.f;
+        if (cudaEventElapsedTime(&m, ctx->prof_ev[i], ctx->prof_ev[i + 1]) == cudaSuccess) ms += m;
     }
-    ctx->last_stats.rays_traced = total;
+    ctx->last_stats.nodes_visited = c[0];
+    ctx->last_stats.prims_tested = c[1];
+    ctx->last_stats.rays_traced = c[2];
+    ctx->last_stats.ms_traverse = ms;
     *stats = ctx->last_stats;
+    // stats accumulate from one read to the next
+    ctx->last_stats = gbt_render_stats{};
+    ctx->n_prof_ev = 0;
+    GBT_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     return GBT_OK;
 }
 
@@ -511,8 +549,15 @@ extern "C" int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, con
     if (!ctx || !bvh || !cam || !p || !rgb) return GBT_EINVAL;
     if (p->width < 2 || p->height < 2) return gbt_fail(ctx, GBT_EINVAL, "render: width and height must be >= 2");
     size_t bytes = (size_t)p->width * p->height * 3 * sizeof(float);
-    float *d = nullptr;
-    GBT_TRY(dalloc(ctx, &d, bytes / sizeof(float)));
+    if (ctx->d_out_bytes < bytes) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_out);
+        ctx->d_out = nullptr;
+        ctx->d_out_bytes = 0;
+        GBT_TRY(dalloc(ctx, &ctx->d_out, bytes / sizeof(float)));
+        ctx->d_out_bytes = bytes;
+    }
+    float *d = ctx->d_out;
     cudaEventRecord(ctx->ev[0], ctx->stream);
     int rc = gbt_render_enqueue(ctx, bvh, cam, p, d);
     cudaEventRecord(ctx->ev[1], ctx->stream);
@@ -520,12 +565,11 @@ extern "C" int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, con
     if (!rc) e = cudaMemcpyAsync(rgb, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (!rc && !e) rc = gbt_check_device_error(ctx, "render");
     cudaStreamSynchronize(ctx->stream);
-    cudaFree(d);
     if (e) return gbt_cuda_fail(ctx, e, "render copy");
     if (rc) return rc;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-    ctx->last_stats.ms_total = ms;
+    ctx->last_stats.ms_total += ms;
     if (stats) return gbt_render_last_stats(ctx, stats);
     return GBT_OK;
 }
@@ -545,6 +589,19 @@ extern "C" int gbt_device_free(gbt_ctx *ctx, void *d_ptr) {
     if (!ctx) return GBT_EINVAL;
     cudaStreamSynchronize(ctx->stream);
     cudaFree(d_ptr);
+    return GBT_OK;
+}
+extern "C" int gbt_host_alloc(gbt_ctx *ctx, size_t bytes, void **h_ptr) {
+    if (!ctx || !h_ptr) return GBT_EINVAL;
+    if (cudaMallocHost(h_ptr, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ENOMEM, "host_alloc");
+    }
+    return GBT_OK;
+}
+extern "C" int gbt_host_free(gbt_ctx *ctx, void *h_ptr) {
+    if (!ctx) return GBT_EINVAL;
+    cudaFreeHost(h_ptr);
     return GBT_OK;
 }
 extern "C" int gbt_copy_h2d_async(gbt_ctx *ctx, void *d_dst, const void *h_src, size_t bytes) {

@@ -33,9 +33,19 @@ struct gbt_ctx {
     void *rstate = nullptr;
     size_t rstate_bytes = 0;
     gbt_render_stats last_stats{};
-    unsigned long long *d_ray_total = nullptr;  // rays traced by the last render (device)
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // profiling (gbt_ctx_set_profiling)
+    int profiling = 0;
+    std::vector<cudaEvent_t> prof_ev;           // pairs around traversal launches
+    int n_prof_ev = 0;
+    unsigned long long *d_counters = nullptr;   // [0] inner nodes fetched, [1] primitive tests, [2] rays traced
+    float *d_out = nullptr;                     // gbt_render's device image (grow-only)
+    size_t d_out_bytes = 0;
 };
+
+// Record a profiling event pair around one traversal launch.
+void gbt_prof_begin(gbt_ctx *ctx);
+void gbt_prof_end(gbt_ctx *ctx);
 
 struct gbt_scene {
     gbt_ctx *ctx = nullptr;
@@ -81,6 +91,8 @@ struct gbt_bvh {
     int32_t *d_parent = nullptr;    // per inner node: parent node (-1 root) -- LBVH only
     uint32_t *d_size = nullptr;     // per inner node: subtree size (bvh.go:159-167)
     int32_t *d_other = nullptr;     // emission hand-off words
+    uint2 *d_range = nullptr;       // per inner node: distinct-code range [l, r]
+    uint32_t n_nodes_host = 0;      // PHR: nodes allocated in d_nodes
 };
 
 // ---------------------------------------------------------------------------
@@ -108,7 +120,8 @@ size_t gbt_lbvh_scratch_bytes(uint32_t n);
 // traverse.cu
 int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits);
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
-                         const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s);
+                         const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s,
+                         unsigned long long *d_counters = nullptr);
 // render.cu
 int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
                        float *d_rgb);

@@ -547,7 +547,7 @@ __device__ __forceinline__ int prefix_len(const uint64_t *__restrict__ ukey, uin
 __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
                                               const uint32_t *__restrict__ run, const uint64_t *__restrict__ ukey,
                                               const float4 *__restrict__ recs, float4 *nodes, int32_t *other,
-                                              uint32_t *subtree, int32_t *parent_of, uint32_t n) {
+                                              uint32_t *subtree, int32_t *parent_of, uint2 *range, uint32_t n) {
     const uint32_t U = hdr_in->n_unique;
     uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= U || u >= n) return;
@@ -594,6 +594,7 @@ __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader
         subtree[p] = size;
         if (left) r = (uint32_t)o;
         else l = (uint32_t)o;
+        range[p] = make_uint2(l, r);  // distinct-code range of inner node p
         ref = (int32_t)p;
         cnt = 0;
     }
@@ -670,7 +671,7 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims);
     GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
     k_emit<<<(n + 255) / 256, 256, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
-                                            bvh->d_other, bvh->d_size, bvh->d_parent, n);
+                                            bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n);
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }

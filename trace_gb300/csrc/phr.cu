@@ -1,7 +1,973 @@
-// PHR refinement on the device (pkg/pt/phr.go).  Filled in below.
+// PHR refinement on the device: pkg/pt/phr.go:47-459 (BuildFromAuxilary).
+//
+//   k_aux_build      unified view of the LBVH (inner nodes and leaves) with
+//                    boxes, subtree sizes (bvh.go:159-167) and primitive ranges
+//   k_initial_cut    findInitialCut (phr.go:257-311), breadth-first in FIFO
+//                    order with the MAX_CUT_SIZE cap, one block
+//   k_phr_level      buildSubTree (phr.go:92-152), one block per cut, one
+//                    launch per tree level:
+//                      SweepSAH (phr.go:368-405): three stable sorts by
+//                      barycenter, chained x -> y -> z as the Go code chains
+//                      them, each followed by minCost (phr.go:414-459), an
+//                      exact float64 sweep done as a prefix/suffix scan of
+//                      boxes and subtree sizes plus an argmin;
+//                      refined (phr.go:313-338) and makeLeaf (phr.go:340-352)
+//   k_phr_finalize   the N-ary tree into 64-byte binary or 128-byte 4-wide nodes
+//
+// The result is the oracle's tree exactly: same splits, same tie orders, same
+// leaves, so SAH cost and hit ids agree with it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "gbt_internal.cuh"
 
+namespace {
+
+constexpr uint32_t MAX_CUT_SIZE = 2500;  // phr.go:11
+constexpr int PT = 256;                  // threads per job block
+constexpr int DEPTH_TABLE = 4096;
+
+struct AuxNode {
+    float lo[3], hi[3];
+    uint32_t size, first, count;
+    int32_t c0, c1;
+    uint32_t pad;
+};
+
+struct PJob {
+    uint32_t off, n;
+    float lo[3], hi[3];
+    int32_t depth, parent, slot, pad;
+};
+
+struct PNode {
+    float lo[3], hi[3];
+    int32_t leaf, nchild;
+    int32_t child[4];
+    uint32_t rec_off, rec_cnt;
+};
+
+struct PhrGlobals {
+    uint32_t pnode_ctr, rec_ctr;
+    int32_t root;
+    uint32_t pad;
+    uint32_t job_ctr[2], pool_ctr[2], max_n[2];
+};
+
+// ---------------------------------------------------------------------------
+// float64 helpers, every operation rounded on its own (no contraction)
+// ---------------------------------------------------------------------------
+// aabb.surface (bounding.go:45-47) of a float32 box evaluated in float64
+__device__ __forceinline__ double surface(const float *lo, const float *hi) {
+    double w = __dsub_rn((double)hi[0], (double)lo[0]);
+    double h = __dsub_rn((double)hi[1], (double)lo[1]);
+    double d = __dsub_rn((double)hi[2], (double)lo[2]);
+    double a = __dmul_rn(__dmul_rn(2.0, w), h);
+    double b = __dmul_rn(__dmul_rn(2.0, w), d);
+    double c = __dmul_rn(__dmul_rn(2.0, h), d);
+    return __dadd_rn(__dadd_rn(a, b), c);
+}
+
+__device__ __forceinline__ double bary(const AuxNode &a, int axis) {
+    return __dmul_rn(__dadd_rn((double)a.lo[axis], (double)a.hi[axis]), 0.5);
+}
+
+__device__ __forceinline__ unsigned long long dbl_key(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+
+struct BoxAgg {
+    float lo[3], hi[3];
+    uint32_t c;
+};
+
+__device__ __forceinline__ BoxAgg agg_identity() {
+    BoxAgg a;
+    a.lo[0] = a.lo[1] = a.lo[2] = INFINITY;
+    a.hi[0] = a.hi[1] = a.hi[2] = -INFINITY;
+    a.c = 0;
+    return a;
+}
+
+__device__ __forceinline__ BoxAgg agg_join(const BoxAgg &a, const BoxAgg &b) {
+    BoxAgg r;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        r.lo[k] = fminf(a.lo[k], b.lo[k]);
+        r.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+    }
+    r.c = a.c + b.c;
+    return r;
+}
+
+__device__ __forceinline__ BoxAgg agg_shfl_up(const BoxAgg &a, int o) {
+    BoxAgg r;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        r.lo[k] = __shfl_up_sync(0xffffffffu, a.lo[k], o);
+        r.hi[k] = __shfl_up_sync(0xffffffffu, a.hi[k], o);
+    }
+    r.c = __shfl_up_sync(0xffffffffu, a.c, o);
+    return r;
+}
+
+// Exclusive scan of one BoxAgg per thread in the order given by `rank`
+// (0..PT-1); blockDim == PT.  s_tmp holds PT/32 aggregates.
+__device__ BoxAgg block_scan_agg(BoxAgg v, int rank, BoxAgg *s_tmp, BoxAgg *s_rank) {
+    // place by rank so that warps scan consecutive ranks
+    s_rank[rank] = v;
+    __syncthreads();
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    BoxAgg x = s_rank[t];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        BoxAgg y = agg_shfl_up(x, o);
+        if (lane >= o) x = agg_join(y, x);
+    }
+    if (lane == 31) s_tmp[w] = x;
+    __syncthreads();
+    BoxAgg pre = agg_identity();
+    for (int j = 0; j < w; j++) pre = agg_join(pre, s_tmp[j]);
+    // exclusive value at position t: earlier warps, then earlier lanes (lane-1's inclusive)
+    BoxAgg prev = agg_shfl_up(x, 1);
+    BoxAgg excl = lane == 0 ? pre : agg_join(pre, prev);
+    __syncthreads();
+    s_rank[t] = excl;
+    __syncthreads();
+    BoxAgg out = s_rank[rank];
+    __syncthreads();
+    return out;
+}
+
+__device__ uint32_t block_scan_u32(uint32_t v, uint32_t *s_tmp, uint32_t *total) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[w] = x;
+    __syncthreads();
+    uint32_t off = 0, tot = 0;
+    for (int j = 0; j < (int)(blockDim.x >> 5); j++) {
+        uint32_t c = s_tmp[j];
+        off += (j < w) ? c : 0u;
+        tot += c;
+    }
+    __syncthreads();
+    *total = tot;
+    return off + x - v;
+}
+
+// ---------------------------------------------------------------------------
+// auxiliary tree
+// ---------------------------------------------------------------------------
+__global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+                            const uint32_t *__restrict__ subtree, const uint2 *__restrict__ range,
+                            const uint32_t *__restrict__ run, AuxNode *aux, uint32_t U, uint32_t n_prim) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {  // the root's own box lives in the header
+        uint32_t rid = hdr->root_cnt > 0 ? 0u : (uint32_t)hdr->root_ref;
+        AuxNode &a = aux[rid];
+        for (int c = 0; c < 3; c++) {
+            a.lo[c] = hdr->root_lo[c];
+            a.hi[c] = hdr->root_hi[c];
+        }
+        if (hdr->root_cnt > 0) {
+            a.size = 1;
+            a.first = 0;
+            a.count = n_prim;
+            a.c0 = a.c1 = -1;
+        }
+    }
+    if (U < 2 || k >= U - 1) return;
+    const float4 *nd = nodes + 4 * (size_t)k;
+    float4 n0 = nd[0], n1 = nd[1], n2 = nd[2];
+    int4 n3 = *reinterpret_cast<const int4 *>(nd + 3);
+    int32_t ids[2];
+    for (int c = 0; c < 2; c++) {
+        float4 xy = c ? n1 : n0;
+        float zl = c ? n2.z : n2.x, zh = c ? n2.w : n2.y;
+        int32_t ref = c ? n3.z : n3.x, cnt = c ? n3.w : n3.y;
+        int32_t id = cnt > 0 ? (int32_t)(U - 1 + k + c) : ref;
+        ids[c] = id;
+        AuxNode &a = aux[id];
+        a.lo[0] = xy.x; a.hi[0] = xy.y; a.lo[1] = xy.z; a.hi[1] = xy.w; a.lo[2] = zl; a.hi[2] = zh;
+        if (cnt > 0) {
+            a.size = 1;
+            a.first = (uint32_t)ref;
+            a.count = (uint32_t)cnt;
+            a.c0 = a.c1 = -1;
+        }
+    }
+    AuxNode &me = aux[k];
+    me.c0 = ids[0];
+    me.c1 = ids[1];
+    me.size = subtree[k];
+    uint2 lr = range[k];
+    me.first = run[lr.x];
+    me.count = run[lr.y + 1] - run[lr.x];
+}
+
+// ---------------------------------------------------------------------------
+// initial cut: FIFO breadth-first expansion with the MAX_CUT_SIZE cap
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_initial_cut(const AuxNode *__restrict__ aux, int32_t root, double thr0,
+                                                      uint32_t *front_a, uint32_t *front_b, uint32_t *cut,
+                                                      PJob *job0, PhrGlobals *g, uint32_t cap) {
+    __shared__ uint32_t s_tmp[32];
+    __shared__ uint32_t s_nf;
+    uint32_t *front = front_a, *next = front_b;
+    uint32_t nf = 1, counter = 0, ncut = 0;
+    if (threadIdx.x == 0) front[0] = (uint32_t)root;
+    __syncthreads();
+    while (nf > 0) {
+        uint32_t nnext = 0;
+        for (uint32_t base = 0; base < nf; base += blockDim.x) {
+            uint32_t i = base + threadIdx.x;
+            bool valid = i < nf;
+            uint32_t id = valid ? front[i] : 0u;
+            bool leaf = !valid || aux[id].c0 < 0;
+            bool attempt = valid && !leaf && surface(aux[id].lo, aux[id].hi) > thr0;
+            uint32_t tot_att, tot_exp, tot_term;
+            uint32_t a_ex = block_scan_u32(attempt ? 1u : 0u, s_tmp, &tot_att);
+            bool expand = attempt && (counter + a_ex + 1 < MAX_CUT_SIZE);
+            bool term = valid && !expand;
+            uint32_t e_ex = block_scan_u32(expand ? 1u : 0u, s_tmp, &tot_exp);
+            uint32_t t_ex = block_scan_u32(term ? 1u : 0u, s_tmp, &tot_term);
+            if (term && ncut + t_ex < cap) cut[ncut + t_ex] = id;
+            if (expand && nnext + 2 * e_ex + 1 < cap) {
+                next[nnext + 2 * e_ex] = (uint32_t)aux[id].c0;
+                next[nnext + 2 * e_ex + 1] = (uint32_t)aux[id].c1;
+            }
+            counter += tot_att;
+            ncut += tot_term;
+            nnext += 2 * tot_exp;
+        }
+        __syncthreads();
+        uint32_t *t = front;
+        front = next;
+        next = t;
+        nf = nnext;
+        if (threadIdx.x == 0) s_nf = nf;
+        __syncthreads();
+        nf = s_nf;
+    }
+    if (threadIdx.x == 0) {
+        job0->off = 0;
+        job0->n = ncut;
+        const AuxNode &r = aux[root];
+        for (int k = 0; k < 3; k++) {
+            job0->lo[k] = r.lo[k];
+            job0->hi[k] = r.hi[k];
+        }
+        job0->depth = 1;
+        job0->parent = -1;
+        job0->slot = 0;
+        g->job_ctr[0] = 1;
+        g->pool_ctr[0] = ncut;
+        g->max_n[0] = ncut;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// one tree level: one block per cut
+// ---------------------------------------------------------------------------
+struct Scratch {
+    uint32_t *ids, *ord[3];
+    unsigned long long *skey;
+    uint32_t *sval;
+    float *lb[6], *rb[6];
+    uint32_t *lc, *rc, *flag;
+};
+
+__host__ __device__ inline uint32_t pow2_at_least(uint32_t n) {
+    uint32_t p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+__host__ __device__ inline size_t scratch_bytes_for(uint32_t nmax) {
+    size_t P = pow2_at_least(nmax > 0 ? nmax : 1);
+    return (size_t)nmax * 4 * 4 + P * 12 + (size_t)nmax * 12 * 4 + (size_t)nmax * 3 * 4 + 256 * 4;
+}
+
+__device__ Scratch carve(unsigned char *base, uint32_t nmax) {
+    Scratch s;
+    uint32_t P = pow2_at_least(nmax > 0 ? nmax : 1);
+    unsigned char *p = base;
+    s.skey = reinterpret_cast<unsigned long long *>(p);
+    p += (size_t)P * 8;
+    s.sval = reinterpret_cast<uint32_t *>(p);
+    p += (size_t)P * 4;
+    s.ids = reinterpret_cast<uint32_t *>(p);
+    p += (size_t)nmax * 4;
+    for (int k = 0; k < 3; k++) {
+        s.ord[k] = reinterpret_cast<uint32_t *>(p);
+        p += (size_t)nmax * 4;
+    }
+    for (int k = 0; k < 6; k++) {
+        s.lb[k] = reinterpret_cast<float *>(p);
+        p += (size_t)nmax * 4;
+    }
+    for (int k = 0; k < 6; k++) {
+        s.rb[k] = reinterpret_cast<float *>(p);
+        p += (size_t)nmax * 4;
+    }
+    s.lc = reinterpret_cast<uint32_t *>(p);
+    p += (size_t)nmax * 4;
+    s.rc = reinterpret_cast<uint32_t *>(p);
+    p += (size_t)nmax * 4;
+    s.flag = reinterpret_cast<uint32_t *>(p);
+    return s;
+}
+
+// sort.SliceStable by barycenter component: bitonic sort of (key, input
+// position), so equal keys keep their input order.
+__device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
+                                 uint32_t *out, const Scratch &s) {
+    uint32_t P = pow2_at_least(n);
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        if (i < n) {
+            s.skey[i] = dbl_key(bary(aux[in[i]], axis));
+        } else {
+            s.skey[i] = ~0ULL;
+        }
+        s.sval[i] = i;
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                uint32_t l = i ^ j;
+                if (l > i) {
+                    unsigned long long ki = s.skey[i], kl = s.skey[l];
+                    uint32_t vi = s.sval[i], vl = s.sval[l];
+                    bool gt = ki > kl || (ki == kl && vi > vl);
+                    bool asc = (i & k) == 0;
+                    if (asc == gt) {
+                        s.skey[i] = kl;
+                        s.skey[l] = ki;
+                        s.sval[i] = vl;
+                        s.sval[l] = vi;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = in[s.sval[i]];
+    __syncthreads();
+}
+
+struct SahResult {
+    double cost;
+    uint32_t split;  // 0: not splitting is cheapest
+    float llo[3], lhi[3], rlo[3], rhi[3];
+};
+
+// minCost (phr.go:414-459) over the order `ord`.
+__device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n, const float *clo,
+                              const float *chi, const Scratch &s, BoxAgg *s_tmp, BoxAgg *s_rank, double *s_cost,
+                              uint32_t *s_idx) {
+    const int t = threadIdx.x;
+    const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = min(n, t * chunk), b = min(n, a + chunk);
+    // forward: exclusive prefix (union, count) -> left box/count at position i
+    BoxAgg loc = agg_identity();
+    for (uint32_t i = a; i < b; i++) {
+        const AuxNode &x = aux[ord[i]];
+        BoxAgg e;
+        for (int k = 0; k < 3; k++) { e.lo[k] = x.lo[k]; e.hi[k] = x.hi[k]; }
+        e.c = x.size;
+        loc = agg_join(loc, e);
+    }
+    BoxAgg run = block_scan_agg(loc, t, s_tmp, s_rank);
+    for (uint32_t i = a; i < b; i++) {
+        for (int k = 0; k < 3; k++) { s.lb[k][i] = run.lo[k]; s.lb[3 + k][i] = run.hi[k]; }
+        s.lc[i] = run.c;
+        const AuxNode &x = aux[ord[i]];
+        BoxAgg e;
+        for (int k = 0; k < 3; k++) { e.lo[k] = x.lo[k]; e.hi[k] = x.hi[k]; }
+        e.c = x.size;
+        run = agg_join(run, e);
+    }
+    // backward: inclusive suffix from position i to the end -> right box/count
+    BoxAgg suf = block_scan_agg(loc, (int)blockDim.x - 1 - t, s_tmp, s_rank);
+    for (uint32_t i = b; i > a; i--) {
+        const AuxNode &x = aux[ord[i - 1]];
+        BoxAgg e;
+        for (int k = 0; k < 3; k++) { e.lo[k] = x.lo[k]; e.hi[k] = x.hi[k]; }
+        e.c = x.size;
+        suf = agg_join(suf, e);
+        for (int k = 0; k < 3; k++) { s.rb[k][i - 1] = suf.lo[k]; s.rb[3 + k][i - 1] = suf.hi[k]; }
+        s.rc[i - 1] = suf.c;
+    }
+    __syncthreads();
+    // costs for every split position, first minimum wins
+    double best = INFINITY;
+    uint32_t bi = 0xffffffffu;
+    for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
+        float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
+        float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
+        double rcost = __dmul_rn(surface(rl, rh), (double)s.rc[i]);
+        double cost = __dadd_rn(rcost, __dmul_rn(surface(ll, lh), (double)s.lc[i]));
+        if (cost < best || (cost == best && i < bi)) {
+            best = cost;
+            bi = i;
+        }
+    }
+    s_cost[t] = best;
+    s_idx[t] = bi;
+    __syncthreads();
+    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+        if (t < off) {
+            double c2 = s_cost[t + off];
+            uint32_t i2 = s_idx[t + off];
+            if (c2 < s_cost[t] || (c2 == s_cost[t] && i2 < s_idx[t])) {
+                s_cost[t] = c2;
+                s_idx[t] = i2;
+            }
+        }
+        __syncthreads();
+    }
+    SahResult r;
+    uint32_t total = s.rc[0];
+    double nosplit = __dmul_rn(surface(clo, chi), (double)total);
+    double bc = s_cost[0];
+    uint32_t bidx = s_idx[0];
+    __syncthreads();
+    if (n > 1 && bc < nosplit) {
+        r.cost = bc;
+        r.split = bidx;
+        for (int k = 0; k < 3; k++) {
+            r.llo[k] = s.lb[k][bidx];
+            r.lhi[k] = s.lb[3 + k][bidx];
+            r.rlo[k] = s.rb[k][bidx];
+            r.rhi[k] = s.rb[3 + k][bidx];
+        }
+    } else {
+        r.cost = nosplit;
+        r.split = 0;
+        for (int k = 0; k < 3; k++) {
+            r.llo[k] = clo[k];
+            r.lhi[k] = chi[k];
+            r.rlo[k] = 0.f;
+            r.rhi[k] = 0.f;
+        }
+    }
+    return r;
+}
+
+struct Cut {  // a cut inside a job: a node list in the output pool, or a finished leaf
+    uint32_t off, n;
+    const uint32_t *src;
+    float lo[3], hi[3];
+    int32_t depth;
+    int32_t leaf;  // >= 0: the PNode of a leaf made from this cut
+};
+
+// Block-cooperative copy of `count` records; ranges outside [0, n) are skipped
+// and reported (they would mean an inconsistent tree).
+__device__ void copy_records(const float4 *__restrict__ src, float4 *__restrict__ dst, uint32_t from, uint32_t count,
+                             uint32_t to, uint32_t n, unsigned int *err) {
+    if ((uint64_t)from + count > n || (uint64_t)to + count > n) {
+        if (threadIdx.x == 0) atomicOr(err, GBT_DEVERR_BOUNDS);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < 3 * count; i += blockDim.x) dst[3 * (size_t)to + i] = src[3 * (size_t)from + i];
+}
+
+struct LevelArgs {
+    const AuxNode *aux;
+    const float4 *aux_recs;
+    float4 *recs;
+    PNode *pn;
+    const double *thr;
+    const PJob *jobs_in;
+    PJob *jobs_out;
+    const uint32_t *pool_in;
+    uint32_t *pool_out;
+    PhrGlobals *g;
+    int parity;
+    uint32_t pool_cap, job_cap, pnode_cap, nmax;
+    unsigned char *scratch;
+    size_t scratch_per_block;
+    int bf;
+    uint32_t n_prim;
+    unsigned int *err;
+};
+
+__device__ int32_t new_pnode(PhrGlobals *g, uint32_t cap, unsigned int *err) {
+    uint32_t id = atomicAdd(&g->pnode_ctr, 1u);
+    if (id >= cap) {
+        atomicOr(err, GBT_DEVERR_CAPACITY);
+        return -1;
+    }
+    return (int32_t)id;
+}
+
+__device__ void attach(const LevelArgs &A, int32_t parent, int32_t slot, int32_t child) {
+    if (parent < 0) A.g->root = child;
+    else A.pn[parent].child[slot] = child;
+}
+
+__global__ void __launch_bounds__(PT) k_phr_level(LevelArgs A) {
+    __shared__ BoxAgg s_tmp[PT / 32];
+    __shared__ BoxAgg s_rank[PT];
+    __shared__ double s_cost[PT];
+    __shared__ uint32_t s_idx[PT];
+    __shared__ uint32_t s_u[32];
+    __shared__ Cut s_cuts[4];
+    __shared__ int32_t s_branch, s_ncuts;
+    __shared__ uint32_t s_off;
+    const int in = A.parity, out = A.parity ^ 1;
+    const uint32_t n_jobs = A.g->job_ctr[in];
+    Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.nmax);
+    for (uint32_t j = blockIdx.x; j < n_jobs; j += gridDim.x) {
+        const PJob job = A.jobs_in[j];
+        if (job.n > A.nmax) {
+            if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            continue;
+        }
+        if (job.n <= 1) {  // only the root job when the auxiliary root is a leaf
+            if (threadIdx.x == 0) {
+                uint32_t id = A.pool_in[job.off];
+                const AuxNode &a = A.aux[id];
+                int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
+                if (p >= 0) {
+                    uint32_t ro = atomicAdd(&A.g->rec_ctr, a.count);
+                    PNode &q = A.pn[p];
+                    for (int k = 0; k < 3; k++) { q.lo[k] = a.lo[k]; q.hi[k] = a.hi[k]; }
+                    q.leaf = 1;
+                    q.nchild = 0;
+                    q.rec_off = ro;
+                    q.rec_cnt = a.count;
+                    attach(A, job.parent, job.slot, p);
+                    s_off = ro;
+                    s_u[0] = a.first;
+                    s_u[1] = a.count;
+                }
+            }
+            __syncthreads();
+            copy_records(A.aux_recs, A.recs, s_u[0], s_u[1], s_off, A.n_prim, A.err);
+            __syncthreads();
+            continue;
+        }
+        if (threadIdx.x == 0) {
+            int32_t b = new_pnode(A.g, A.pnode_cap, A.err);
+            s_branch = b;
+            if (b >= 0) {
+                PNode &q = A.pn[b];
+                for (int k = 0; k < 3; k++) { q.lo[k] = job.lo[k]; q.hi[k] = job.hi[k]; }
+                q.leaf = 0;
+                q.nchild = 0;
+                attach(A, job.parent, job.slot, b);
+            }
+            Cut c0;
+            c0.off = job.off;
+            c0.n = job.n;
+            c0.src = A.pool_in + job.off;
+            for (int k = 0; k < 3; k++) { c0.lo[k] = job.lo[k]; c0.hi[k] = job.hi[k]; }
+            c0.depth = job.depth;
+            c0.leaf = -1;
+            s_cuts[0] = c0;
+            s_ncuts = 1;
+        }
+        __syncthreads();
+        if (s_branch < 0) continue;
+        // buildSubTree's loop: split the largest cut until BranchingFactor cuts
+        while (s_ncuts < A.bf) {
+            int nc = s_ncuts, mi = 0;
+            uint32_t mx = 0;
+            for (int i = 0; i < nc; i++)
+                if (s_cuts[i].n > mx) { mx = s_cuts[i].n; mi = i; }
+            if (mx <= 1) break;
+            const Cut cut = s_cuts[mi];
+            const uint32_t n = cut.n;
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
+            __syncthreads();
+            // SweepSAH: x from the cut order, y from the x order
+            stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
+            stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+            SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+            SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+            SahResult win;
+            int warr;
+            if (xs.cost < ys.cost) {  // z from the y order
+                stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
+                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+                if (xs.cost < zs.cost) { win = xs; warr = 0; }
+                else { win = zs; warr = 2; }
+            } else {  // z from the x order
+                stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
+                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+                if (ys.cost < zs.cost) { win = ys; warr = 1; }
+                else { win = zs; warr = 2; }
+            }
+            const uint32_t *ord = S.ord[warr];
+            if (win.split == 0) {
+                // makeLeaf(left.bounding, left.nodes...) over the winning order
+                uint32_t loc = 0;
+                const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
+                const uint32_t a = min(n, threadIdx.x * chunk), b = min(n, a + chunk);
+                for (uint32_t i = a; i < b; i++) loc += A.aux[ord[i]].count;
+                uint32_t tot;
+                uint32_t ex = block_scan_u32(loc, s_u, &tot);
+                for (uint32_t i = a; i < b; i++) {
+                    S.flag[i] = ex;
+                    ex += A.aux[ord[i]].count;
+                }
+                if (threadIdx.x == 0) {
+                    int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
+                    s_off = atomicAdd(&A.g->rec_ctr, tot);
+                    if (p >= 0) {
+                        PNode &q = A.pn[p];
+                        for (int k = 0; k < 3; k++) { q.lo[k] = win.llo[k]; q.hi[k] = win.lhi[k]; }
+                        q.leaf = 1;
+                        q.nchild = 0;
+                        q.rec_off = s_off;
+                        q.rec_cnt = tot;
+                    }
+                    Cut c;
+                    c.n = 1;
+                    c.leaf = p;
+                    s_cuts[mi] = c;
+                }
+                __syncthreads();
+                for (uint32_t i = 0; i < n; i++) {
+                    const AuxNode &x = A.aux[ord[i]];
+                    copy_records(A.aux_recs, A.recs, x.first, x.count, s_off + S.flag[i], A.n_prim, A.err);
+                }
+                __syncthreads();
+                continue;
+            }
+            // refined(left), refined(right)
+            const uint32_t ns[2] = {win.split, n - win.split};
+            const uint32_t *srcs[2] = {ord, ord + win.split};
+            const double thr = A.thr[min(cut.depth, DEPTH_TABLE - 1)];
+            if (cut.depth >= DEPTH_TABLE - 1 && threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            for (int side = 0; side < 2; side++) {
+                const uint32_t m = ns[side];
+                const uint32_t *sr = srcs[side];
+                const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
+                const uint32_t a = min(m, threadIdx.x * chunk), b = min(m, a + chunk);
+                uint32_t loc = 0;
+                for (uint32_t i = a; i < b; i++) {
+                    const AuxNode &x = A.aux[sr[i]];
+                    bool keep = x.c0 < 0 || surface(x.lo, x.hi) < thr;
+                    S.flag[i] = keep ? 1u : 2u;
+                    loc += S.flag[i];
+                }
+                uint32_t tot;
+                uint32_t ex = block_scan_u32(loc, s_u, &tot);
+                const float *blo = side ? win.rlo : win.llo, *bhi = side ? win.rhi : win.lhi;
+                if (tot == 1) {  // a one-node cut becomes a leaf of everything below it
+                    if (threadIdx.x == 0) {
+                        const AuxNode &x = A.aux[sr[0]];
+                        int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
+                        s_off = atomicAdd(&A.g->rec_ctr, x.count);
+                        s_u[8] = x.first;
+                        s_u[9] = x.count;
+                        if (p >= 0) {
+                            PNode &q = A.pn[p];
+                            for (int k = 0; k < 3; k++) { q.lo[k] = blo[k]; q.hi[k] = bhi[k]; }
+                            q.leaf = 1;
+                            q.nchild = 0;
+                            q.rec_off = s_off;
+                            q.rec_cnt = x.count;
+                        }
+                        Cut c;
+                        c.n = 1;
+                        c.leaf = p;
+                        s_cuts[side == 0 ? mi : s_ncuts] = c;
+                    }
+                    __syncthreads();
+                    copy_records(A.aux_recs, A.recs, s_u[8], s_u[9], s_off, A.n_prim, A.err);
+                } else {
+                    if (threadIdx.x == 0) {
+                        uint32_t o = atomicAdd(&A.g->pool_ctr[out], tot);
+                        if (o + tot > A.pool_cap) {
+                            atomicOr(A.err, GBT_DEVERR_CAPACITY);
+                            o = 0xffffffffu;
+                        }
+                        s_off = o;
+                    }
+                    __syncthreads();
+                    const uint32_t o = s_off;
+                    if (o != 0xffffffffu) {
+                        for (uint32_t i = a; i < b; i++) {
+                            const AuxNode &x = A.aux[sr[i]];
+                            if (S.flag[i] == 1u) {
+                                A.pool_out[o + ex] = sr[i];
+                                ex += 1;
+                            } else {
+                                A.pool_out[o + ex] = (uint32_t)x.c0;
+                                A.pool_out[o + ex + 1] = (uint32_t)x.c1;
+                                ex += 2;
+                            }
+                        }
+                    }
+                    if (threadIdx.x == 0) {
+                        Cut c;
+                        c.off = o == 0xffffffffu ? 0 : o;
+                        c.n = o == 0xffffffffu ? 1 : tot;
+                        c.src = A.pool_out + c.off;
+                        for (int k = 0; k < 3; k++) { c.lo[k] = blo[k]; c.hi[k] = bhi[k]; }
+                        c.depth = cut.depth + 1;
+                        c.leaf = o == 0xffffffffu ? -2 : -1;
+                        s_cuts[side == 0 ? mi : s_ncuts] = c;
+                    }
+                }
+                __syncthreads();
+            }
+            if (threadIdx.x == 0) s_ncuts = s_ncuts + 1;
+            __syncthreads();
+        }
+        // the branch and its children
+        if (threadIdx.x == 0) {
+            const int32_t b = s_branch;
+            const int nc = s_ncuts;
+            A.pn[b].nchild = nc;
+            for (int i = 0; i < nc; i++) {
+                const Cut &c = s_cuts[i];
+                if (c.leaf >= 0) {
+                    A.pn[b].child[i] = c.leaf;
+                } else if (c.leaf == -1) {
+                    uint32_t q = atomicAdd(&A.g->job_ctr[out], 1u);
+                    if (q >= A.job_cap) {
+                        atomicOr(A.err, GBT_DEVERR_CAPACITY);
+                        continue;
+                    }
+                    PJob nj;
+                    nj.off = c.off;
+                    nj.n = c.n;
+                    for (int k = 0; k < 3; k++) { nj.lo[k] = c.lo[k]; nj.hi[k] = c.hi[k]; }
+                    nj.depth = c.depth;
+                    nj.parent = b;
+                    nj.slot = i;
+                    nj.pad = 0;
+                    A.jobs_out[q] = nj;
+                    atomicMax(&A.g->max_n[out], c.n);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// traversal nodes
+// ---------------------------------------------------------------------------
+__global__ void k_phr_finalize(const PNode *__restrict__ pn, const PhrGlobals *__restrict__ g, float4 *nodes, int arity,
+                               BvhHeader *hdr, uint32_t n_prim, unsigned int *err) {
+    const uint32_t count = g->pnode_ctr;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        if (g->root < 0 || (uint32_t)g->root >= count) {
+            atomicOr(err, GBT_DEVERR_BOUNDS);
+            return;
+        }
+        const PNode &r = pn[g->root];
+        hdr->root_ref = r.leaf ? (int32_t)r.rec_off : g->root;
+        hdr->root_cnt = r.leaf ? (int32_t)r.rec_cnt : 0;
+        for (int k = 0; k < 3; k++) {
+            hdr->root_lo[k] = r.lo[k];
+            hdr->root_hi[k] = r.hi[k];
+        }
+        hdr->root_lo[3] = hdr->root_hi[3] = 0.f;
+        hdr->n_nodes = count;
+        hdr->n_unique = 0;
+        hdr->sorted_sel = 0;
+    }
+    if (i >= count) return;
+    const PNode &b = pn[i];
+    if (b.leaf) return;
+    float lo[4][3], hi[4][3];
+    int32_t ref[4], cnt[4];
+    for (int c = 0; c < 4; c++) {
+        const int32_t ci = c < b.nchild ? b.child[c] : -1;
+        if (c < b.nchild && (ci < 0 || (uint32_t)ci >= count)) atomicOr(err, GBT_DEVERR_BOUNDS);
+        if (c < b.nchild && ci >= 0 && (uint32_t)ci < count) {
+            const PNode &ch = pn[ci];
+            for (int k = 0; k < 3; k++) { lo[c][k] = ch.lo[k]; hi[c][k] = ch.hi[k]; }
+            ref[c] = ch.leaf ? (int32_t)ch.rec_off : b.child[c];
+            cnt[c] = ch.leaf ? (int32_t)ch.rec_cnt : 0;
+        } else {
+            for (int k = 0; k < 3; k++) { lo[c][k] = INFINITY; hi[c][k] = -INFINITY; }
+            ref[c] = 0;
+            cnt[c] = -1;
+        }
+    }
+    if (arity == 2) {
+        float4 *nd = nodes + 4 * (size_t)i;
+        nd[0] = make_float4(lo[0][0], hi[0][0], lo[0][1], hi[0][1]);
+        nd[1] = make_float4(lo[1][0], hi[1][0], lo[1][1], hi[1][1]);
+        nd[2] = make_float4(lo[0][2], hi[0][2], lo[1][2], hi[1][2]);
+        reinterpret_cast<int4 *>(nd)[3] = make_int4(ref[0], cnt[0], ref[1], cnt[1]);
+    } else {
+        float4 *nd = nodes + 8 * (size_t)i;
+        nd[0] = make_float4(lo[0][0], lo[1][0], lo[2][0], lo[3][0]);
+        nd[1] = make_float4(hi[0][0], hi[1][0], hi[2][0], hi[3][0]);
+        nd[2] = make_float4(lo[0][1], lo[1][1], lo[2][1], lo[3][1]);
+        nd[3] = make_float4(hi[0][1], hi[1][1], hi[2][1], hi[3][1]);
+        nd[4] = make_float4(lo[0][2], lo[1][2], lo[2][2], lo[3][2]);
+        nd[5] = make_float4(hi[0][2], hi[1][2], hi[2][2], hi[3][2]);
+        reinterpret_cast<int4 *>(nd)[6] = make_int4(ref[0], ref[1], ref[2], ref[3]);
+        reinterpret_cast<int4 *>(nd)[7] = make_int4(cnt[0], cnt[1], cnt[2], cnt[3]);
+    }
+    (void)n_prim;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+template <class T>
+static int palloc(gbt_ctx *ctx, T **p, size_t count, std::vector<void *> &owned) {
+    *p = nullptr;
+    if (cudaMalloc(reinterpret_cast<void **>(p), (count ? count : 1) * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ENOMEM, "phr: device allocation of " + std::to_string(count * sizeof(T)) + " bytes");
+    }
+    owned.push_back(*p);
+    return GBT_OK;
+}
+
 int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, gbt_bvh *out) {
-    (void)aux; (void)alpha; (void)delta; (void)bf; (void)out;
-    return gbt_fail(ctx, GBT_EUNSUPPORTED, "phr_build: not built yet");
+    cudaStream_t st = ctx->stream;
+    BvhHeader h;
+    GBT_CUDA(ctx, cudaMemcpyAsync(&h, aux->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    const uint32_t U = h.n_unique, N = aux->n_prim;
+    const uint32_t n_aux = U > 0 ? 2 * U - 1 : 1;
+    std::vector<void *> tmp;  // freed at the end
+    int rc = GBT_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        for (void *p : tmp) cudaFree(p);
+    };
+    // outputs
+    out->n_prim = N;
+    const size_t per_node = bf == 2 ? 4 : 8;
+    const uint32_t pnode_cap = 2 * n_aux + 2;
+    if (cudaMalloc(&out->d_prims, (size_t)N * 3 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&out->d_nodes, (size_t)pnode_cap * per_node * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&out->d_hdr, sizeof(BvhHeader)) != cudaSuccess) {
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
+    }
+    out->node_cap = pnode_cap;
+    AuxNode *d_aux;
+    PNode *d_pn;
+    PhrGlobals *d_g;
+    uint32_t *d_front[2], *d_pool[2];
+    PJob *d_jobs[2];
+    double *d_thr;
+    const uint32_t pool_cap = 3 * n_aux + 4096, job_cap = n_aux + 16;
+    if (!rc) rc = palloc(ctx, &d_aux, n_aux, tmp);
+    if (!rc) rc = palloc(ctx, &d_pn, pnode_cap, tmp);
+    if (!rc) rc = palloc(ctx, &d_g, 1, tmp);
+    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_front[i], 2 * (size_t)n_aux + 2, tmp);
+    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_pool[i], pool_cap, tmp);
+    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_jobs[i], job_cap, tmp);
+    if (!rc) rc = palloc(ctx, &d_thr, DEPTH_TABLE, tmp);
+    if (rc) { cleanup(); return rc; }
+    // DefaultThreshold table (phr.go:356-358), host float64
+    double S;
+    {
+        const float *lo = h.root_lo, *hi = h.root_hi;
+        double w = (double)hi[0] - (double)lo[0], hh = (double)hi[1] - (double)lo[1], d = (double)hi[2] - (double)lo[2];
+        S = 2 * w * hh + 2 * w * d + 2 * hh * d;
+    }
+    std::vector<double> thr(DEPTH_TABLE);
+    for (int d = 0; d < DEPTH_TABLE; d++) thr[d] = S / std::pow(2.0, alpha * (double)d + delta);
+    GBT_CUDA(ctx, cudaMemcpyAsync(d_thr, thr.data(), DEPTH_TABLE * sizeof(double), cudaMemcpyHostToDevice, st));
+    GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, sizeof(PhrGlobals), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0xff, offsetof(PhrGlobals, pad), st));  // counters 0, root -1 below
+    GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, offsetof(PhrGlobals, root), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(d_pn, 0, (size_t)pnode_cap * sizeof(PNode), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(d_aux, 0, (size_t)n_aux * sizeof(AuxNode), st));
+    k_aux_build<<<(U + 255) / 256 + 1, 256, 0, st>>>(aux->d_hdr, aux->d_nodes, aux->d_size, aux->d_range, aux->d_run,
+                                                     d_aux, U, N);
+    const int32_t root = h.root_cnt > 0 ? 0 : h.root_ref;
+    k_initial_cut<<<1, 1024, 0, st>>>(d_aux, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
+    GBT_CUDA(ctx, cudaGetLastError());
+    PhrGlobals g;
+    GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    uint32_t n_jobs = g.job_ctr[0], nmax = g.max_n[0];
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int parity = 0;
+    const int max_grid = ctx->num_sms * 4;
+    int levels = 0;
+    while (n_jobs > 0) {
+        uint32_t grid = std::min<uint32_t>(n_jobs, (uint32_t)max_grid);
+        size_t per_block = gbt_align(scratch_bytes_for(nmax));
+        size_t need = per_block * grid;
+        if (need > scratch_bytes) {
+            if (scratch) {
+                cudaStreamSynchronize(st);
+                cudaFree(scratch);
+            }
+            if (cudaMalloc(&scratch, need) != cudaSuccess) {
+                cudaGetLastError();
+                cleanup();
+                return gbt_fail(ctx, GBT_ENOMEM, "phr: scratch");
+            }
+            scratch_bytes = need;
+        }
+        const int o = parity ^ 1;
+        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, job_ctr) + o * 4, 0, 4, st));
+        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, pool_ctr) + o * 4, 0, 4, st));
+        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, max_n) + o * 4, 0, 4, st));
+        LevelArgs A;
+        A.aux = d_aux;
+        A.aux_recs = aux->d_prims;
+        A.recs = out->d_prims;
+        A.pn = d_pn;
+        A.thr = d_thr;
+        A.jobs_in = d_jobs[parity];
+        A.jobs_out = d_jobs[o];
+        A.pool_in = d_pool[parity];
+        A.pool_out = d_pool[o];
+        A.g = d_g;
+        A.parity = parity;
+        A.pool_cap = pool_cap;
+        A.job_cap = job_cap;
+        A.pnode_cap = pnode_cap;
+        A.nmax = nmax;
+        A.scratch = static_cast<unsigned char *>(scratch);
+        A.scratch_per_block = per_block;
+        A.bf = bf;
+        A.n_prim = N;
+        A.err = ctx->d_error;
+        k_phr_level<<<grid, PT, 0, st>>>(A);
+        GBT_CUDA(ctx, cudaGetLastError());
+        GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
+        GBT_CUDA(ctx, cudaStreamSynchronize(st));
+        unsigned int flags = 0;
+        GBT_CUDA(ctx, cudaMemcpy(&flags, ctx->d_error, sizeof(flags), cudaMemcpyDeviceToHost));
+        if (flags) break;  // reported by the caller's device-error check
+        n_jobs = g.job_ctr[o];
+        nmax = g.max_n[o];
+        parity = o;
+        levels++;
+    }
+    k_phr_finalize<<<(pnode_cap + 255) / 256, 256, 0, st>>>(d_pn, d_g, out->d_nodes, bf == 2 ? 2 : 4, out->d_hdr, N,
+                                                            ctx->d_error);
+    GBT_CUDA(ctx, cudaGetLastError());
+    GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    out->n_nodes_host = g.pnode_ctr;
+    if (scratch) cudaFree(scratch);
+    cleanup();
+    return GBT_OK;
 }

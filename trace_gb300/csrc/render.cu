@@ -231,7 +231,6 @@ struct RenderState {
     float4 *rays[2], *aux[2];
     float4 *hits;
     uint32_t *counts;     // per level
-    unsigned long long *total;
     float *acc;
 };
 
@@ -273,7 +272,6 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
     rs.aux[1] = reinterpret_cast<float4 *>(b + off[3]);
     rs.hits = reinterpret_cast<float4 *>(b + off[4]);
     rs.counts = reinterpret_cast<uint32_t *>(b + off[5]);
-    rs.total = reinterpret_cast<unsigned long long *>(b + off[6]);
     rs.acc = reinterpret_cast<float *>(b + off[7]);
 
     cudaStream_t st = ctx->stream;
@@ -293,24 +291,33 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
     const int levels = p->max_depth + 2;  // surfaces at depth 0..MaxDepth+1 are traced
 
     GBT_CUDA(ctx, cudaMemsetAsync(rs.acc, 0, npix * 3 * sizeof(float), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(rs.total, 0, sizeof(unsigned long long), st));
+    uint64_t launches = 0, trav = 0;
+    unsigned long long *ctr = ctx->profiling >= 2 ? ctx->d_counters : nullptr;
     for (size_t g0 = 0; g0 < total; g0 += cap) {
         uint32_t count = (uint32_t)((total - g0) < cap ? (total - g0) : cap);
         GBT_CUDA(ctx, cudaMemsetAsync(rs.counts, 0, 64 * sizeof(uint32_t), st));
         uint32_t blocks = (count + 255) / 256;
         k_raygen<<<blocks, 256, 0, st>>>(cf, sp, (uint32_t)g0, count, rs.rays[0], rs.aux[0], rs.counts);
+        launches++;
         for (int lv = 0; lv < levels; lv++) {
             int a = lv & 1;
-            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st);
+            gbt_prof_begin(ctx);
+            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr);
+            gbt_prof_end(ctx);
             k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],
                                             rs.aux[a ^ 1], rs.counts + lv + 1, bvh->d_prims, sc->d_prim_mat, sc->d_mats,
                                             sc->d_normals, rs.acc, (uint32_t)cap);
+            launches += 2;
+            trav++;
         }
-        k_sum_counts<<<1, 32, 0, st>>>(rs.counts, levels, rs.total);
+        k_sum_counts<<<1, 32, 0, st>>>(rs.counts, levels, ctx->d_counters + 2);
+        launches++;
     }
     k_resolve<<<(uint32_t)((npix * 3 + 255) / 256), 256, 0, st>>>(rs.acc, d_rgb, (uint32_t)(npix * 3), 1.0f / p->spp);
+    launches++;
     GBT_CUDA(ctx, cudaGetLastError());
-    ctx->last_stats.paths = total;
-    ctx->d_ray_total = rs.total;
+    ctx->last_stats.paths += total;
+    ctx->last_stats.kernel_launches += launches;
+    ctx->last_stats.traverse_launches += trav;
     return GBT_OK;
 }

@@ -117,9 +117,15 @@ __device__ __forceinline__ void leaf(const float4 *__restrict__ recs, int first,
     for (int s = first; s < first + cnt; ++s) test_record(recs, s, r, h);
 }
 
-template <int STACK>
+// Per-thread traversal work counters (profiling level 2).
+struct Work {
+    uint32_t nodes = 0, prims = 0;
+};
+
+template <int STACK, bool COUNT = false>
 __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *__restrict__ nodes,
-                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err) {
+                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
+                                            Work *work = nullptr) {
     Hit h;
     h.t = r.tmax;
     h.u = h.v = 0.f;
@@ -133,6 +139,7 @@ __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *
     int2 cur = make_int2(hdr.root_ref, hdr.root_cnt);
     for (;;) {
         if (cur.y == 0) {
+            if (COUNT) work->nodes++;
             const float4 *nd = nodes + 4 * (size_t)cur.x;
             float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
             int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
@@ -161,6 +168,7 @@ __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *
             if (h0) { cur = make_int2(n3.x, n3.y); continue; }
             if (h1) { cur = make_int2(n3.z, n3.w); continue; }
         } else if (cur.y > 0) {
+            if (COUNT) work->prims += (uint32_t)cur.y;
             leaf(recs, cur.x, cur.y, r, h);
         }
         bool found = false;
@@ -177,9 +185,10 @@ __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *
     return h;
 }
 
-template <int STACK>
+template <int STACK, bool COUNT = false>
 __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *__restrict__ nodes,
-                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err) {
+                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
+                                            Work *work = nullptr) {
     Hit h;
     h.t = r.tmax;
     h.u = h.v = 0.f;
@@ -193,6 +202,7 @@ __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *
     int2 cur = make_int2(hdr.root_ref, hdr.root_cnt);
     for (;;) {
         if (cur.y == 0) {
+            if (COUNT) work->nodes++;
             const float4 *nd = nodes + 8 * (size_t)cur.x;
             float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
             float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
@@ -226,6 +236,7 @@ __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *
                 continue;
             }
         } else if (cur.y > 0) {
+            if (COUNT) work->prims += (uint32_t)cur.y;
             leaf(recs, cur.x, cur.y, r, h);
         }
         bool found = false;

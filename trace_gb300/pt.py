@@ -21,6 +21,7 @@ is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -46,6 +47,11 @@ class Context:
         if rc != 0:
             raise GbtError(rc, "gbt_ctx_create(device=%d) failed" % device)
         self.h = h
+        # scenes and BVHs refer to the context: they are destroyed before it
+        self._children = weakref.WeakSet()
+
+    def _adopt(self, obj):
+        self._children.add(obj)
 
     def check(self, rc, what=""):
         if rc != 0:
@@ -61,8 +67,18 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            kids = list(getattr(self, "_children", ()))
+            for k in kids:  # BVHs first, then the scenes they were built from
+                if isinstance(k, BVH):
+                    k.close()
+            for k in kids:
+                k.close()
             self.L.gbt_ctx_destroy(self.h)
             self.h = None
+
+    @property
+    def alive(self):
+        return getattr(self, "h", None) is not None
 
     def __del__(self):
         try:
@@ -114,6 +130,7 @@ class DeviceScene:
                                          len(mt), C.byref(h)), "scene_upload")
         self.h = h
         self.n_prim = n
+        ctx._adopt(self)
 
     @classmethod
     def from_dict(cls, ctx, s):
@@ -122,7 +139,8 @@ class DeviceScene:
 
     def close(self):
         if getattr(self, "h", None):
-            self.ctx.L.gbt_scene_destroy(self.h)
+            if self.ctx.alive:  # a closed context has already destroyed this scene
+                self.ctx.L.gbt_scene_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -137,10 +155,12 @@ class BVH:
 
     def __init__(self, ctx, h, scene, kind):
         self.ctx, self.h, self.scene, self.kind = ctx, h, scene, kind
+        ctx._adopt(self)
 
     def close(self):
         if getattr(self, "h", None):
-            self.ctx.L.gbt_bvh_destroy(self.h)
+            if self.ctx.alive:
+                self.ctx.L.gbt_bvh_destroy(self.h)
             self.h = None
 
     def __del__(self):
