@@ -25,11 +25,13 @@ namespace {
 template <bool COUNT>
 __device__ __forceinline__ void flush_work(const gbt_dev::Work &w, unsigned long long *counters) {
     if (!COUNT) return;
+    // every lane of the warp reaches this point (no early return in the kernels)
+    __syncwarp();
     unsigned long long a = w.nodes, b = w.prims;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(__activemask(), a, o);
-        b += __shfl_xor_sync(__activemask(), b, o);
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
     }
     if ((threadIdx.x & 31) == 0) {
         atomicAdd(counters, a);
