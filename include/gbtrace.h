@@ -138,6 +138,26 @@ int gbt_bvh_export(gbt_ctx *ctx, gbt_bvh *bvh, int8_t *kind, int32_t *count, dou
 /* LBVH only: the sorted (Morton code, primitive index) pairs (lbvh.go:216-219). */
 int gbt_lbvh_sorted(gbt_ctx *ctx, gbt_bvh *bvh, uint64_t *codes, int32_t *idx);
 
+/* The LBVH's pair sort for callers that may not allocate device memory.  No
+ * counterpart in the reference.  Some callers cannot call cudaMalloc: a plugin
+ * whose host application owns all device memory through its own pool, or a
+ * per-frame loop that cannot take cudaMalloc's implicit synchronisation.  This
+ * call sorts n 63-bit Morton codes ascending with their input positions as
+ * values (stable: equal codes keep input order), exactly as the pairs
+ * gbt_lbvh_build produces, and allocates nothing: the caller passes the device
+ * input (d_codes_in, not modified) and outputs (d_codes_out, d_idx_out, n
+ * entries each); the scratch is a fixed static device array of about 4 MiB
+ * that every GPU loading the library holds until exit, so
+ * n <= GBT_NOALLOC_MAX_PAIRS, else GBT_EINVAL.  No context is needed: work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) of the
+ * current device, and the call returns after that stream has finished.  The
+ * first call on a device looks up the array's device address, so make it
+ * before any stream capture.  All calls share the one array: calls whose work
+ * overlaps on the GPU race and corrupt each other's results. */
+#define GBT_NOALLOC_MAX_PAIRS 262144u
+int gbt_sort_morton_pairs_noalloc(void *stream, const uint64_t *d_codes_in, uint64_t *d_codes_out,
+                                  uint32_t *d_idx_out, uint32_t n);
+
 /* ---- queries -------------------------------------------------------- */
 /* Closest hit per ray (bvh.go:74-77 BVH.intersected over primitive.go:56-86
  * and :172-208), host buffers. */

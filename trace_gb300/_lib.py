@@ -24,6 +24,7 @@ EXPORTS = [
     "gbt_bvh_cost", "gbt_bvh_size", "gbt_bvh_counts", "gbt_bvh_export", "gbt_lbvh_sorted",
     "gbt_trace", "gbt_trace_async", "gbt_render", "gbt_render_async", "gbt_render_last_stats",
     "gbt_device_alloc", "gbt_device_free", "gbt_copy_h2d_async", "gbt_copy_d2h_async",
+    "gbt_sort_morton_pairs_noalloc",
 ]
 
 
@@ -97,6 +98,7 @@ def load():
         "gbt_device_free": ([P, P], C.c_int),
         "gbt_copy_h2d_async": ([P, P, P, C.c_size_t], C.c_int),
         "gbt_copy_d2h_async": ([P, P, P, C.c_size_t], C.c_int),
+        "gbt_sort_morton_pairs_noalloc": ([P, P, P, P, u32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -675,3 +675,66 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }
+
+// ---------------------------------------------------------------------------
+// pair sort into caller-given scratch (used by the entry point that allocates nothing)
+// ---------------------------------------------------------------------------
+namespace {
+
+// All eight passes, reading the caller's codes first and ping-ponging
+// out -> scratch -> out so that the sorted pairs land in the caller's output.
+__global__ void __launch_bounds__(256) k_sort_plan_all(SortPlan *plan, const uint32_t *__restrict__ ghist,
+                                                       const uint64_t *codes_in, uint64_t *kA, uint32_t *vA,
+                                                       uint64_t *kB, uint32_t *vB) {
+    __shared__ uint32_t s_tmp[8];
+    const int t = threadIdx.x;
+    for (int p = 0; p < 8; p++) plan->digit_base[p][t] = block_excl_scan256(ghist[p * 256 + t], s_tmp, nullptr);
+    if (t == 0) {
+        for (int p = 0; p < 8; p++) {
+            plan->active[p] = 1;
+            plan->identity[p] = p == 0 ? 1u : 0u;
+            const bool to_b = (p & 1) == 0;  // pass 0: in -> B, 1: B -> A, 2: A -> B, ...
+            plan->in_k[p] = p == 0 ? codes_in : (to_b ? kA : kB);
+            plan->in_v[p] = to_b ? vA : vB;
+            plan->out_k[p] = to_b ? kB : kA;
+            plan->out_v[p] = to_b ? vB : vA;
+        }
+        plan->final_k = kA;
+        plan->final_v = vA;
+        plan->final_sel = 0;
+    }
+}
+
+}  // namespace
+
+size_t gbt_sort_static_bytes(uint32_t max_pairs) {
+    SortScratch ss = sort_layout(max_pairs, 0);
+    return gbt_align(ss.total + (size_t)max_pairs * (sizeof(uint64_t) + sizeof(uint32_t)) + 256);
+}
+
+int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, uint32_t max_pairs,
+                          const uint64_t *codes_in, uint64_t *codes_out, uint32_t *idx_out, uint32_t n,
+                          unsigned int **err_word) {
+    SortScratch ss = sort_layout(n, 0);
+    SortScratch smax = sort_layout(max_pairs, 0);
+    uint64_t *kB = reinterpret_cast<uint64_t *>(sbase + smax.total);
+    uint32_t *vB = reinterpret_cast<uint32_t *>(sbase + smax.total + (size_t)max_pairs * sizeof(uint64_t));
+    unsigned int *err = reinterpret_cast<unsigned int *>(
+        sbase + gbt_align(smax.total + (size_t)max_pairs * (sizeof(uint64_t) + sizeof(uint32_t))));
+    *err_word = err;
+    SortPlan *plan = reinterpret_cast<SortPlan *>(sbase + ss.plan);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(sbase + ss.hist);
+    uint32_t *ctr = reinterpret_cast<uint32_t *>(sbase + ss.ctr);
+    uint32_t *status = reinterpret_cast<uint32_t *>(sbase + ss.status);
+    // state left by the previous call: histograms, tile counters, look-back words, error word
+    if (cudaMemsetAsync(sbase + ss.hist, 0, ss.total - ss.hist, st) != cudaSuccess) return GBT_ECUDA;
+    if (cudaMemsetAsync(err, 0, sizeof(unsigned int), st) != cudaSuccess) return GBT_ECUDA;
+    k_hist<<<num_sms * 2, 256, 0, st>>>(codes_in, n, hist);
+    k_sort_plan_all<<<1, 256, 0, st>>>(plan, hist, codes_in, codes_out, idx_out, kB, vB);
+    size_t smem = (8 * 256 + 256 + 256 + 32) * sizeof(uint32_t) + (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+    if (cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return GBT_ECUDA;
+    for (int p = 0; p < 8; p++)
+        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr, err);
+    return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_ECUDA;
+}
