@@ -207,6 +207,152 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def run_batch_workload(args):
+    """64 scenes of log-uniform size in [1k, 2M] triangles (seed 3), each a soup or
+    an fBm terrain patch, 512x512, 16 spp, depth 4: the per-scene wavefront loop
+    (gbt_render_async per scene) against one persistent launch over all scenes,
+    and that launch replayed from a CUDA graph.  Mrays/s counts every traced ray."""
+    import torch
+
+    from trace_gb300 import _lib, pt, scenes
+
+    count = args.batch_scenes
+    ctx = pt.Context(0)
+    t0 = time.perf_counter()
+    ss = scenes.batch(count=count, seed=3, width=512, height=512, spp=16, max_depth=4)
+    gen_s = time.perf_counter() - t0
+    bvhs, cams, params, tris = [], [], [], 0
+    for k, s in enumerate(ss):
+        ds = pt.DeviceScene.from_dict(ctx, s)
+        bvhs.append(pt.DefaultLBVH(ds))
+        cams.append(s["camera"])
+        p = dict(s["render"])
+        p["seed"] = 1000 + k
+        params.append(p)
+        tris += s["verts"].shape[0]
+    b = pt.Batch(ctx, bvhs, cams, params)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    st = _lib.RenderStats()
+
+    def timed(mode, steps, cfg=None):
+        for _ in range(args.warmup):
+            b.render(mode, cfg)
+        ctx.sync()
+        ctx.check(ctx.L.gbt_render_last_stats(ctx.h, C.byref(st)))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            b.render(mode, cfg)
+        e1.record(stream)
+        ctx.sync()
+        ctx.check(ctx.L.gbt_render_last_stats(ctx.h, C.byref(st)))
+        ms = e0.elapsed_time(e1) / steps
+        return ms, st.rays_traced / steps
+
+    steps = max(2, args.steps // 2)
+    ms_plain, rays_plain = timed("plain", steps)
+    plain = [b.read(i) for i in range(b.n)]
+    cfg, tune_ms = b.autotune()
+    ms_batch, rays_batch = timed("batched", steps, cfg)
+    batched = [b.read(i) for i in range(b.n)]
+    b.make_graph(rebuild=False, cfg=cfg)
+    ms_graph, rays_graph = timed("graph", steps)
+    diff = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, batched))
+    rmse = float(np.sqrt(np.mean([np.mean((x - y) ** 2) for x, y in zip(plain, batched)])))
+    line = {"metric": "Mrays/s (64-scene batch)", "unit": "Mrays/s", "workload": "batch%d_512x512_spp16_depth4" % count,
+            "triangles_total": tris, "scenes": count,
+            "plain": {"value": rays_plain / ms_plain / 1e3, "ms_per_frame": ms_plain, "rays": rays_plain},
+            "batched": {"value": rays_batch / ms_batch / 1e3, "ms_per_frame": ms_batch, "rays": rays_batch,
+                        "config": {"block": cfg.block, "fetch_min": cfg.fetch_min, "stack": cfg.stack},
+                        "autotune_best_ms": tune_ms},
+            "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},
+            "speedup_batched_vs_plain": (rays_batch / ms_batch) / (rays_plain / ms_plain),
+            "images": {"max_abs_diff_batched_vs_plain": diff, "rmse_batched_vs_plain": rmse},
+            "scene_generation_s": gen_s}
+    print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
+def run_adjoint_workload(args):
+    """Cornell-box scene with a 256x128 sphere (65,036 triangles), per-triangle albedo and
+    emission U[0.2, 0.8] (seed 4), target rendered from seed-5 parameters, 512x512,
+    64 spp, depth 5: milliseconds per forward + L2 loss + backward iteration."""
+    import torch
+
+    from trace_gb300 import pt, scenes
+
+    ctx = pt.Context(0)
+    s = scenes.cornell(sphere_u=256, sphere_v=128, width=512, height=512)
+    n = s["verts"].shape[0]
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    r4, r5 = np.random.default_rng(4), np.random.default_rng(5)
+    a0, e0 = r4.uniform(0.2, 0.8, (n, 3)).astype(np.float32), r4.uniform(0.2, 0.8, n).astype(np.float32)
+    a1, e1 = r5.uniform(0.2, 0.8, (n, 3)).astype(np.float32), r5.uniform(0.2, 0.8, n).astype(np.float32)
+    f = pt.RenderFunction(g, s["camera"], dict(width=512, height=512, spp=64, max_depth=5, miss_mode=0, seed=7))
+    f.set_target(f.Forward(a1, e1))
+    f._set(a0, e0)
+    L, h = ctx.L, ctx.h
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def iteration():
+        ctx.check(L.gbt_adjoint_forward_async(h, g.h, C.byref(f.cam), C.byref(f.params), C.c_void_p(f.d_alb),
+                                              C.c_void_p(f.d_emi), C.c_void_p(f.d_img)))
+        ctx.check(L.gbt_l2_loss_async(h, C.c_void_p(f.d_img), C.c_void_p(f.d_tgt), 512 * 512 * 3,
+                                      C.c_void_p(f.d_dimg), C.c_void_p(f.d_loss)))
+        ctx.check(L.gbt_adjoint_backward_async(h, g.h, C.byref(f.cam), C.byref(f.params), C.c_void_p(f.d_alb),
+                                               C.c_void_p(f.d_emi), C.c_void_p(f.d_dimg), C.c_void_p(f.d_ga),
+                                               C.c_void_p(f.d_ge)))
+
+    for _ in range(max(1, args.warmup)):
+        iteration()
+    ctx.sync()
+    steps = max(2, args.steps // 2)
+    e_0, e_1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_0.record(stream)
+    for _ in range(steps):
+        iteration()
+    e_1.record(stream)
+    ctx.sync()
+    ms = e_0.elapsed_time(e_1) / steps
+    line = {"metric": "adjoint ms/iter", "value": ms, "unit": "ms", "higher_is_better": False,
+            "workload": "cornell_sphere256x128_512x512_spp64_depth5", "triangles": n,
+            "parameters": n * 4, "paths_per_pass": 512 * 512 * 64, "steps": steps}
+    print(json.dumps(line), flush=True)
+    f.close()
+    return 0
+
+
+def run_profile_case(args):
+    """The benchmark's scene, without timing: a case small enough for an ncu capture
+    (about 0.3 GB on the device).  `render`: 3 frames on the chosen tree;
+    `lbvh`: 3 LBVH builds."""
+    from trace_gb300 import _lib, pt, scenes
+
+    ctx = pt.Context(0)
+    s = scenes.soup(N_TRI, seed=1, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    aux = pt.DefaultLBVH(ds)
+    if args.profile == "lbvh":
+        for _ in range(3):
+            ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
+        ctx.sync()
+        print("profile case lbvh: 3 builds of %d triangles" % N_TRI)
+        return 0
+    bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux) if args.bvh == "phr" else aux
+    ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, bvh.h, args.layout), "layout")
+    cam = pt.make_camera(s["camera"])
+    rp = _lib.RenderParams(W, H, SPP, MAX_DEPTH, pt.MISS_WHITE, (C.c_float * 3)(1, 1, 1), 7)
+    d_img = ctx.alloc(W * H * 3 * 4)
+    for _ in range(3):
+        ctx.check(ctx.L.gbt_render_async(ctx.h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+    ctx.sync()
+    ctx.free(d_img)
+    print("profile case render: 3 frames on %s" % args.bvh)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,12 +360,26 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbt", choices=["gbt", "reference"])
     ap.add_argument("--bvh", default="phr", choices=["phr", "lbvh"])
+    ap.add_argument("--layout", type=int, default=4, choices=[2, 4],
+                    help="traversal layout: the 4-wide view collapsed from the binary tree, or the binary nodes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--profile", choices=["render", "lbvh"], default=None,
+                    help="run a small fixed case for an ncu capture and exit: 3 frames (render) or 3 LBVH builds")
+    ap.add_argument("--workload", choices=["soup", "batch", "adjoint"], default="soup",
+                    help="soup: the headline 1M-triangle frame; batch: the 64-scene batched render; "
+                         "adjoint: forward+backward iteration of the differentiable render")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.profile:
+        return run_profile_case(args)
+    if args.workload == "batch":
+        return run_batch_workload(args)
+    if args.workload == "adjoint":
+        return run_adjoint_workload(args)
     args.warmup = max(args.warmup, 3)
 
     import torch
@@ -242,6 +402,7 @@ def main():
             if e.code != -6:
                 raise
     L, h = ctx.L, ctx.h
+    ctx.check(L.gbt_bvh_set_layout(h, bvh.h, args.layout), "layout")
     cam = pt.make_camera(s["camera"])
     rp = _lib.RenderParams(W, H, SPP, MAX_DEPTH, pt.MISS_WHITE, (C.c_float * 3)(1, 1, 1), 7)
     d_img = ctx.alloc(W * H * 3 * 4)
@@ -289,11 +450,13 @@ def main():
     # roofline of the traversal kernels
     hbm, peak_kind = peaks()
     rays_per_frame = count_stats["rays_traced"]
-    bytes_frame = 64 * count_stats["nodes_visited"] + 48 * count_stats["prims_tested"] + 48 * rays_per_frame
+    node_bytes = 128 if args.layout == 4 else 64
+    bytes_frame = node_bytes * count_stats["nodes_visited"] + 48 * count_stats["prims_tested"] + 48 * rays_per_frame
     trav_ms_frame = timed["ms_traverse"] / args.steps
     achieved = bytes_frame / (trav_ms_frame * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": TRAVERSAL_TRAFFIC.get(bvh_name.split("(")[0]), "kernel": "k_trace2 (closest hit)",
+            "traffic": TRAVERSAL_TRAFFIC.get(bvh_name.split("(")[0]),
+            "kernel": "k_trace4 (closest hit, 4-wide view)" if args.layout == 4 else "k_trace2 (closest hit)",
             "peak_source": peak_kind, "bytes_per_frame": bytes_frame,
             "traversal_ms_per_frame": trav_ms_frame, "traversal_share": timed["ms_traverse"] / ms,
             "nodes_per_ray": count_stats["nodes_visited"] / rays_per_frame,
@@ -343,6 +506,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
                        "max_depth": MAX_DEPTH, "miss": "white", "bvh": bvh_name,
+                       "traversal_layout": "%d-wide" % args.layout,
                        "rays_per_step": timed["rays_traced"] / args.steps,
                        "l2": "flushed before every timed step (256 MiB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},

@@ -127,6 +127,11 @@ int gbt_scene_update_async(gbt_ctx *ctx, gbt_scene *scene, const float *d_verts)
  * gbt_lbvh_build; alpha/delta/branching as NewPHRBuilder (phr.go:30-40). */
 int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out);
 int gbt_bvh_destroy(gbt_bvh *bvh);
+/* Traversal layout of a binary tree: 4 (default after gbt_lbvh_build and a
+ * branching-2 gbt_phr_build) traverses a 4-wide view collapsed from it; 2
+ * traverses the binary nodes.  Results are identical; only speed differs.
+ * gbt_lbvh_rebuild_async drops the 4-wide view.  No counterpart in the reference. */
+int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width);
 
 int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost); /* bvh.go:46-48 BVH.Cost */
 int gbt_bvh_size(gbt_ctx *ctx, gbt_bvh *bvh, int64_t *size); /* bvh.go:50-52 BVH.Size */
@@ -174,6 +179,62 @@ int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_rend
 int gbt_render_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
                      float *d_rgb);
 int gbt_render_last_stats(gbt_ctx *ctx, gbt_render_stats *stats);
+
+/* ---- batched rendering (no counterpart in the reference, which renders one
+ * scene per RenderToBuffer call, render.go:91-129) ------------------------ */
+typedef struct {
+    gbt_bvh *bvh;              /* the scene's BVH; materials and normals come from its scene */
+    gbt_camera camera;
+    gbt_render_params params;  /* this render's size, spp, depth, miss shader and seed */
+    float *d_rgb;              /* device image, width*height*3 floats */
+} gbt_batch_item;
+
+typedef struct {
+    int32_t block;     /* threads per block: 64, 128 or 256 */
+    int32_t fetch_min; /* 0: a warp refills only when all its lanes are idle; 16: when fewer than 16 are busy */
+    int32_t stack;     /* 0: traversal stack in local memory; 1: its top 8 entries in shared memory */
+} gbt_batch_config;
+
+/* All items in one persistent launch pulling (scene, path) work from a device
+ * queue; each path runs to completion in one lane.  Images equal those of
+ * gbt_render_async per item up to float summation order.  cfg NULL: the
+ * autotuned choice of this context, else block 128 / fetch_min 16 / local
+ * stack.  All BVHs must share a traversal layout (gbt_bvh_set_layout).
+ * Enqueue only; the first call may grow the context's batch state. */
+int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, const gbt_batch_config *cfg);
+/* The baseline: the same items as one gbt_render_async per item. */
+int gbt_render_batch_plain_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n);
+/* Times every configuration on these items (one warm frame, best of two
+ * timed frames), keeps the fastest for this context and returns it. */
+int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, gbt_batch_config *best,
+                       double *best_ms);
+/* A CUDA graph of one batched frame: optionally the in-place LBVH rebuild of
+ * every item (which switches their traversal to the binary nodes), then the
+ * accumulator clear, the persistent launch and the resolve.  Items, outputs
+ * and BVHs must outlive the graph. */
+typedef struct gbt_graph gbt_graph;
+int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, const gbt_batch_config *cfg,
+                           int32_t rebuild_lbvh, gbt_graph **out);
+int gbt_graph_launch(gbt_ctx *ctx, gbt_graph *graph); /* enqueue one replay */
+int gbt_graph_destroy(gbt_graph *graph);
+
+/* ---- differentiable rendering (no counterpart in the reference) -------
+ * Material model of these calls: every triangle t emits e_t (white, d_emission
+ * n_tri floats) and scatters diffusely with albedo a_t (d_albedo n_tri*3),
+ * with the camera, sampling, Diffuse scatter and MaxDepth semantics of
+ * gbt_render (render.go:91-129, 209-224).  Triangle scenes only, max_depth <= 14.
+ * The forward image is bitwise reproducible (each pixel sums its paths in a
+ * fixed order); the backward pass re-traces the same paths from their random
+ * counters (path replay) and accumulates dLoss/d(albedo, emission) given
+ * dLoss/dImage.  All device buffers; enqueue only. */
+int gbt_adjoint_forward_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+                              const float *d_albedo, const float *d_emission, float *d_img);
+int gbt_adjoint_backward_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+                               const float *d_albedo, const float *d_emission, const float *d_dimg,
+                               float *d_grad_albedo, float *d_grad_emission);
+/* loss = sum((img - target)^2) in float64 into *d_loss; d_dimg = 2 (img - target). */
+int gbt_l2_loss_async(gbt_ctx *ctx, const float *d_img, const float *d_target, uint32_t n, float *d_dimg,
+                      double *d_loss);
 
 /* ---- device memory helpers for callers without a CUDA runtime ------- */
 int gbt_device_alloc(gbt_ctx *ctx, size_t bytes, void **d_ptr);

@@ -1054,6 +1054,166 @@ int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_typ
 }
 
 /* ------------------------------------------------------------------------ */
+/* float64 adjoint with the GPU's random numbers                             */
+/* ------------------------------------------------------------------------ */
+/* Philox-2x32-10 (Salmon et al., SC'11), as the device code uses it */
+static void philox2x32(uint32_t c0, uint32_t c1, uint32_t key, uint32_t out[2]) {
+    for (int i = 0; i < 10; i++) {
+        uint64_t prod = (uint64_t)0xD256D193u * c0;
+        uint32_t hi = (uint32_t)(prod >> 32), lo = (uint32_t)prod;
+        c0 = hi ^ key ^ c1;
+        c1 = lo;
+        key += 0x9E3779B9u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+}
+static double u01_24(uint32_t x) { return (double)(x >> 8) * (1.0 / 16777216.0); }
+
+typedef struct { int tri; v3 P, a; } adj_vertex;
+
+typedef struct {
+    const orc_bvh *b;
+    const orc_render_desc *rd;
+    ocam cam;
+    const float *albedo, *emission, *dimg;
+    double *img, *ga, *ge;
+    pthread_mutex_t lock;
+} adj_ctx;
+
+/* one path: vertices, radiance L and the miss colour after the last vertex */
+static int adj_path(const adj_ctx *x, uint32_t g, adj_vertex *vx, int maxv, v3 *L, v3 *miss) {
+    const orc_render_desc *rd = x->rd;
+    uint32_t npix = (uint32_t)rd->width * (uint32_t)rd->height, key = (uint32_t)rd->seed ^ (uint32_t)(rd->seed >> 32);
+    uint32_t pix = g % npix, px = pix % (uint32_t)rd->width, py = pix / (uint32_t)rd->width;
+    uint32_t rnd[2];
+    philox2x32(g, 0xFFFFu, key, rnd);
+    double s = ((double)px + u01_24(rnd[0])) / (double)(rd->width - 1);
+    double t = ((double)py + u01_24(rnd[1])) / (double)(rd->height - 1);
+    oray r = make_ray(x->cam.origin, cam_dir(&x->cam, s, t));
+    double tmin = 0.001;
+    v3 T = mk(1, 1, 1);
+    *L = mk(0, 0, 0);
+    *miss = mk(0, 0, 0);
+    int nv = 0;
+    for (int level = 0;; level++) {
+        ohit h;
+        memset(&h, 0, sizeof(h));
+        if (!bvh_hit(x->b, &r, tmin, INFINITY, &h, 0)) {
+            render_ctx rc;
+            memset(&rc, 0, sizeof(rc));
+            rc.rd = rd;
+            *miss = miss_color(&rc, &r);
+            *L = vadd(*L, vemul(T, *miss));
+            break;
+        }
+        if (level > rd->max_depth || nv >= maxv) break;
+        int tri = h.prim;
+        double e = x->emission[tri];
+        v3 a = mk(x->albedo[3 * tri], x->albedo[3 * tri + 1], x->albedo[3 * tri + 2]);
+        vx[nv].tri = tri;
+        vx[nv].P = T;
+        vx[nv].a = a;
+        nv++;
+        *L = vadd(*L, vmul(T, e));
+        /* geometric normal facing the ray, then normal + uniform unit vector */
+        const double *tv = x->b->tri + 9 * (int64_t)tri;
+        v3 v0 = mk(tv[0], tv[1], tv[2]);
+        v3 ng = vcross(vsub(mk(tv[3], tv[4], tv[5]), v0), vsub(mk(tv[6], tv[7], tv[8]), v0));
+        v3 n = vunit(ng);
+        if (!(vdot(r.d, ng) < 0)) n = vmul(n, -1);
+        philox2x32(g, (uint32_t)level, key, rnd);
+        double z = 1.0 - 2.0 * u01_24(rnd[0]);
+        double rr = sqrt(fmax(0.0, 1.0 - z * z));
+        double phi = 2.0 * M_PI * u01_24(rnd[1]);
+        v3 sd = mk(n.x + rr * cos(phi), n.y + rr * sin(phi), n.z + z);
+        if (fabs(sd.x) <= ORC_APPROX_THRESH && fabs(sd.y) <= ORC_APPROX_THRESH && fabs(sd.z) <= ORC_APPROX_THRESH) sd = n;
+        v3 p = vadd(r.o, vmul(r.d, h.t));
+        T = vemul(T, a);
+        r = make_ray(p, sd);
+        tmin = 0.0001;
+    }
+    return nv;
+}
+
+static void adj_row(void *c, int64_t y) {
+    adj_ctx *x = (adj_ctx *)c;
+    const orc_render_desc *rd = x->rd;
+    const uint32_t npix = (uint32_t)rd->width * (uint32_t)rd->height;
+    enum { MAXV = 16 };
+    adj_vertex vx[MAXV];
+    v3 S[MAXV];
+    int n_tri = (int)x->b->n_tri;
+    double *ga = (double *)calloc((size_t)n_tri * 3, sizeof(double));
+    double *ge = (double *)calloc((size_t)n_tri, sizeof(double));
+    for (int32_t px = 0; px < rd->width; px++) {
+        uint32_t pix = (uint32_t)y * (uint32_t)rd->width + (uint32_t)px;
+        v3 sum = mk(0, 0, 0);
+        v3 delta = mk(0, 0, 0);
+        if (x->dimg)
+            delta = mk(x->dimg[3 * pix] / rd->spp, x->dimg[3 * pix + 1] / rd->spp, x->dimg[3 * pix + 2] / rd->spp);
+        for (int32_t s = 0; s < rd->spp; s++) {
+            v3 L, m;
+            int nv = adj_path(x, (uint32_t)s * npix + pix, vx, MAXV, &L, &m);
+            sum = vadd(sum, L);
+            if (!x->dimg) continue;
+            v3 acc = m;
+            for (int i = nv - 1; i >= 0; i--) {
+                S[i] = acc;
+                double e = x->emission[vx[i].tri];
+                acc = vadd(mk(e, e, e), vemul(vx[i].a, acc));
+            }
+            for (int i = 0; i < nv; i++) {
+                int t = vx[i].tri;
+                v3 P = vx[i].P;
+                ga[3 * t] += delta.x * P.x * S[i].x;
+                ga[3 * t + 1] += delta.y * P.y * S[i].y;
+                ga[3 * t + 2] += delta.z * P.z * S[i].z;
+                ge[t] += delta.x * P.x + delta.y * P.y + delta.z * P.z;
+            }
+        }
+        x->img[3 * pix] = sum.x / rd->spp;
+        x->img[3 * pix + 1] = sum.y / rd->spp;
+        x->img[3 * pix + 2] = sum.z / rd->spp;
+    }
+    if (x->dimg) {
+        pthread_mutex_lock(&x->lock);
+        for (int t = 0; t < n_tri; t++) {
+            x->ga[3 * t] += ga[3 * t];
+            x->ga[3 * t + 1] += ga[3 * t + 1];
+            x->ga[3 * t + 2] += ga[3 * t + 2];
+            x->ge[t] += ge[t];
+        }
+        pthread_mutex_unlock(&x->lock);
+    }
+    free(ga);
+    free(ge);
+}
+
+int orc_adjoint(const orc_bvh *b, const orc_camera_desc *cam, const orc_render_desc *rd, const float *albedo,
+                const float *emission, const float *dimg, double *img, double *g_albedo, double *g_emission) {
+    if (b->n_sph || rd->width < 2 || rd->height < 2 || rd->spp < 1) return ORC_E_ARG;
+    adj_ctx x;
+    x.b = b;
+    x.rd = rd;
+    x.cam = make_camera(cam);
+    x.albedo = albedo;
+    x.emission = emission;
+    x.dimg = dimg;
+    x.img = img;
+    x.ga = g_albedo;
+    x.ge = g_emission;
+    pthread_mutex_init(&x.lock, NULL);
+    if (dimg) {
+        memset(g_albedo, 0, (size_t)b->n_tri * 3 * sizeof(double));
+        memset(g_emission, 0, (size_t)b->n_tri * sizeof(double));
+    }
+    orc_parallel(rd->threads, rd->height, adj_row, &x);
+    pthread_mutex_destroy(&x.lock);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* PHR: phr.go:42-459                                                        */
 /* ------------------------------------------------------------------------ */
 /* A cut holds aux-node ids (>= 0) or, for a one-node cut made by makeLeaf,

@@ -87,6 +87,15 @@ int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_typ
 void orc_camera_rays(const orc_camera_desc *cam, int32_t width, int32_t height,
                      const double *su, const double *sv, int64_t n, double *dirs, double origin[3]);
 
+/* ---- float64 adjoint of the differentiable render (test of the GPU adjoint) ----
+ * Material model: every triangle emits emission[t] (white) and scatters
+ * diffusely with albedo[3t..3t+2]; camera rays, Diffuse scatter and MaxDepth as
+ * orc_render, but driven by the same counter-based random numbers as the GPU
+ * (Philox-2x32-10, counter (path, level)), so both sides sample the same paths.
+ * img: width*height*3; dimg: dLoss/dImage; gradients accumulate into g_*. */
+int orc_adjoint(const orc_bvh *b, const orc_camera_desc *cam, const orc_render_desc *rd, const float *albedo,
+                const float *emission, const float *dimg, double *img, double *g_albedo, double *g_emission);
+
 /* ---- PHR ---- */
 int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[4]);
 

@@ -59,6 +59,8 @@ def lib():
         L.orc_traversal_steps.argtypes = [P, P, i64, C.c_int, P]
         L.orc_render.restype = C.c_int
         L.orc_render.argtypes = [P, P, P, P, P, P, P]
+        L.orc_adjoint.restype = C.c_int
+        L.orc_adjoint.argtypes = [P, P, P, P, P, P, P, P, P]
         L.orc_phr_build.restype = C.c_int
         L.orc_phr_build.argtypes = [P, d, d, C.c_int, C.POINTER(P), P]
         _lib = L
@@ -200,6 +202,31 @@ class BVH:
             raise RuntimeError("oracle render failed: %d" % rc)
         self.last_rays = int(r.rays_traced)
         return img
+
+    def adjoint(self, camera, width, height, spp, max_depth, albedo, emission, dimg=None, seed=1, miss_mode=0,
+                threads=None):
+        """float64 image and (if dimg is given) dLoss/d(albedo, emission) with the GPU's random numbers."""
+        cd = CameraDesc()
+        cd.look_from[:] = camera["look_from"]
+        cd.look_at[:] = camera["look_at"]
+        cd.up[:] = camera["up"]
+        cd.aspect = camera["aspect"]
+        cd.fov_deg = camera["fov"]
+        r = RenderDesc()
+        r.width, r.height, r.spp, r.max_depth, r.miss_mode = width, height, spp, max_depth, miss_mode
+        r.seed = seed
+        r.threads = threads or (os.cpu_count() or 1)
+        n = len(emission)
+        alb = np.ascontiguousarray(albedo, np.float32).reshape(n, 3)
+        emi = np.ascontiguousarray(emission, np.float32).reshape(n)
+        img = np.empty((height, width, 3), np.float64)
+        ga = np.zeros((n, 3), np.float64)
+        ge = np.zeros(n, np.float64)
+        d = None if dimg is None else np.ascontiguousarray(dimg, np.float32)
+        rc = lib().orc_adjoint(self.h, C.byref(cd), C.byref(r), _p(alb), _p(emi), _p(d), _p(img), _p(ga), _p(ge))
+        if rc != 0:
+            raise RuntimeError("oracle adjoint failed: %d" % rc)
+        return img, ga, ge
 
     def phr(self, alpha=0.5, delta=6.0, bf=2):
         h = C.c_void_p()

@@ -98,6 +98,25 @@ def test_trace_terrain_with_sphere(ctx):
     check(ctx, g, o, rr, "terrain sphere rays")
 
 
+@pytest.mark.parametrize("kind", ["lbvh", "phr"])
+def test_four_wide_view_gives_the_binary_hits(ctx, kind):
+    """The collapsed 4-wide traversal view returns what the binary tree returns."""
+    s = scenes.soup(200_000, seed=3)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    if kind == "phr":
+        g = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(g)
+    rays = scenes.camera_rays(s["camera"], 480, 270, jitter_seed=4)
+    p4, t4, u4, v4 = g.trace(rays)
+    ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, g.h, 2), "layout")
+    p2, t2, u2, v2 = g.trace(rays)
+    ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, g.h, 4), "layout")
+    assert np.array_equal(t4, t2)
+    same = p4 == p2
+    assert same.mean() >= 0.99999  # an exact equal-distance tie may resolve either way
+    assert np.array_equal(u4[same], u2[same]) and np.array_equal(v4[same], v2[same])
+
+
 def test_trace_empty_and_miss(ctx):
     s = scenes.soup(1000, seed=3)
     ds = pt.DeviceScene.from_dict(ctx, s)

@@ -24,7 +24,10 @@ EXPORTS = [
     "gbt_bvh_cost", "gbt_bvh_size", "gbt_bvh_counts", "gbt_bvh_export", "gbt_lbvh_sorted",
     "gbt_trace", "gbt_trace_async", "gbt_render", "gbt_render_async", "gbt_render_last_stats",
     "gbt_device_alloc", "gbt_device_free", "gbt_copy_h2d_async", "gbt_copy_d2h_async",
-    "gbt_sort_morton_pairs_noalloc",
+    "gbt_sort_morton_pairs_noalloc", "gbt_bvh_set_layout",
+    "gbt_render_batch_async", "gbt_render_batch_plain_async", "gbt_batch_autotune", "gbt_batch_graph_create",
+    "gbt_graph_launch", "gbt_graph_destroy",
+    "gbt_adjoint_forward_async", "gbt_adjoint_backward_async", "gbt_l2_loss_async",
 ]
 
 
@@ -44,6 +47,14 @@ class Camera(C.Structure):
 class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_depth", C.c_int32),
                 ("miss_mode", C.c_int32), ("miss_color", C.c_float * 3), ("seed", C.c_uint64)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("bvh", C.c_void_p), ("camera", Camera), ("params", RenderParams), ("d_rgb", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("block", C.c_int32), ("fetch_min", C.c_int32), ("stack", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -99,6 +110,16 @@ def load():
         "gbt_copy_h2d_async": ([P, P, P, C.c_size_t], C.c_int),
         "gbt_copy_d2h_async": ([P, P, P, C.c_size_t], C.c_int),
         "gbt_sort_morton_pairs_noalloc": ([P, P, P, P, u32], C.c_int),
+        "gbt_bvh_set_layout": ([P, P, i32], C.c_int),
+        "gbt_render_batch_async": ([P, P, u32, P], C.c_int),
+        "gbt_render_batch_plain_async": ([P, P, u32], C.c_int),
+        "gbt_batch_autotune": ([P, P, u32, P, C.POINTER(d)], C.c_int),
+        "gbt_batch_graph_create": ([P, P, u32, P, i32, PP], C.c_int),
+        "gbt_graph_launch": ([P, P], C.c_int),
+        "gbt_graph_destroy": ([P], C.c_int),
+        "gbt_adjoint_forward_async": ([P, P, P, P, P, P, P], C.c_int),
+        "gbt_adjoint_backward_async": ([P, P, P, P, P, P, P, P, P], C.c_int),
+        "gbt_l2_loss_async": ([P, P, P, u32, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

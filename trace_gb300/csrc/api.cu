@@ -101,6 +101,8 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
         return GBT_ECUDA;
     }
     for (auto &e : c->ev) cudaEventCreate(&e);
+    if (const char *t = std::getenv("GBT_TRAVERSAL"))
+        c->traversal = std::strcmp(t, "simple") == 0 ? 1 : std::strcmp(t, "ww") == 0 ? 2 : 0;
     *out = c;
     return GBT_OK;
 }
@@ -114,6 +116,7 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_out) cudaFree(ctx->d_out);
+    if (ctx->bstate) cudaFree(ctx->bstate);
     for (auto &e : ctx->prof_ev) cudaEventDestroy(e);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -251,6 +254,8 @@ extern "C" int gbt_bvh_destroy(gbt_bvh *b) {
     cudaFree(b->d_size);
     cudaFree(b->d_other);
     cudaFree(b->d_range);
+    cudaFree(b->d_nodes4);
+    cudaFree(b->d_hdr4);
     delete b;
     return GBT_OK;
 }
@@ -288,6 +293,8 @@ extern "C" int gbt_lbvh_build(gbt_ctx *ctx, gbt_scene *scene, gbt_bvh **out) {
     GBT_TRY(lbvh_alloc(ctx, scene, &b));
     int rc = gbt_lbvh_enqueue(ctx, b);
     if (!rc) rc = gbt_check_device_error(ctx, "lbvh_build");
+    if (!rc) rc = gbt_collapse4(ctx, b);
+    if (!rc) rc = gbt_check_device_error(ctx, "lbvh_build traversal view");
     if (rc) { gbt_bvh_destroy(b); return rc; }
     *out = b;
     return GBT_OK;
@@ -295,7 +302,18 @@ extern "C" int gbt_lbvh_build(gbt_ctx *ctx, gbt_scene *scene, gbt_bvh **out) {
 
 extern "C" int gbt_lbvh_rebuild_async(gbt_ctx *ctx, gbt_bvh *bvh) {
     if (!ctx || !bvh || bvh->kind != GBT_BVH_LBVH) return gbt_fail(ctx, GBT_EINVAL, "rebuild: not an LBVH");
+    bvh->has_nodes4 = 0;  // traversal uses the rebuilt binary nodes until gbt_bvh_set_layout(.., 4)
     return gbt_lbvh_enqueue(ctx, bvh);
+}
+
+extern "C" int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width) {
+    if (!ctx || !bvh || (width != 2 && width != 4)) return GBT_EINVAL;
+    if (width == 2) {
+        bvh->has_nodes4 = 0;
+        return GBT_OK;
+    }
+    GBT_TRY(gbt_collapse4(ctx, bvh));
+    return gbt_check_device_error(ctx, "bvh_set_layout");
 }
 
 extern "C" int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out) {
@@ -310,6 +328,8 @@ extern "C" int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double de
     b->arity = branching == 2 ? 2 : 4;
     int rc = gbt_phr_run(ctx, aux, alpha, delta, branching, b);
     if (!rc) rc = gbt_check_device_error(ctx, "phr_build");
+    if (!rc) rc = gbt_collapse4(ctx, b);
+    if (!rc) rc = gbt_check_device_error(ctx, "phr_build traversal view");
     if (rc) { gbt_bvh_destroy(b); return rc; }
     *out = b;
     return GBT_OK;

@@ -1,0 +1,520 @@
+// Batched rendering: many scenes and many independent renders in one
+// persistent launch.
+//
+// Every (scene, path) pair of the batch is one entry of a device work queue
+// (a counter over the concatenated path ranges of the items).  Each lane of a
+// resident warp pulls a path, runs it to completion -- camera ray, closest
+// hit, shading, next bounce (shade.cuh) -- and pulls the next one; lanes are
+// refilled with warp-aggregated atomics.  The paths are the ones the per-scene
+// wavefront renderer traces (same Philox counters), so the images agree up to
+// the order of float additions.  The per-frame sequence (accumulator clear,
+// the persistent kernel, the resolve) can be captured in a CUDA graph together
+// with in-place LBVH rebuilds.  Launch parameters come from a small autotuner.
+//
+// The reference renders one scene at a time (render.go:91-129); batching has
+// no counterpart there.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <type_traits>
+#include <cstring>
+#include <vector>
+
+#include "gbt_internal.cuh"
+#include "shade.cuh"
+
+using namespace gbt_dev;
+
+namespace {
+
+constexpr int MAX_ITEMS = 1024;
+
+struct ItemDev {
+    const BvhHeader *hdr;
+    const float4 *nodes;
+    const float4 *recs;
+    const uint32_t *prim_mat;
+    const float4 *mats;
+    const float *normals;
+    float *acc;
+    float *out;
+    CamF cam;
+    ShadeParams sp;
+    uint32_t path_base;  // first queue entry of this item
+    uint32_t pix_base;   // first accumulator float of this item / 3
+    float inv_spp;
+    uint32_t pad;
+};
+
+__device__ __forceinline__ uint32_t lane_lt_mask() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// item of queue entry q: last item whose path_base <= q (binary search in shared memory)
+__device__ __forceinline__ int find_item(const uint32_t *s_base, int n, uint32_t q) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_base[mid] <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int W, int BLOCK, int DYN, int SH>
+__global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ items, int n_items, uint32_t total,
+                                                 uint32_t *fetch, unsigned int *err, unsigned long long *ray_total) {
+    constexpr int STACK = W == 2 ? 64 : 96;
+    __shared__ uint32_t s_base[MAX_ITEMS];
+    __shared__ int2 s_se[SH > 0 ? SH * BLOCK : 1];
+    __shared__ float s_st[SH > 0 ? SH * BLOCK : 1];
+    for (int i = threadIdx.x; i < n_items; i += BLOCK) s_base[i] = items[i].path_base;
+    __syncthreads();
+    using StackT = typename std::conditional<(SH > 0), SharedTopStack<STACK, (SH > 0 ? SH : 1)>, LocalStack<STACK>>::type;
+    StackT st;
+    if constexpr (SH > 0) {
+        st.se = s_se + threadIdx.x;
+        st.st = s_st + threadIdx.x;
+        st.stride = BLOCK;
+    }
+    const uint32_t lane = threadIdx.x & 31;
+    int sp = 0;
+    int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
+    Ray r;
+    Hit h;
+    h.t = 0.f;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    // path state
+    int item = -1;  // -1: no path
+    uint32_t g = 0;
+    int level = 0;
+    float3 T = f3(1.f, 1.f, 1.f), L = f3(0.f, 0.f, 0.f);
+    const float4 *nodes = nullptr, *recs = nullptr;
+    uint32_t rays = 0;
+    bool pool_empty = false;
+    for (;;) {
+        // a finished ray: shade it, continue the path or end it
+        if (item >= 0 && node.y < 0 && leaf.y <= 0) {
+            const ItemDev &it = items[item];
+            float3 no, nd;
+            bool cont = shade_step(it.sp, level, g, r.o, r.d, h.t, h.u, h.v, h.rec, recs, it.prim_mat, it.mats,
+                                   it.normals, T, L, no, nd);
+            if (cont) {
+                level++;
+                r.o = no;
+                r.d = nd;
+                r.tmin = 0.0001f;
+                r.tmax = __int_as_float(0x7f800000);
+                finish_ray(r);
+                h.t = r.tmax;
+                h.rec = -1;
+                sp = 0;
+                leaf = make_int2(0, 0);
+                float te;
+                const BvhHeader *hd = it.hdr;
+                node = slab(hd->root_lo[0], hd->root_lo[1], hd->root_lo[2], hd->root_hi[0], hd->root_hi[1],
+                            hd->root_hi[2], r, h.t, te)
+                           ? make_int2(hd->root_ref, hd->root_cnt)
+                           : make_int2(0, -1);
+                if (node.y > 0) {
+                    leaf = node;
+                    node = make_int2(0, -1);
+                }
+                rays++;
+            } else {
+                deposit(it.acc, g % it.sp.npix, L);
+                item = -1;
+            }
+        }
+        // refill lanes without a path from the queue
+        const bool want = item < 0 && !pool_empty;
+        const uint32_t need = __ballot_sync(0xffffffffu, want);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == (uint32_t)leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            bool empty_here = false;
+            if (want) {
+                const uint32_t q = base + __popc(need & lane_lt_mask());
+                if (q < total) {
+                    item = find_item(s_base, n_items, q);
+                    const ItemDev &it = items[item];
+                    g = q - it.path_base;
+                    nodes = it.nodes;
+                    recs = it.recs;
+                    level = 0;
+                    T = f3(1.f, 1.f, 1.f);
+                    L = f3(0.f, 0.f, 0.f);
+                    primary_ray(it.cam, it.sp, g, r.o, r.d);
+                    r.tmin = 0.001f;
+                    r.tmax = __int_as_float(0x7f800000);
+                    finish_ray(r);
+                    h.t = r.tmax;
+                    h.u = h.v = 0.f;
+                    h.rec = -1;
+                    sp = 0;
+                    leaf = make_int2(0, 0);
+                    float te;
+                    const BvhHeader *hd = it.hdr;
+                    node = slab(hd->root_lo[0], hd->root_lo[1], hd->root_lo[2], hd->root_hi[0], hd->root_hi[1],
+                                hd->root_hi[2], r, h.t, te)
+                               ? make_int2(hd->root_ref, hd->root_cnt)
+                               : make_int2(0, -1);
+                    if (node.y > 0) {
+                        leaf = node;
+                        node = make_int2(0, -1);
+                    }
+                    rays++;
+                } else {
+                    empty_here = true;
+                }
+            }
+            pool_empty = __any_sync(0xffffffffu, empty_here) || pool_empty;
+        }
+        if (__all_sync(0xffffffffu, item < 0)) break;
+        // closest-hit traversal of the current rays (while-while, postponed leaves)
+        while (node.y >= 0 || leaf.y > 0) {
+            while (node.y == 0) {
+                node = W == 2 ? step2(nodes, node, st, sp, r, h.t, err) : step4(nodes, node, st, sp, r, h.t, err);
+                if (node.y > 0 && leaf.y <= 0) {
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                }
+                if (!__any_sync(__activemask(), leaf.y <= 0)) break;
+            }
+            while (leaf.y > 0) {
+                gbt_dev::leaf(recs, leaf.x, leaf.y, r, h);
+                if (node.y > 0) {
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                } else {
+                    leaf = make_int2(0, 0);
+                }
+            }
+            if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
+        }
+    }
+    // rays traced, for the statistics
+    __syncwarp();
+    unsigned long long c = rays;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) atomicAdd(ray_total, c);
+}
+
+__global__ void k_resolve_batch(const ItemDev *__restrict__ items, int n_items, uint32_t total_floats) {
+    __shared__ uint32_t s_pb[MAX_ITEMS];
+    for (int i = threadIdx.x; i < n_items; i += blockDim.x) s_pb[i] = items[i].pix_base * 3;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total_floats; i += gridDim.x * blockDim.x) {
+        int it = find_item(s_pb, n_items, i);
+        const ItemDev &d = items[it];
+        uint32_t k = i - s_pb[it];
+        d.out[k] = d.acc[k] * d.inv_spp;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct gbt_graph {
+    gbt_ctx *ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *pinned_items = nullptr;  // page-locked source of the graph's descriptor upload
+    uint64_t paths = 0;
+};
+
+namespace {
+
+using Launcher = void (*)(const ItemDev *, int, uint32_t, uint32_t *, unsigned int *, unsigned long long *, int,
+                          cudaStream_t);
+
+template <int W, int BLOCK, int DYN, int SH>
+void launch_batch(const ItemDev *items, int n, uint32_t total, uint32_t *fetch, unsigned int *err,
+                  unsigned long long *rays, int num_sms, cudaStream_t s) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<W, BLOCK, DYN, SH>, BLOCK, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    uint32_t grid = (uint32_t)(num_sms * per_sm);
+    uint32_t need = (total + BLOCK - 1) / BLOCK;
+    if (need < grid) grid = need;
+    if (grid == 0) grid = 1;
+    k_batch<W, BLOCK, DYN, SH><<<grid, BLOCK, 0, s>>>(items, n, total, fetch, err, rays);
+}
+
+// config: block in {64,128,256} x fetch_min in {0,16} x stack in {local, top 8 entries in shared memory}
+template <int W>
+Launcher pick(const gbt_batch_config &c) {
+    const int b = c.block, d = c.fetch_min > 0 ? 1 : 0, s = c.stack ? 1 : 0;
+#define GBT_PICK(B, D, S) \
+    if (b == B && d == (D > 0) && s == (S > 0)) return &launch_batch<W, B, D, S>;
+    GBT_PICK(64, 0, 0) GBT_PICK(64, 0, 8) GBT_PICK(64, 16, 0) GBT_PICK(64, 16, 8)
+    GBT_PICK(128, 0, 0) GBT_PICK(128, 0, 8) GBT_PICK(128, 16, 0) GBT_PICK(128, 16, 8)
+    GBT_PICK(256, 0, 0) GBT_PICK(256, 0, 8) GBT_PICK(256, 16, 0) GBT_PICK(256, 16, 8)
+#undef GBT_PICK
+    return nullptr;
+}
+
+int check_items(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, int *width) {
+    if (!items || n == 0 || n > (uint32_t)MAX_ITEMS) return gbt_fail(ctx, GBT_EINVAL, "batch: 1..1024 items");
+    int w = -1;
+    uint64_t paths = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const gbt_batch_item &it = items[i];
+        if (!it.bvh || !it.d_rgb) return gbt_fail(ctx, GBT_EINVAL, "batch: item without BVH or output");
+        const gbt_render_params &p = it.params;
+        if (p.width < 2 || p.height < 2 || p.spp < 1 || p.max_depth < 0 || p.max_depth > 60)
+            return gbt_fail(ctx, GBT_EINVAL, "batch: width/height >= 2, spp >= 1, 0 <= max_depth <= 60");
+        int wi = (it.bvh->has_nodes4 || it.bvh->arity == 4) ? 4 : 2;
+        if (w < 0) w = wi;
+        if (wi != w) return gbt_fail(ctx, GBT_EINVAL, "batch: all BVHs need the same traversal layout");
+        paths += (uint64_t)p.width * p.height * p.spp;
+    }
+    if (paths >= (1ull << 32)) return gbt_fail(ctx, GBT_EINVAL, "batch: more than 2^32 paths");
+    *width = w;
+    return GBT_OK;
+}
+
+// Per-context batch state: item descriptors, accumulators, queue counter.
+int prepare(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<ItemDev> &hi, uint64_t *total_paths,
+            size_t *acc_floats) {
+    hi.resize(n);
+    uint64_t paths = 0, pix = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        const gbt_batch_item &it = items[i];
+        const gbt_bvh *b = it.bvh;
+        ItemDev &d = hi[i];
+        d.hdr = b->has_nodes4 ? b->d_hdr4 : b->d_hdr;
+        d.nodes = b->has_nodes4 ? b->d_nodes4 : b->d_nodes;
+        d.recs = b->d_prims;
+        d.prim_mat = b->scene->d_prim_mat;
+        d.mats = b->scene->d_mats;
+        d.normals = b->scene->d_normals;
+        d.out = it.d_rgb;
+        d.cam = gbt_make_cam(&it.camera);
+        d.sp = gbt_make_shade_params(&it.params, b->scene->n_tri);
+        d.path_base = (uint32_t)paths;
+        d.pix_base = (uint32_t)pix;
+        d.inv_spp = 1.0f / it.params.spp;
+        d.pad = 0;
+        paths += (uint64_t)it.params.width * it.params.height * it.params.spp;
+        pix += (uint64_t)it.params.width * it.params.height;
+    }
+    *total_paths = paths;
+    *acc_floats = pix * 3;
+    if (pix * 3 >= (1ull << 32)) return gbt_fail(ctx, GBT_EINVAL, "batch: too many pixels");
+    size_t need = gbt_align(n * sizeof(ItemDev)) + gbt_align(*acc_floats * sizeof(float)) + 256;
+    if (ctx->bstate_bytes < need) {
+        if (ctx->bstate) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->bstate);
+        }
+        ctx->bstate = nullptr;
+        ctx->bstate_bytes = 0;
+        if (cudaMalloc(&ctx->bstate, need) != cudaSuccess) {
+            cudaGetLastError();
+            return gbt_fail(ctx, GBT_ENOMEM, "batch: state allocation");
+        }
+        ctx->bstate_bytes = need;
+    }
+    unsigned char *base = static_cast<unsigned char *>(ctx->bstate);
+    float *acc = reinterpret_cast<float *>(base + gbt_align(n * sizeof(ItemDev)));
+    for (uint32_t i = 0; i < n; i++) hi[i].acc = acc + (size_t)hi[i].pix_base * 3;
+    return GBT_OK;
+}
+
+int enqueue_frame(gbt_ctx *ctx, const ItemDev *h_items, size_t n_items, uint64_t paths, size_t acc_floats,
+                  const gbt_batch_config &cfg, int width) {
+    cudaStream_t st = ctx->stream;
+    unsigned char *base = static_cast<unsigned char *>(ctx->bstate);
+    ItemDev *d_items = reinterpret_cast<ItemDev *>(base);
+    float *acc = reinterpret_cast<float *>(base + gbt_align(n_items * sizeof(ItemDev)));
+    uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
+    Launcher f = width == 4 ? pick<4>(cfg) : pick<2>(cfg);
+    if (!f) return gbt_fail(ctx, GBT_EINVAL, "batch: unsupported configuration");
+    GBT_CUDA(ctx, cudaMemcpyAsync(d_items, h_items, n_items * sizeof(ItemDev), cudaMemcpyHostToDevice, st));
+    GBT_CUDA(ctx, cudaMemsetAsync(acc, 0, acc_floats * sizeof(float), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st));
+    f(d_items, (int)n_items, (uint32_t)paths, fetch, ctx->d_error, ctx->d_counters + 2, ctx->num_sms, st);
+    k_resolve_batch<<<ctx->num_sms * 4, 256, 0, st>>>(d_items, (int)n_items, (uint32_t)acc_floats);
+    GBT_CUDA(ctx, cudaGetLastError());
+    ctx->last_stats.paths += paths;
+    ctx->last_stats.kernel_launches += 2;
+    return GBT_OK;
+}
+
+gbt_batch_config default_config(const gbt_ctx *ctx) {
+    if (ctx->batch_tuned) return ctx->batch_cfg;
+    gbt_batch_config c;
+    c.block = 128;
+    c.fetch_min = 16;
+    c.stack = 0;
+    return c;
+}
+
+}  // namespace
+
+extern "C" int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n,
+                                      const gbt_batch_config *cfg) {
+    if (!ctx) return GBT_EINVAL;
+    int width;
+    int rc = check_items(ctx, items, n, &width);
+    if (rc) return rc;
+    std::vector<ItemDev> hi;
+    uint64_t paths;
+    size_t accf;
+    rc = prepare(ctx, items, n, hi, &paths, &accf);
+    if (rc) return rc;
+    // a copy from pageable memory is staged before cudaMemcpyAsync returns, so hi may go
+    return enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, cfg ? *cfg : default_config(ctx), width);
+}
+
+extern "C" int gbt_render_batch_plain_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n) {
+    if (!ctx) return GBT_EINVAL;
+    int width;
+    int rc = check_items(ctx, items, n, &width);
+    if (rc) return rc;
+    for (uint32_t i = 0; i < n; i++) {
+        rc = gbt_render_enqueue(ctx, items[i].bvh, &items[i].camera, &items[i].params, items[i].d_rgb);
+        if (rc) return rc;
+    }
+    return GBT_OK;
+}
+
+extern "C" int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, gbt_batch_config *best,
+                                  double *best_ms) {
+    if (!ctx || !best) return GBT_EINVAL;
+    int width;
+    int rc = check_items(ctx, items, n, &width);
+    if (rc) return rc;
+    std::vector<ItemDev> hi;
+    uint64_t paths;
+    size_t accf;
+    rc = prepare(ctx, items, n, hi, &paths, &accf);
+    if (rc) return rc;
+    const int blocks[3] = {64, 128, 256}, fetches[2] = {0, 16}, stacks[2] = {0, 1};
+    double bms = 1e30;
+    gbt_batch_config bc{128, 16, 0};
+    for (int b : blocks)
+        for (int f : fetches)
+            for (int s : stacks) {
+                gbt_batch_config c{b, f, s};
+                // one untimed frame, then the best of two timed frames
+                rc = enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, c, width);
+                if (rc) return rc;
+                double m = 1e30;
+                for (int rep = 0; rep < 2; rep++) {
+                    GBT_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+                    rc = enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, c, width);
+                    if (rc) return rc;
+                    GBT_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+                    GBT_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+                    m = std::min(m, (double)ms);
+                }
+                if (m < bms) {
+                    bms = m;
+                    bc = c;
+                }
+            }
+    rc = gbt_check_device_error(ctx, "batch_autotune");
+    if (rc) return rc;
+    ctx->batch_cfg = bc;
+    ctx->batch_tuned = 1;
+    *best = bc;
+    if (best_ms) *best_ms = bms;
+    return GBT_OK;
+}
+
+extern "C" int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n,
+                                      const gbt_batch_config *cfg, int32_t rebuild_lbvh, gbt_graph **out) {
+    if (!ctx || !out) return GBT_EINVAL;
+    *out = nullptr;
+    int width;
+    int rc = check_items(ctx, items, n, &width);
+    if (rc) return rc;
+    if (rebuild_lbvh) {
+        for (uint32_t i = 0; i < n; i++)
+            if (items[i].bvh->kind != GBT_BVH_LBVH)
+                return gbt_fail(ctx, GBT_EINVAL, "batch graph: rebuilding needs LBVH items");
+        // rebuilds replace the binary nodes, so the frame traverses those
+        for (uint32_t i = 0; i < n; i++) items[i].bvh->has_nodes4 = 0;
+        width = 2;
+    }
+    gbt_graph *g = new gbt_graph();
+    g->ctx = ctx;
+    uint64_t paths;
+    size_t accf;
+    std::vector<ItemDev> hi;
+    rc = prepare(ctx, items, n, hi, &paths, &accf);
+    if (rc) { delete g; return rc; }
+    g->paths = paths;
+    if (cudaMallocHost(&g->pinned_items, hi.size() * sizeof(ItemDev)) != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return gbt_fail(ctx, GBT_ENOMEM, "batch graph: pinned descriptors");
+    }
+    std::memcpy(g->pinned_items, hi.data(), hi.size() * sizeof(ItemDev));
+    // grow every scratch buffer the captured work uses before capturing
+    for (uint32_t i = 0; rebuild_lbvh && i < n; i++) {
+        void *scr;
+        rc = gbt_scratch(ctx, gbt_lbvh_scratch_bytes(items[i].bvh->n_prim), &scr);
+        if (rc) { delete g; return rc; }
+    }
+    cudaStream_t st = ctx->stream;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        delete g;
+        return gbt_fail(ctx, GBT_ECUDA, "batch graph: begin capture");
+    }
+    for (uint32_t i = 0; rebuild_lbvh && i < n && !rc; i++) rc = gbt_lbvh_enqueue(ctx, items[i].bvh);
+    if (!rc)
+        rc = enqueue_frame(ctx, static_cast<const ItemDev *>(g->pinned_items), hi.size(), paths, accf,
+                           cfg ? *cfg : default_config(ctx), width);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaFreeHost(g->pinned_items);
+        delete g;
+        cudaGetLastError();
+        return rc ? rc : gbt_fail(ctx, GBT_ECUDA, std::string("batch graph: capture: ") + cudaGetErrorString(e));
+    }
+    g->graph = graph;
+    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cudaFreeHost(g->pinned_items);
+        delete g;
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ECUDA, "batch graph: instantiate");
+    }
+    ctx->last_stats.paths = 0;
+    *out = g;
+    return GBT_OK;
+}
+
+extern "C" int gbt_graph_launch(gbt_ctx *ctx, gbt_graph *g) {
+    if (!ctx || !g || g->ctx != ctx) return GBT_EINVAL;
+    GBT_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+    ctx->last_stats.paths += g->paths;
+    return GBT_OK;
+}
+
+extern "C" int gbt_graph_destroy(gbt_graph *g) {
+    if (!g) return GBT_EINVAL;
+    if (g->ctx) cudaStreamSynchronize(g->ctx->stream);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->pinned_items) cudaFreeHost(g->pinned_items);
+    delete g;
+    return GBT_OK;
+}

@@ -1,0 +1,161 @@
+// Four-wide traversal view of a binary BVH.
+//
+// The binary tree (LBVH, or PHR with branching factor 2) is what the
+// reference builds and what parity checks export.  For traversal it is
+// collapsed top-down into 128-byte 4-wide nodes: starting from a node's two
+// children, the inner child with the largest surface area is repeatedly
+// replaced by its own two children until there are four.  Closest-hit results
+// do not depend on the node layout; only the number of node fetches does.
+#include <cuda_runtime.h>
+
+#include "gbt_internal.cuh"
+
+namespace {
+
+struct Child {
+    float lo[3], hi[3];
+    int32_t ref, cnt;
+};
+
+__device__ __forceinline__ void load_slots(const float4 *__restrict__ bin, int32_t node, Child &a, Child &b) {
+    const float4 *nd = bin + 4 * (size_t)node;
+    float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+    int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+    a.lo[0] = n0.x; a.hi[0] = n0.y; a.lo[1] = n0.z; a.hi[1] = n0.w; a.lo[2] = n2.x; a.hi[2] = n2.y;
+    a.ref = n3.x; a.cnt = n3.y;
+    b.lo[0] = n1.x; b.hi[0] = n1.y; b.lo[1] = n1.z; b.hi[1] = n1.w; b.lo[2] = n2.z; b.hi[2] = n2.w;
+    b.ref = n3.z; b.cnt = n3.w;
+}
+
+__device__ __forceinline__ float area(const Child &c) {
+    float w = c.hi[0] - c.lo[0], h = c.hi[1] - c.lo[1], d = c.hi[2] - c.lo[2];
+    return w * h + w * d + h * d;
+}
+
+// One level: every queued binary node becomes the 4-wide node already assigned to it.
+__global__ void k_collapse_level(const float4 *__restrict__ bin, const int2 *__restrict__ q_in,
+                                 const uint32_t *__restrict__ n_in, int2 *__restrict__ q_out, uint32_t *n_out,
+                                 uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *n_in) return;
+    const int2 e = q_in[i];  // (binary node, 4-wide node)
+    Child c[4];
+    load_slots(bin, e.x, c[0], c[1]);
+    int nc = 0;
+    if (c[0].cnt >= 0) nc++;
+    if (c[1].cnt >= 0) { c[nc] = c[1]; nc++; }
+    while (nc < 4) {
+        int best = -1;
+        float ba = -1.f;
+        for (int k = 0; k < nc; k++)
+            if (c[k].cnt == 0) {
+                float a = area(c[k]);
+                if (a > ba) { ba = a; best = k; }
+            }
+        if (best < 0) break;
+        Child x, y;
+        load_slots(bin, c[best].ref, x, y);  // slot 0 is always filled; slot 1 is empty for a one-child PHR branch
+        if (y.cnt >= 0) {  // replace in place, the second grandchild right after it
+            for (int k = nc; k > best + 1; k--) c[k] = c[k - 1];
+            c[best] = x;
+            c[best + 1] = y;
+            nc++;
+        } else {
+            c[best] = x;
+        }
+    }
+    float lo[3][4], hi[3][4];
+    int32_t ref[4], cnt[4];
+    for (int k = 0; k < 4; k++) {
+        if (k < nc) {
+            for (int a = 0; a < 3; a++) { lo[a][k] = c[k].lo[a]; hi[a][k] = c[k].hi[a]; }
+            cnt[k] = c[k].cnt;
+            ref[k] = c[k].ref;
+            if (c[k].cnt == 0) {
+                uint32_t idx = atomicAdd(n_nodes4, 1u);
+                uint32_t q = atomicAdd(n_out, 1u);
+                if (idx >= cap || q >= cap) {
+                    atomicOr(err, GBT_DEVERR_CAPACITY);
+                    cnt[k] = -1;
+                    continue;
+                }
+                q_out[q] = make_int2(c[k].ref, (int32_t)idx);
+                ref[k] = (int32_t)idx;
+            }
+        } else {
+            for (int a = 0; a < 3; a++) { lo[a][k] = INFINITY; hi[a][k] = -INFINITY; }
+            ref[k] = 0;
+            cnt[k] = -1;
+        }
+    }
+    float4 *nd = out + 8 * (size_t)e.y;
+    nd[0] = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+    nd[1] = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+    nd[2] = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+    nd[3] = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+    nd[4] = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+    nd[5] = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+    reinterpret_cast<int4 *>(nd)[6] = make_int4(ref[0], ref[1], ref[2], ref[3]);
+    reinterpret_cast<int4 *>(nd)[7] = make_int4(cnt[0], cnt[1], cnt[2], cnt[3]);
+}
+
+__global__ void k_collapse_root(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q, uint32_t *n_q,
+                                uint32_t *n_nodes4) {
+    *hdr4 = *hdr;
+    if (hdr->root_cnt == 0) {  // an inner root becomes 4-wide node 0
+        q[0] = make_int2(hdr->root_ref, 0);
+        *n_q = 1;
+        *n_nodes4 = 1;
+        hdr4->root_ref = 0;
+    } else {
+        *n_q = 0;
+        *n_nodes4 = 0;
+    }
+}
+
+}  // namespace
+
+int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
+    if (bvh->arity != 2) return GBT_OK;
+    cudaStream_t st = ctx->stream;
+    BvhHeader h;
+    GBT_CUDA(ctx, cudaMemcpyAsync(&h, bvh->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    const uint32_t cap = h.n_nodes + 1;  // a 4-wide tree never has more nodes than the binary one
+    if (bvh->nodes4_cap < cap) {
+        cudaFree(bvh->d_nodes4);
+        bvh->d_nodes4 = nullptr;
+        bvh->nodes4_cap = 0;
+        if (cudaMalloc(&bvh->d_nodes4, (size_t)cap * 8 * sizeof(float4)) != cudaSuccess) {
+            cudaGetLastError();
+            return gbt_fail(ctx, GBT_ENOMEM, "collapse: node allocation");
+        }
+        bvh->nodes4_cap = cap;
+    }
+    if (!bvh->d_hdr4 && cudaMalloc(&bvh->d_hdr4, sizeof(BvhHeader)) != cudaSuccess) {
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ENOMEM, "collapse: header allocation");
+    }
+    // queues (two halves), counters
+    size_t qbytes = gbt_align((size_t)cap * sizeof(int2));
+    void *scr = nullptr;
+    int rc = gbt_scratch(ctx, 2 * qbytes + 256, &scr);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(scr);
+    int2 *q[2] = {reinterpret_cast<int2 *>(sb), reinterpret_cast<int2 *>(sb + qbytes)};
+    uint32_t *ctr = reinterpret_cast<uint32_t *>(sb + 2 * qbytes);  // [0],[1] queue sizes, [2] node count
+    k_collapse_root<<<1, 1, 0, st>>>(bvh->d_hdr, bvh->d_hdr4, q[0], ctr + 0, ctr + 2);
+    uint32_t n_in = h.root_cnt == 0 ? 1u : 0u;
+    int par = 0;
+    while (n_in > 0) {
+        GBT_CUDA(ctx, cudaMemsetAsync(ctr + (par ^ 1), 0, sizeof(uint32_t), st));
+        k_collapse_level<<<(n_in + 127) / 128, 128, 0, st>>>(bvh->d_nodes, q[par], ctr + par, q[par ^ 1],
+                                                             ctr + (par ^ 1), ctr + 2, bvh->d_nodes4, cap, ctx->d_error);
+        GBT_CUDA(ctx, cudaGetLastError());
+        GBT_CUDA(ctx, cudaMemcpyAsync(&n_in, ctr + (par ^ 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GBT_CUDA(ctx, cudaStreamSynchronize(st));
+        par ^= 1;
+    }
+    bvh->has_nodes4 = 1;
+    return GBT_OK;
+}

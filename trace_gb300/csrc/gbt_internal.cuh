@@ -41,6 +41,14 @@ struct gbt_ctx {
     unsigned long long *d_counters = nullptr;   // [0] inner nodes fetched, [1] primitive tests, [2] rays traced
     float *d_out = nullptr;                     // gbt_render's device image (grow-only)
     size_t d_out_bytes = 0;
+    // batched rendering (batch.cu): item descriptors + accumulators, autotuned launch config
+    void *bstate = nullptr;
+    size_t bstate_bytes = 0;
+    gbt_batch_config batch_cfg{128, 16, 0};
+    int batch_tuned = 0;
+    // traversal kernel: 0 persistent with dynamic ray fetch (default), 1 one thread per ray,
+    // 2 persistent without mid-ray refills (GBT_TRAVERSAL=simple|ww at context creation)
+    int traversal = 0;
 };
 
 // Record a profiling event pair around one traversal launch.
@@ -93,7 +101,15 @@ struct gbt_bvh {
     int32_t *d_other = nullptr;     // emission hand-off words
     uint2 *d_range = nullptr;       // per inner node: distinct-code range [l, r]
     uint32_t n_nodes_host = 0;      // PHR: nodes allocated in d_nodes
+    // 4-wide traversal view of a binary tree (collapse.cu); used by traversal when present
+    float4 *d_nodes4 = nullptr;
+    BvhHeader *d_hdr4 = nullptr;
+    uint32_t nodes4_cap = 0;
+    int has_nodes4 = 0;
 };
+
+// collapse.cu
+int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh);
 
 // ---------------------------------------------------------------------------
 // helpers

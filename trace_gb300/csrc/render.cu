@@ -3,11 +3,11 @@
 // (material.go:13-42) and the miss shaders (render.go:228-246).
 //
 // A wave is a range of path indices g in [0, W*H*spp); path g samples pixel
-// g % (W*H).  Per bounce level b the kernels are
-//   k_raygen (b = 0)   camera rays                          camera.go:95-97, render.go:201-205
-//   traversal          closest hit of every live ray        traverse.cu
-//   k_shade            miss / emission / Lambertian scatter render.go:209-224
-//                      and compaction of the live paths into the next level
+// g % (W*H).  Per bounce level the kernels are
+//   k_raygen (level 0)  camera rays                          camera.go:95-97, render.go:201-205
+//   traversal           closest hit of every live ray        traverse.cu
+//   k_shade             miss / emission / Lambertian scatter render.go:209-224
+//                       and compaction of the live paths into the next level
 // and k_resolve divides the accumulated radiance by spp.  The recursion of the
 // reference, L = Le + albedo * L(next), becomes a throughput T carried along
 // the path: L += T * Le, T *= albedo.  A surface at depth > MaxDepth returns
@@ -17,39 +17,11 @@
 #include <cmath>
 
 #include "gbt_internal.cuh"
-#include "traverse.cuh"
+#include "shade.cuh"
 
 using namespace gbt_dev;
 
 namespace {
-
-struct CamF {
-    float3 origin, llc, hor, ver;
-};
-
-struct ShadeParams {
-    uint32_t npix, width, height, spp;
-    int32_t max_depth;
-    int32_t miss_mode;
-    float3 miss_color;
-    uint32_t seed_lo, seed_hi;
-    uint32_t n_tri;
-};
-
-// Philox-2x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2,
-// 3", SC'11): counter (path, stream) and key from the seed.
-__device__ __forceinline__ uint2 philox2x32(uint32_t c0, uint32_t c1, uint32_t key) {
-#pragma unroll
-    for (int i = 0; i < 10; i++) {
-        uint32_t hi = __umulhi(0xD256D193u, c0);
-        uint32_t lo = 0xD256D193u * c0;
-        c0 = hi ^ key ^ c1;
-        c1 = lo;
-        key += 0x9E3779B9u;
-    }
-    return make_uint2(c0, c1);
-}
-__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
 __global__ void __launch_bounds__(256) k_raygen(CamF cam, ShadeParams sp, uint32_t g0, uint32_t count,
                                                 float4 *__restrict__ rays, float4 *__restrict__ aux, uint32_t *counts) {
@@ -57,35 +29,12 @@ __global__ void __launch_bounds__(256) k_raygen(CamF cam, ShadeParams sp, uint32
     if (i == 0) counts[0] = count;
     if (i >= count) return;
     uint32_t g = g0 + i;
-    uint32_t pix = g % sp.npix;
-    uint32_t x = pix % sp.width, y = pix / sp.width;
-    uint2 rnd = philox2x32(g, 0xFFFFu, sp.seed_lo ^ sp.seed_hi);
-    float s = ((float)x + u01(rnd.x)) / (float)(sp.width - 1);   // RandomSampling: /(w-1)
-    float t = ((float)y + u01(rnd.y)) / (float)(sp.height - 1);
-    float3 d = sub3(add3(add3(cam.llc, mul3(cam.hor, s)), mul3(cam.ver, t)), cam.origin);
-    rays[2 * (size_t)i] = make_float4(cam.origin.x, cam.origin.y, cam.origin.z, 0.001f);
+    float3 o, d;
+    primary_ray(cam, sp, g, o, d);
+    rays[2 * (size_t)i] = make_float4(o.x, o.y, o.z, 0.001f);
     rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
     aux[2 * (size_t)i] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)g));
     aux[2 * (size_t)i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-__device__ __forceinline__ float3 miss_colour(const ShadeParams &sp, float3 d) {
-    switch (sp.miss_mode) {
-    case GBT_MISS_WHITE: return f3(1.f, 1.f, 1.f);
-    case GBT_MISS_SKY: {
-        float inv = rsqrtf(dot3(d, d));
-        float t = 0.5f * (d.y * inv + 1.f);
-        return f3(0.8f * (1.f - t) + 0.25f * t, 0.8f * (1.f - t) + 0.35f * t, 0.8f * (1.f - t) + 0.5f * t);
-    }
-    case GBT_MISS_CONSTANT: return sp.miss_color;
-    default: return f3(0.f, 0.f, 0.f);
-    }
-}
-
-__device__ __forceinline__ void deposit(float *__restrict__ acc, uint32_t pix, float3 L) {
-    if (L.x != 0.f) atomicAdd(acc + 3 * (size_t)pix, L.x);
-    if (L.y != 0.f) atomicAdd(acc + 3 * (size_t)pix + 1, L.y);
-    if (L.z != 0.f) atomicAdd(acc + 3 * (size_t)pix + 2, L.z);
 }
 
 __global__ void __launch_bounds__(256) k_shade(ShadeParams sp, int level, const float4 *__restrict__ rays_in,
@@ -103,61 +52,18 @@ __global__ void __launch_bounds__(256) k_shade(ShadeParams sp, int level, const 
         float4 a0 = aux_in[2 * (size_t)i], a1 = aux_in[2 * (size_t)i + 1];
         float3 T = f3(a0.x, a0.y, a0.z), L = f3(a1.x, a1.y, a1.z);
         uint32_t g = (uint32_t)__float_as_int(a0.w);
-        uint32_t pix = g % sp.npix;
         float4 h = hits[i];
-        int rec = __float_as_int(h.w);
         float4 ro = rays_in[2 * (size_t)i], rd = rays_in[2 * (size_t)i + 1];
-        float3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z);
-        if (rec < 0) {
-            L = add3(L, emul3(T, miss_colour(sp, d)));
-            deposit(acc, pix, L);
-        } else if (level > sp.max_depth) {
-            deposit(acc, pix, L);  // render.go:210-212: beyond MaxDepth the surface returns black
+        float3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z), no, nd;
+        alive = shade_step(sp, level, g, o, d, h.x, h.y, h.z, __float_as_int(h.w), recs, prim_mat, mats, normals, T, L,
+                           no, nd);
+        if (alive) {
+            out_r0 = make_float4(no.x, no.y, no.z, 0.0001f);
+            out_r1 = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
+            out_a0 = make_float4(T.x, T.y, T.z, a0.w);
+            out_a1 = make_float4(L.x, L.y, L.z, 0.f);
         } else {
-            const float4 *pr = recs + 3 * (size_t)rec;
-            float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
-            uint32_t id = (uint32_t)__float_as_int(r0.w);
-            float4 m = __ldg(mats + __ldg(prim_mat + id));
-            float3 col = f3(m.x, m.y, m.z);
-            if (__float_as_int(m.w) == GBT_MAT_LIGHT) {
-                L = add3(L, emul3(T, col));
-                deposit(acc, pix, L);
-            } else {
-                float3 p = add3(o, mul3(d, h.x));  // ray.position(t)
-                float3 nrm;
-                if (__float_as_int(r1.w) == 0) {
-                    float4 r2 = __ldg(pr + 2);
-                    float3 e1 = f3(r1.x - r0.x, r1.y - r0.y, r1.z - r0.z), e2 = f3(r2.x - r0.x, r2.y - r0.y, r2.z - r0.z);
-                    float3 ng = cross3(e1, e2);
-                    bool front = dot3(d, ng) < 0.f;  // det > 0 (primitive.go:201)
-                    if (normals) {                   // interpolated vertex normals (primitive.go:144-150)
-                        const float *nv = normals + 9 * (size_t)id;
-                        float w = 1.f - h.y - h.z;
-                        nrm = f3(nv[3] * h.y + nv[6] * h.z + nv[0] * w, nv[4] * h.y + nv[7] * h.z + nv[1] * w,
-                                 nv[5] * h.y + nv[8] * h.z + nv[2] * w);
-                    } else {
-                        nrm = mul3(ng, rsqrtf(dot3(ng, ng)));
-                    }
-                    if (!front) nrm = mul3(nrm, -1.f);
-                } else {
-                    nrm = mul3(sub3(p, f3(r0.x, r0.y, r0.z)), 1.f / r1.x);
-                    if (!(dot3(d, nrm) < 0.f)) nrm = mul3(nrm, -1.f);
-                }
-                // Diffuse.scatter: normal + RandomUnitVector (uniform on the sphere)
-                uint2 rnd = philox2x32(g, (uint32_t)level, sp.seed_lo ^ sp.seed_hi);
-                float z = 1.f - 2.f * u01(rnd.x);
-                float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
-                float sphi, cphi;
-                sincospif(2.f * u01(rnd.y), &sphi, &cphi);
-                float3 sd = f3(nrm.x + rr * cphi, nrm.y + rr * sphi, nrm.z + z);
-                if (fabsf(sd.x) <= 1e-7f && fabsf(sd.y) <= 1e-7f && fabsf(sd.z) <= 1e-7f) sd = nrm;
-                T = emul3(T, col);
-                alive = true;
-                out_r0 = make_float4(p.x, p.y, p.z, 0.0001f);
-                out_r1 = make_float4(sd.x, sd.y, sd.z, __int_as_float(0x7f800000));
-                out_a0 = make_float4(T.x, T.y, T.z, a0.w);
-                out_a1 = make_float4(L.x, L.y, L.z, 0.f);
-            }
+            deposit(acc, g % sp.npix, L);
         }
     }
     // compaction: one atomic per warp
@@ -193,8 +99,9 @@ __global__ void k_sum_counts(const uint32_t *counts, int levels, unsigned long l
     }
 }
 
-CamF make_cam(const gbt_camera *c) {
-    // camera.go:53-66 in float64, then rounded
+}  // namespace
+
+CamF gbt_make_cam(const gbt_camera *c) {
     auto sub = [](const double *a, const double *b, double *o) { for (int k = 0; k < 3; k++) o[k] = a[k] - b[k]; };
     auto unit = [](double *v) { double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); for (int k = 0; k < 3; k++) v[k] /= l; };
     auto cross = [](const double *a, const double *b, double *o) {
@@ -223,14 +130,27 @@ CamF make_cam(const gbt_camera *c) {
     return f;
 }
 
-}  // namespace
+ShadeParams gbt_make_shade_params(const gbt_render_params *p, uint32_t n_tri) {
+    ShadeParams sp;
+    sp.npix = (uint32_t)p->width * (uint32_t)p->height;
+    sp.width = (uint32_t)p->width;
+    sp.height = (uint32_t)p->height;
+    sp.spp = (uint32_t)p->spp;
+    sp.max_depth = p->max_depth;
+    sp.miss_mode = p->miss_mode;
+    sp.miss_color = make_float3(p->miss_color[0], p->miss_color[1], p->miss_color[2]);
+    sp.seed_lo = (uint32_t)p->seed;
+    sp.seed_hi = (uint32_t)(p->seed >> 32);
+    sp.n_tri = n_tri;
+    return sp;
+}
 
 // Per-context render state: ping-pong path buffers, hits, counters, accumulator.
 struct RenderState {
-    size_t cap;           // paths per wave
+    size_t cap;  // paths per wave
     float4 *rays[2], *aux[2];
     float4 *hits;
-    uint32_t *counts;     // per level
+    uint32_t *counts;  // per level
     float *acc;
 };
 
@@ -242,25 +162,37 @@ static size_t render_layout(size_t cap, size_t npix, size_t *off) {
     off[3] = o; o = gbt_align(o + cap * 32);  // aux[1]
     off[4] = o; o = gbt_align(o + cap * 16);  // hits
     off[5] = o; o = gbt_align(o + 64 * sizeof(uint32_t));
-    off[6] = o; o = gbt_align(o + sizeof(unsigned long long));
-    off[7] = o; o = gbt_align(o + npix * 3 * sizeof(float));
+    off[6] = o; o = gbt_align(o + npix * 3 * sizeof(float));
     return o;
 }
 
-int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p, float *d_rgb) {
+int gbt_render_check(gbt_ctx *ctx, const gbt_render_params *p) {
     if (p->width < 2 || p->height < 2 || p->spp < 1 || p->max_depth < 0 || p->max_depth > 60)
         return gbt_fail(ctx, GBT_EINVAL, "render: width/height >= 2, spp >= 1, 0 <= max_depth <= 60");
+    if ((uint64_t)p->width * p->height * (uint64_t)p->spp >= (1ull << 32))
+        return gbt_fail(ctx, GBT_EINVAL, "render: width*height*spp must be < 2^32");
+    return GBT_OK;
+}
+
+int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p, float *d_rgb) {
+    int rc = gbt_render_check(ctx, p);
+    if (rc) return rc;
     const size_t npix = (size_t)p->width * p->height;
     const size_t total = npix * (size_t)p->spp;
-    if (total >= (1ull << 32)) return gbt_fail(ctx, GBT_EINVAL, "render: width*height*spp must be < 2^32");
     size_t cap = total < (size_t)(1u << 23) ? total : (size_t)(1u << 23);
-    size_t off[8];
+    size_t off[7];
     size_t need = render_layout(cap, npix, off);
     if (ctx->rstate_bytes < need) {
-        if (ctx->rstate) cudaFree(ctx->rstate);
+        if (ctx->rstate) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->rstate);
+        }
         ctx->rstate = nullptr;
         ctx->rstate_bytes = 0;
-        if (cudaMalloc(&ctx->rstate, need) != cudaSuccess) return gbt_fail(ctx, GBT_ENOMEM, "render: state allocation");
+        if (cudaMalloc(&ctx->rstate, need) != cudaSuccess) {
+            cudaGetLastError();
+            return gbt_fail(ctx, GBT_ENOMEM, "render: state allocation");
+        }
         ctx->rstate_bytes = need;
     }
     unsigned char *b = static_cast<unsigned char *>(ctx->rstate);
@@ -272,22 +204,12 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
     rs.aux[1] = reinterpret_cast<float4 *>(b + off[3]);
     rs.hits = reinterpret_cast<float4 *>(b + off[4]);
     rs.counts = reinterpret_cast<uint32_t *>(b + off[5]);
-    rs.acc = reinterpret_cast<float *>(b + off[7]);
+    rs.acc = reinterpret_cast<float *>(b + off[6]);
 
     cudaStream_t st = ctx->stream;
     gbt_scene *sc = bvh->scene;
-    CamF cf = make_cam(cam);
-    ShadeParams sp;
-    sp.npix = (uint32_t)npix;
-    sp.width = (uint32_t)p->width;
-    sp.height = (uint32_t)p->height;
-    sp.spp = (uint32_t)p->spp;
-    sp.max_depth = p->max_depth;
-    sp.miss_mode = p->miss_mode;
-    sp.miss_color = make_float3(p->miss_color[0], p->miss_color[1], p->miss_color[2]);
-    sp.seed_lo = (uint32_t)p->seed;
-    sp.seed_hi = (uint32_t)(p->seed >> 32);
-    sp.n_tri = sc->n_tri;
+    CamF cf = gbt_make_cam(cam);
+    ShadeParams sp = gbt_make_shade_params(p, sc->n_tri);
     const int levels = p->max_depth + 2;  // surfaces at depth 0..MaxDepth+1 are traced
 
     GBT_CUDA(ctx, cudaMemsetAsync(rs.acc, 0, npix * 3 * sizeof(float), st));

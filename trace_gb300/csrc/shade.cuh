@@ -1,0 +1,149 @@
+// Camera rays and surface shading shared by the wavefront renderer and the
+// batched persistent renderer, so that both trace exactly the same paths.
+//
+//   primary_ray   castRayReuse (camera.go:95-97) with RandomSampling's
+//                 u = (x + xi) / (w - 1), v = (y + xi) / (h - 1) (render.go:201-205)
+//   shade_step    DefaultClosestHitShader (render.go:209-224): miss colour,
+//                 Light emission, Diffuse scatter = normal + uniform unit vector
+//                 (material.go:29-38, util.go:15-26), MaxDepth cut-off
+// Random numbers are Philox-2x32-10 keyed by the seed with counter (path, level),
+// so a path is the same whichever kernel traces it.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbt_internal.cuh"
+#include "traverse.cuh"
+
+namespace gbt_dev {
+
+struct CamF {
+    float3 origin, llc, hor, ver;
+};
+
+struct ShadeParams {
+    uint32_t npix, width, height, spp;
+    int32_t max_depth;
+    int32_t miss_mode;
+    float3 miss_color;
+    uint32_t seed_lo, seed_hi;
+    uint32_t n_tri;
+};
+
+// Philox-2x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2,
+// 3", SC'11): counter (path, stream) and key from the seed.
+__device__ __forceinline__ uint2 philox2x32(uint32_t c0, uint32_t c1, uint32_t key) {
+#pragma unroll
+    for (int i = 0; i < 10; i++) {
+        uint32_t hi = __umulhi(0xD256D193u, c0);
+        uint32_t lo = 0xD256D193u * c0;
+        c0 = hi ^ key ^ c1;
+        c1 = lo;
+        key += 0x9E3779B9u;
+    }
+    return make_uint2(c0, c1);
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// Primary ray of path g (pixel g % npix).
+__device__ __forceinline__ void primary_ray(const CamF &cam, const ShadeParams &sp, uint32_t g, float3 &o, float3 &d) {
+    uint32_t pix = g % sp.npix;
+    uint32_t x = pix % sp.width, y = pix / sp.width;
+    uint2 rnd = philox2x32(g, 0xFFFFu, sp.seed_lo ^ sp.seed_hi);
+    float s = ((float)x + u01(rnd.x)) / (float)(sp.width - 1);
+    float t = ((float)y + u01(rnd.y)) / (float)(sp.height - 1);
+    d = sub3(add3(add3(cam.llc, mul3(cam.hor, s)), mul3(cam.ver, t)), cam.origin);
+    o = cam.origin;
+}
+
+__device__ __forceinline__ float3 miss_colour(const ShadeParams &sp, float3 d) {
+    switch (sp.miss_mode) {
+    case GBT_MISS_WHITE: return f3(1.f, 1.f, 1.f);
+    case GBT_MISS_SKY: {
+        float inv = rsqrtf(dot3(d, d));
+        float t = 0.5f * (d.y * inv + 1.f);
+        return f3(0.8f * (1.f - t) + 0.25f * t, 0.8f * (1.f - t) + 0.35f * t, 0.8f * (1.f - t) + 0.5f * t);
+    }
+    case GBT_MISS_CONSTANT: return sp.miss_color;
+    default: return f3(0.f, 0.f, 0.f);
+    }
+}
+
+__device__ __forceinline__ void deposit(float *__restrict__ acc, uint32_t pix, float3 L) {
+    if (L.x != 0.f) atomicAdd(acc + 3 * (size_t)pix, L.x);
+    if (L.y != 0.f) atomicAdd(acc + 3 * (size_t)pix + 1, L.y);
+    if (L.z != 0.f) atomicAdd(acc + 3 * (size_t)pix + 2, L.z);
+}
+
+// Diffuse.scatter (material.go:29-38): hit point p and the new direction
+// normal + uniform unit vector (util.go:15-26) for a triangle or sphere record.
+__device__ __forceinline__ void diffuse_scatter(const float4 *__restrict__ recs, const float *__restrict__ normals,
+                                                int rec, float3 o, float3 d, float t, float u, float v, uint32_t g,
+                                                int level, const ShadeParams &sp, float3 &p, float3 &sd) {
+    const float4 *pr = recs + 3 * (size_t)rec;
+    float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+    p = add3(o, mul3(d, t));  // ray.position(t)
+    float3 nrm;
+    if (__float_as_int(r1.w) == 0) {
+        float4 r2 = __ldg(pr + 2);
+        float3 e1 = f3(r1.x - r0.x, r1.y - r0.y, r1.z - r0.z), e2 = f3(r2.x - r0.x, r2.y - r0.y, r2.z - r0.z);
+        float3 ng = cross3(e1, e2);
+        bool front = dot3(d, ng) < 0.f;  // det > 0 (primitive.go:201)
+        if (normals) {                   // interpolated vertex normals (primitive.go:144-150)
+            const float *nv = normals + 9 * (size_t)(uint32_t)__float_as_int(r0.w);
+            float w = 1.f - u - v;
+            nrm = f3(nv[3] * u + nv[6] * v + nv[0] * w, nv[4] * u + nv[7] * v + nv[1] * w,
+                     nv[5] * u + nv[8] * v + nv[2] * w);
+        } else {
+            nrm = mul3(ng, rsqrtf(dot3(ng, ng)));
+        }
+        if (!front) nrm = mul3(nrm, -1.f);
+    } else {
+        nrm = mul3(sub3(p, f3(r0.x, r0.y, r0.z)), 1.f / r1.x);
+        if (!(dot3(d, nrm) < 0.f)) nrm = mul3(nrm, -1.f);
+    }
+    uint2 rnd = philox2x32(g, (uint32_t)level, sp.seed_lo ^ sp.seed_hi);
+    float z = 1.f - 2.f * u01(rnd.x);
+    float rr = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float sphi, cphi;
+    sincospif(2.f * u01(rnd.y), &sphi, &cphi);
+    sd = f3(nrm.x + rr * cphi, nrm.y + rr * sphi, nrm.z + z);
+    if (fabsf(sd.x) <= 1e-7f && fabsf(sd.y) <= 1e-7f && fabsf(sd.z) <= 1e-7f) sd = nrm;
+}
+
+// One shading event of path g at bounce `level` for ray (o, d) with the
+// closest hit (t, u, v, rec).  Updates throughput T and radiance L.  Returns
+// true when the path continues with the new ray (no, nd); false when it ends
+// (L is then final).
+__device__ __forceinline__ bool shade_step(const ShadeParams &sp, int level, uint32_t g, float3 o, float3 d, float t,
+                                           float u, float v, int rec, const float4 *__restrict__ recs,
+                                           const uint32_t *__restrict__ prim_mat, const float4 *__restrict__ mats,
+                                           const float *__restrict__ normals, float3 &T, float3 &L, float3 &no,
+                                           float3 &nd) {
+    if (rec < 0) {
+        L = add3(L, emul3(T, miss_colour(sp, d)));
+        return false;
+    }
+    if (level > sp.max_depth) return false;  // render.go:210-212: beyond MaxDepth the surface returns black
+    const float4 *pr = recs + 3 * (size_t)rec;
+    float4 r0 = __ldg(pr), r1 = __ldg(pr + 1);
+    uint32_t id = (uint32_t)__float_as_int(r0.w);
+    float4 m = __ldg(mats + __ldg(prim_mat + id));
+    float3 col = f3(m.x, m.y, m.z);
+    if (__float_as_int(m.w) == GBT_MAT_LIGHT) {
+        L = add3(L, emul3(T, col));
+        return false;
+    }
+    float3 p, sd;
+    diffuse_scatter(recs, normals, rec, o, d, t, u, v, g, level, sp, p, sd);
+    T = emul3(T, col);
+    no = p;
+    nd = sd;
+    return true;
+}
+
+}  // namespace gbt_dev
+
+// host: camera basis of camera.go:53-66 computed in float64 and rounded
+gbt_dev::CamF gbt_make_cam(const gbt_camera *c);
+gbt_dev::ShadeParams gbt_make_shade_params(const gbt_render_params *p, uint32_t n_tri);

@@ -71,13 +71,152 @@ __global__ void __launch_bounds__(128) k_trace4(const BvhHeader *__restrict__ hd
     flush_work<COUNT>(w, counters);
 }
 
+__device__ __forceinline__ uint32_t lane_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <int W, bool COUNT, int DYN>
+__global__ void __launch_bounds__(128) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+                                                  const float4 *__restrict__ recs, const float4 *__restrict__ rays,
+                                                  float4 *__restrict__ hits, uint32_t n,
+                                                  const uint32_t *__restrict__ d_count, int out_mode, unsigned int *err,
+                                                  unsigned long long *counters, uint32_t *fetch) {
+    constexpr int STACK = W == 2 ? 64 : 96;
+    const uint32_t total = d_count ? *d_count : n;
+    const uint32_t lane = threadIdx.x & 31;
+    gbt_dev::LocalStack<STACK> st;
+    int sp = 0;
+    int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
+    gbt_dev::Ray r;
+    gbt_dev::Hit h;
+    gbt_dev::Work w;
+    h.t = 0.f;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    uint32_t rid = 0xffffffffu;
+    bool pool_empty = false;  // warp-uniform
+    for (;;) {
+        if (node.y < 0 && leaf.y <= 0 && rid != 0xffffffffu) {  // this lane's ray is done
+            gbt_dev::store_hit(hits, rid, h, recs, out_mode);
+            rid = 0xffffffffu;
+        }
+        const bool want = rid == 0xffffffffu && !pool_empty;
+        const uint32_t need = __ballot_sync(0xffffffffu, want);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == (uint32_t)leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            bool empty_here = false;
+            if (want) {
+                const uint32_t id = base + __popc(need & lane_lt());
+                if (id < total) {
+                    rid = id;
+                    r = gbt_dev::load_ray(rays, id);
+                    h.t = r.tmax;
+                    h.u = h.v = 0.f;
+                    h.rec = -1;
+                    sp = 0;
+                    leaf = make_int2(0, 0);
+                    float te;
+                    const float *lo = hdr->root_lo, *hi = hdr->root_hi;
+                    node = gbt_dev::slab(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], r, h.t, te)
+                               ? make_int2(hdr->root_ref, hdr->root_cnt)
+                               : make_int2(0, -1);
+                    if (node.y > 0) {  // a leaf root
+                        leaf = node;
+                        node = make_int2(0, -1);
+                    }
+                } else {
+                    empty_here = true;
+                }
+            }
+            pool_empty = __any_sync(0xffffffffu, empty_here) || pool_empty;
+        }
+        if (__all_sync(0xffffffffu, rid == 0xffffffffu)) break;
+        while (node.y >= 0 || leaf.y > 0) {
+            while (node.y == 0) {
+                if (COUNT) w.nodes++;
+                node = W == 2 ? gbt_dev::step2(nodes, node, st, sp, r, h.t, err)
+                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err);
+                if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf, keep descending
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                }
+                if (!__any_sync(__activemask(), leaf.y <= 0)) break;  // every lane here holds a leaf
+            }
+            while (leaf.y > 0) {
+                if (COUNT) w.prims += (uint32_t)leaf.y;
+                gbt_dev::leaf(recs, leaf.x, leaf.y, r, h);
+                if (node.y > 0) {
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                } else {
+                    leaf = make_int2(0, 0);
+                }
+            }
+            if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
+        }
+    }
+    flush_work<COUNT>(w, counters);
+}
+
+template <int W, bool COUNT, int DYN>
+void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
+               float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
+               cudaStream_t s) {
+    static int per_sm = 0;  // resident blocks per SM of this instantiation
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN>, 128, 0);
+        if (per_sm <= 0) per_sm = 1;
+    }
+    uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
+    cudaMemsetAsync(fetch, 0, sizeof(uint32_t), s);
+    uint32_t grid = (uint32_t)(ctx->num_sms * per_sm);
+    uint32_t need = (n + 127) / 128;
+    if (need < grid) grid = need;
+    k_trace_pt<W, COUNT, DYN><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
+                                                  counters, fetch);
+}
+
+template <int W, int DYN>
+void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
+                   float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
+                   cudaStream_t s) {
+    if (counters) launch_pt<W, true, DYN>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+    else launch_pt<W, false, DYN>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+}
+
 }  // namespace
 
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, const uint32_t *d_count,
                          int out_mode, unsigned int *d_error, cudaStream_t s, unsigned long long *counters) {
     if (n == 0) return;
     uint32_t blocks = (n + 127) / 128;
-    if (bvh->arity == 4) {
+    gbt_ctx *ctx = bvh->ctx;
+    if (ctx && ctx->traversal != 1) {  // persistent kernels
+        const bool four = bvh->has_nodes4 || bvh->arity == 4;
+        const BvhHeader *hd = bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr;
+        const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
+        const bool dyn = ctx->traversal == 0;
+        if (four) {
+            if (dyn) launch_pt_any<4, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+            else launch_pt_any<4, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+        } else {
+            if (dyn) launch_pt_any<2, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+            else launch_pt_any<2, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+        }
+        return;
+    }
+    (void)d_error;
+    if (bvh->has_nodes4) {  // the 4-wide view of a binary tree
+        if (counters)
+            k_trace4<true><<<blocks, 128, 0, s>>>(bvh->d_hdr4, bvh->d_nodes4, bvh->d_prims, rays, hits, n, d_count, out_mode, d_error, counters);
+        else
+            k_trace4<false><<<blocks, 128, 0, s>>>(bvh->d_hdr4, bvh->d_nodes4, bvh->d_prims, rays, hits, n, d_count, out_mode, d_error, nullptr);
+    } else if (bvh->arity == 4) {
         if (counters)
             k_trace4<true><<<blocks, 128, 0, s>>>(bvh->d_hdr, bvh->d_nodes, bvh->d_prims, rays, hits, n, d_count, out_mode, d_error, counters);
         else

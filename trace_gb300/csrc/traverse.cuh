@@ -253,6 +253,140 @@ __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *
     return h;
 }
 
+// ---------------------------------------------------------------------------
+// Persistent traversal: each warp keeps its lanes busy by fetching new rays as
+// old ones finish, and runs inner-node steps until every busy lane holds a leaf
+// before testing primitives ("while-while" with postponed leaves, after Aila &
+// Laine, HPG 2009), so inner-node and leaf work are not interleaved across
+// lanes of one warp.  The scalar state (current entry, postponed leaf, stack
+// depth) stays in registers; only the stack arrays live in local memory.
+// ---------------------------------------------------------------------------
+// Traversal stacks: entries (ref, cnt) with the entry distance used to skip
+// subtrees that lie beyond the current closest hit.
+template <int STACK>
+struct LocalStack {  // all entries in local memory
+    int2 e[STACK];
+    float t[STACK];
+    __device__ __forceinline__ void push(int &sp, int2 v, float tv, unsigned int *err) {
+        if (sp < STACK) {
+            e[sp] = v;
+            t[sp] = tv;
+            ++sp;
+        } else {
+            atomicOr(err, GBT_DEVERR_STACK);
+        }
+    }
+    __device__ __forceinline__ int2 pop(int &sp, float tmax) {
+        while (sp > 0) {
+            --sp;
+            if (t[sp] <= tmax * 1.0000005f) return e[sp];
+        }
+        return make_int2(0, -1);
+    }
+};
+
+// The top SH entries of each thread's stack in shared memory (column `lane`
+// of a [SH][stride] array), deeper entries in local memory.
+template <int STACK, int SH>
+struct SharedTopStack {
+    int2 *se;
+    float *st;
+    int stride;
+    int2 e[STACK - SH];
+    float t[STACK - SH];
+    __device__ __forceinline__ void push(int &sp, int2 v, float tv, unsigned int *err) {
+        if (sp < SH) {
+            se[sp * stride] = v;
+            st[sp * stride] = tv;
+            ++sp;
+        } else if (sp < STACK) {
+            e[sp - SH] = v;
+            t[sp - SH] = tv;
+            ++sp;
+        } else {
+            atomicOr(err, GBT_DEVERR_STACK);
+        }
+    }
+    __device__ __forceinline__ int2 pop(int &sp, float tmax) {
+        while (sp > 0) {
+            --sp;
+            float tv = sp < SH ? st[sp * stride] : t[sp - SH];
+            if (tv <= tmax * 1.0000005f) return sp < SH ? se[sp * stride] : e[sp - SH];
+        }
+        return make_int2(0, -1);
+    }
+};
+
+// One inner-node step on a binary node: returns the next entry.
+template <class StackT>
+__device__ __forceinline__ int2 step2(const float4 *__restrict__ nodes, int2 node, StackT &st, int &sp, const Ray &r,
+                                      float tmax, unsigned int *err) {
+    const float4 *nd = nodes + 4 * (size_t)node.x;
+    float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
+    int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+    float t0, t1;
+    bool h0 = n3.y >= 0 && slab(n0.x, n0.z, n2.x, n0.y, n0.w, n2.y, r, tmax, t0);
+    bool h1 = n3.w >= 0 && slab(n1.x, n1.z, n2.z, n1.y, n1.w, n2.w, r, tmax, t1);
+    if (h0 && h1) {
+        int2 a = make_int2(n3.x, n3.y), b = make_int2(n3.z, n3.w);
+        if (t1 < t0) {
+            st.push(sp, a, t0, err);
+            return b;
+        }
+        st.push(sp, b, t1, err);
+        return a;
+    }
+    if (h0) return make_int2(n3.x, n3.y);
+    if (h1) return make_int2(n3.z, n3.w);
+    return st.pop(sp, tmax);
+}
+
+struct Cand {
+    float t;
+    int2 e;
+};
+
+__device__ __forceinline__ void cx(Cand &a, Cand &b) {  // compare-exchange, ascending by t
+    if (b.t < a.t) {
+        Cand x = a;
+        a = b;
+        b = x;
+    }
+}
+
+// One inner-node step on a 4-wide node: children sorted near to far by a
+// register sorting network, the nearest taken, the others pushed far first.
+template <class StackT>
+__device__ __forceinline__ int2 step4(const float4 *__restrict__ nodes, int2 node, StackT &st, int &sp, const Ray &r,
+                                      float tmax, unsigned int *err) {
+    const float4 *nd = nodes + 8 * (size_t)node.x;
+    float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
+    float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+    int4 rf = __ldg(reinterpret_cast<const int4 *>(nd + 6));
+    int4 cn = __ldg(reinterpret_cast<const int4 *>(nd + 7));
+    const float MISS = __int_as_float(0x7f800000);
+    Cand c0, c1, c2, c3;
+    float t;
+    c0.t = (cn.x >= 0 && slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, tmax, t)) ? t : MISS;
+    c1.t = (cn.y >= 0 && slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, tmax, t)) ? t : MISS;
+    c2.t = (cn.z >= 0 && slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, tmax, t)) ? t : MISS;
+    c3.t = (cn.w >= 0 && slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, tmax, t)) ? t : MISS;
+    c0.e = make_int2(rf.x, cn.x);
+    c1.e = make_int2(rf.y, cn.y);
+    c2.e = make_int2(rf.z, cn.z);
+    c3.e = make_int2(rf.w, cn.w);
+    cx(c0, c1);
+    cx(c2, c3);
+    cx(c0, c2);
+    cx(c1, c3);
+    cx(c1, c2);
+    if (c0.t == MISS) return st.pop(sp, tmax);
+    if (c3.t != MISS) st.push(sp, c3.e, c3.t, err);
+    if (c2.t != MISS) st.push(sp, c2.e, c2.t, err);
+    if (c1.t != MISS) st.push(sp, c1.e, c1.t, err);
+    return c0.e;
+}
+
 // out_mode 0: gbt_hit (primitive id, t, u, v); 1: (t, u, v, record) for the renderer
 __device__ __forceinline__ void store_hit(float4 *__restrict__ hits, uint32_t i, const Hit &h,
                                           const float4 *__restrict__ recs, int out_mode) {

@@ -218,6 +218,150 @@ class BVH:
         return img, dict(rays_traced=st.rays_traced, paths=st.paths, ms=st.ms_total)
 
 
+class Batch:
+    """Many renders in one call (gbt_render_batch_async): items of (BVH, camera, params)."""
+
+    def __init__(self, ctx, bvhs, cameras, params):
+        self.ctx = ctx
+        n = len(bvhs)
+        self.items = (_lib.BatchItem * n)()
+        self.images = []
+        self.bvhs = list(bvhs)  # kept alive with the batch
+        self.paths = 0
+        for i, (b, cam, p) in enumerate(zip(bvhs, cameras, params)):
+            it = self.items[i]
+            it.bvh = b.h
+            it.camera = cam if isinstance(cam, _lib.Camera) else make_camera(cam)
+            w, h = int(p["width"]), int(p["height"])
+            it.params = _lib.RenderParams(w, h, int(p["spp"]), int(p["max_depth"]), int(p.get("miss_mode", 0)),
+                                          (C.c_float * 3)(*p.get("miss_color", (0, 0, 0))), int(p.get("seed", 1)))
+            d = ctx.alloc(w * h * 3 * 4)
+            it.d_rgb = d
+            self.images.append((d, h, w))
+            self.paths += w * h * int(p["spp"])
+        self.n = n
+        self.graph = None
+
+    def render(self, mode="batched", cfg=None):
+        L, h = self.ctx.L, self.ctx.h
+        if mode == "batched":
+            self.ctx.check(L.gbt_render_batch_async(h, self.items, self.n, C.byref(cfg) if cfg else None), "batch")
+        elif mode == "plain":
+            self.ctx.check(L.gbt_render_batch_plain_async(h, self.items, self.n), "batch plain")
+        elif mode == "graph":
+            self.ctx.check(L.gbt_graph_launch(h, self.graph), "graph launch")
+        else:
+            raise ValueError(mode)
+
+    def autotune(self):
+        best = _lib.BatchConfig()
+        ms = C.c_double()
+        self.ctx.check(self.ctx.L.gbt_batch_autotune(self.ctx.h, self.items, self.n, C.byref(best), C.byref(ms)),
+                       "autotune")
+        return best, ms.value
+
+    def make_graph(self, rebuild=False, cfg=None):
+        g = C.c_void_p()
+        self.ctx.check(self.ctx.L.gbt_batch_graph_create(self.ctx.h, self.items, self.n, C.byref(cfg) if cfg else None,
+                                                         1 if rebuild else 0, C.byref(g)), "graph create")
+        self.graph = g
+
+    def read(self, i):
+        d, h, w = self.images[i]
+        img = np.empty((h, w, 3), np.float32)
+        self.ctx.d2h(img, d)
+        self.ctx.sync()
+        return img
+
+    def close(self):
+        if self.graph:
+            self.ctx.L.gbt_graph_destroy(self.graph)
+            self.graph = None
+        for d, _, _ in self.images:
+            self.ctx.free(d)
+        self.images = []
+
+
+class RenderFunction:
+    """Differentiable render with Forward/Backward in the manner of
+    torch.autograd.Function (gbt_adjoint_*): per-triangle albedo (n, 3) and
+    emission (n,) in, image out; Backward maps dLoss/dImage to the parameter
+    gradients by path replay."""
+
+    def __init__(self, bvh, camera, params):
+        self.ctx, self.bvh = bvh.ctx, bvh
+        self.cam = camera if isinstance(camera, _lib.Camera) else make_camera(camera)
+        p = params
+        self.w, self.h = int(p["width"]), int(p["height"])
+        self.params = _lib.RenderParams(self.w, self.h, int(p["spp"]), int(p["max_depth"]), int(p.get("miss_mode", 0)),
+                                        (C.c_float * 3)(*p.get("miss_color", (0, 0, 0))), int(p.get("seed", 1)))
+        n = bvh.scene.verts.shape[0]
+        self.n = n
+        c = self.ctx
+        npx = self.w * self.h * 3
+        self.d_alb, self.d_emi = c.alloc(n * 12), c.alloc(n * 4)
+        self.d_img, self.d_tgt, self.d_dimg = c.alloc(npx * 4), c.alloc(npx * 4), c.alloc(npx * 4)
+        self.d_ga, self.d_ge, self.d_loss = c.alloc(n * 12), c.alloc(n * 4), c.alloc(8)
+
+    def _set(self, albedo, emission):
+        self.ctx.h2d(self.d_alb, np.ascontiguousarray(albedo, np.float32).reshape(self.n, 3))
+        self.ctx.h2d(self.d_emi, np.ascontiguousarray(emission, np.float32).reshape(self.n))
+
+    def Forward(self, albedo, emission):
+        self._set(albedo, emission)
+        L, h = self.ctx.L, self.ctx.h
+        self.ctx.check(L.gbt_adjoint_forward_async(h, self.bvh.h, C.byref(self.cam), C.byref(self.params),
+                                                   C.c_void_p(self.d_alb), C.c_void_p(self.d_emi),
+                                                   C.c_void_p(self.d_img)), "adjoint forward")
+        img = np.empty((self.h, self.w, 3), np.float32)
+        self.ctx.d2h(img, self.d_img)
+        self.ctx.sync()
+        return img
+
+    def Backward(self, dimage):
+        """dLoss/dImage (h, w, 3) -> (dLoss/dalbedo (n, 3), dLoss/demission (n,)) at the last Forward's parameters."""
+        self.ctx.h2d(self.d_dimg, np.ascontiguousarray(dimage, np.float32))
+        return self._backward()
+
+    def _backward(self):
+        L, h = self.ctx.L, self.ctx.h
+        self.ctx.check(L.gbt_adjoint_backward_async(h, self.bvh.h, C.byref(self.cam), C.byref(self.params),
+                                                    C.c_void_p(self.d_alb), C.c_void_p(self.d_emi),
+                                                    C.c_void_p(self.d_dimg), C.c_void_p(self.d_ga),
+                                                    C.c_void_p(self.d_ge)), "adjoint backward")
+        ga = np.empty((self.n, 3), np.float32)
+        ge = np.empty(self.n, np.float32)
+        self.ctx.d2h(ga, self.d_ga)
+        self.ctx.d2h(ge, self.d_ge)
+        self.ctx.sync()
+        return ga, ge
+
+    def set_target(self, target):
+        self.ctx.h2d(self.d_tgt, np.ascontiguousarray(target, np.float32))
+        self.ctx.sync()
+
+    def loss(self, albedo, emission):
+        """L2 loss of the image at these parameters against the target (float64)."""
+        self.Forward(albedo, emission)
+        L, h = self.ctx.L, self.ctx.h
+        self.ctx.check(L.gbt_l2_loss_async(h, C.c_void_p(self.d_img), C.c_void_p(self.d_tgt), self.w * self.h * 3,
+                                           C.c_void_p(self.d_dimg), C.c_void_p(self.d_loss)), "l2")
+        out = np.zeros(1, np.float64)
+        self.ctx.d2h(out, self.d_loss)
+        self.ctx.sync()
+        return float(out[0])
+
+    def loss_and_grad(self, albedo, emission):
+        """One optimisation step's worth: forward, loss, backward (dLoss/dImage stays on the device)."""
+        loss = self.loss(albedo, emission)
+        ga, ge = self._backward()
+        return loss, ga, ge
+
+    def close(self):
+        for p in (self.d_alb, self.d_emi, self.d_img, self.d_tgt, self.d_dimg, self.d_ga, self.d_ge, self.d_loss):
+            self.ctx.free(p)
+
+
 def make_camera(cam):
     c = _lib.Camera()
     c.look_from[:] = [float(x) for x in cam["look_from"]]
