@@ -113,7 +113,7 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                       "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
@@ -456,7 +456,9 @@ def main():
     achieved = bytes_frame / (trav_ms_frame * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": TRAVERSAL_TRAFFIC.get(bvh_name.split("(")[0]),
-            "kernel": "k_trace4 (closest hit, 4-wide view)" if args.layout == 4 else "k_trace2 (closest hit)",
+            "kernel": "k_trace_pt (persistent, dynamic ray fetch, %s)" % (
+                "4-wide view" if args.layout == 4 else "binary nodes"),
+            "traffic_scope": "DRAM bytes per frame (both traversal launches), ncu cold-cache capture",
             "peak_source": peak_kind, "bytes_per_frame": bytes_frame,
             "traversal_ms_per_frame": trav_ms_frame, "traversal_share": timed["ms_traverse"] / ms,
             "nodes_per_ray": count_stats["nodes_visited"] / rays_per_frame,
@@ -507,6 +509,7 @@ def main():
             "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
                        "max_depth": MAX_DEPTH, "miss": "white", "bvh": bvh_name,
                        "traversal_layout": "%d-wide" % args.layout,
+                       "camera_rays": "8x4 pixel tiles per warp", "past_max_depth": "any-hit query",
                        "rays_per_step": timed["rays_traced"] / args.steps,
                        "l2": "flushed before every timed step (256 MiB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},

@@ -99,6 +99,22 @@ int gbt_ctx_sync(gbt_ctx *ctx);
  * launch (ms_traverse); 2 also counts inner nodes and primitive tests (a
  * slower counting traversal).  No counterpart in the reference. */
 int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
+/* Execution options of later calls on this context.  None of them changes a
+ * result: hits, images and gradients are identical under every setting.
+ *   GBT_OPT_TRAVERSAL      0 persistent with dynamic ray fetch (default),
+ *                          1 one thread per ray, 2 persistent without refills
+ *   GBT_OPT_ANYHIT_LAST    1 (default): rays of the level past MaxDepth, whose
+ *                          hit shades black (pkg/pt/render.go:210-212), stop at
+ *                          the first hit found
+ *   GBT_OPT_PRIMARY_TILES  1 (default): the 32 camera rays of a warp cover an
+ *                          8x4 pixel tile instead of 32 pixels of one row
+ * The environment variables GBT_TRAVERSAL (persistent|simple|ww),
+ * GBT_ANYHIT_LAST and GBT_PRIMARY_TILES (0|1) set the initial values.
+ * No counterpart in the reference. */
+#define GBT_OPT_TRAVERSAL 0
+#define GBT_OPT_ANYHIT_LAST 1
+#define GBT_OPT_PRIMARY_TILES 2
+int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */
 /* verts: n_tri*9 floats (v0 v1 v2); normals: n_tri*9 per-vertex normals or

@@ -76,3 +76,35 @@ def test_render_emitter_exact(ctx):
     cam = dict(look_from=(0, 0, 2), look_at=(0, 0, 0), up=(0, 1, 0), fov=20.0, aspect=1.0)
     img, st = g.render(cam, 8, 8, 2, 0)
     np.testing.assert_allclose(img, 10.0)
+
+
+@pytest.mark.parametrize("kind", ["cornell", "soup"])
+def test_execution_options_leave_images_identical(ctx, kind):
+    """Any-hit past MaxDepth, tiled camera rays and the traversal kernel change the
+    order of work only: with spp 2 (two deposits per pixel add commutatively) the
+    images and ray counts are bitwise equal under every setting.  The frame size is
+    no multiple of the 8x4 tile, so the right and bottom strips are covered too."""
+    s = scenes.cornell() if kind == "cornell" else scenes.soup(100_000, seed=3)
+    rd = s["render"]
+    w, h, spp, md = 83, 61, 2, (3 if kind == "cornell" else 0)
+    cam = dict(s["camera"], aspect=w / h)
+    g = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s))
+    ref = None
+    try:
+        for trav in (0, 1, 2):
+            for anyhit in (0, 1):
+                for tiles in (0, 1):
+                    ctx.set_option("traversal", trav)
+                    ctx.set_option("anyhit_last", anyhit)
+                    ctx.set_option("primary_tiles", tiles)
+                    img, st = g.render(cam, w, h, spp, md, rd["miss_mode"], rd["miss_color"], seed=5)
+                    if ref is None:
+                        ref = (img, st["rays_traced"])
+                        assert img.mean() > 0
+                    else:
+                        assert st["rays_traced"] == ref[1], (trav, anyhit, tiles)
+                        assert np.array_equal(img, ref[0]), (trav, anyhit, tiles, np.abs(img - ref[0]).max())
+    finally:
+        ctx.set_option("traversal", 0)
+        ctx.set_option("anyhit_last", 1)
+        ctx.set_option("primary_tiles", 1)

@@ -18,7 +18,7 @@ ERRORS = {-1: "GBT_EINVAL", -2: "GBT_ECUDA", -3: "GBT_ENOMEM", -4: "GBT_ETIMEOUT
 # every symbol include/gbtrace.h declares
 EXPORTS = [
     "gbt_ctx_create", "gbt_ctx_destroy", "gbt_last_error", "gbt_ctx_stream", "gbt_ctx_sync",
-    "gbt_ctx_set_profiling", "gbt_host_alloc", "gbt_host_free",
+    "gbt_ctx_set_profiling", "gbt_ctx_set_option", "gbt_host_alloc", "gbt_host_free",
     "gbt_scene_upload", "gbt_scene_destroy", "gbt_obj_parse",
     "gbt_lbvh_build", "gbt_lbvh_rebuild_async", "gbt_scene_update_async", "gbt_phr_build", "gbt_bvh_destroy",
     "gbt_bvh_cost", "gbt_bvh_size", "gbt_bvh_counts", "gbt_bvh_export", "gbt_lbvh_sorted",
@@ -85,6 +85,7 @@ def load():
         "gbt_ctx_stream": ([P], C.c_void_p),
         "gbt_ctx_sync": ([P], C.c_int),
         "gbt_ctx_set_profiling": ([P, i32], C.c_int),
+        "gbt_ctx_set_option": ([P, i32, i32], C.c_int),
         "gbt_host_alloc": ([P, C.c_size_t, PP], C.c_int),
         "gbt_host_free": ([P, P], C.c_int),
         "gbt_scene_upload": ([P, P, P, u32, P, u32, P, P, u32, PP], C.c_int),

@@ -103,6 +103,8 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
     for (auto &e : c->ev) cudaEventCreate(&e);
     if (const char *t = std::getenv("GBT_TRAVERSAL"))
         c->traversal = std::strcmp(t, "simple") == 0 ? 1 : std::strcmp(t, "ww") == 0 ? 2 : 0;
+    if (const char *t = std::getenv("GBT_ANYHIT_LAST")) c->anyhit_last = std::strcmp(t, "0") != 0;
+    if (const char *t = std::getenv("GBT_PRIMARY_TILES")) c->primary_tiles = std::strcmp(t, "0") != 0;
     *out = c;
     return GBT_OK;
 }
@@ -137,6 +139,23 @@ extern "C" int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level) {
     ctx->profiling = level;
     ctx->n_prof_ev = 0;
     return GBT_OK;
+}
+
+extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
+    if (!ctx) return GBT_EINVAL;
+    switch (option) {
+    case GBT_OPT_TRAVERSAL:
+        if (value < 0 || value > 2) return gbt_fail(ctx, GBT_EINVAL, "set_option: traversal must be 0, 1 or 2");
+        ctx->traversal = value;
+        return GBT_OK;
+    case GBT_OPT_ANYHIT_LAST:
+    case GBT_OPT_PRIMARY_TILES:
+        if (value < 0 || value > 1) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 0 or 1");
+        (option == GBT_OPT_ANYHIT_LAST ? ctx->anyhit_last : ctx->primary_tiles) = value;
+        return GBT_OK;
+    default:
+        return gbt_fail(ctx, GBT_EINVAL, "set_option: unknown option " + std::to_string(option));
+    }
 }
 
 void gbt_prof_begin(gbt_ctx *ctx) {

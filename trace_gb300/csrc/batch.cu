@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
     int item = -1;  // -1: no path
     uint32_t g = 0;
     int level = 0;
+    bool any = false;  // the current ray only needs hit or miss (level past MaxDepth)
     float3 T = f3(1.f, 1.f, 1.f), L = f3(0.f, 0.f, 0.f);
     const float4 *nodes = nullptr, *recs = nullptr;
     uint32_t rays = 0;
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
                                    it.normals, T, L, no, nd);
             if (cont) {
                 level++;
+                any = it.sp.any_last && level == it.sp.max_depth + 1;
                 r.o = no;
                 r.d = nd;
                 r.tmin = 0.0001f;
@@ -143,10 +145,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
                 if (q < total) {
                     item = find_item(s_base, n_items, q);
                     const ItemDev &it = items[item];
-                    g = q - it.path_base;
+                    g = path_id(it.sp, q - it.path_base);
                     nodes = it.nodes;
                     recs = it.recs;
                     level = 0;
+                    any = false;
                     T = f3(1.f, 1.f, 1.f);
                     L = f3(0.f, 0.f, 0.f);
                     primary_ray(it.cam, it.sp, g, r.o, r.d);
@@ -188,7 +191,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
             }
             while (leaf.y > 0) {
                 gbt_dev::leaf(recs, leaf.x, leaf.y, r, h);
-                if (node.y > 0) {
+                if (any && h.rec >= 0) {  // any hit ends the query
+                    node = make_int2(0, -1);
+                    leaf = make_int2(0, 0);
+                    sp = 0;
+                } else if (node.y > 0) {
                     leaf = node;
                     node = st.pop(sp, h.t);
                 } else {
@@ -302,6 +309,8 @@ int prepare(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<I
         d.out = it.d_rgb;
         d.cam = gbt_make_cam(&it.camera);
         d.sp = gbt_make_shade_params(&it.params, b->scene->n_tri);
+        d.sp.tiles = ctx->primary_tiles ? 1u : 0u;
+        d.sp.any_last = ctx->anyhit_last ? 1u : 0u;
         d.path_base = (uint32_t)paths;
         d.pix_base = (uint32_t)pix;
         d.inv_spp = 1.0f / it.params.spp;

@@ -49,6 +49,10 @@ struct gbt_ctx {
     // traversal kernel: 0 persistent with dynamic ray fetch (default), 1 one thread per ray,
     // 2 persistent without mid-ray refills (GBT_TRAVERSAL=simple|ww at context creation)
     int traversal = 0;
+    // renderer options (gbt_ctx_set_option): answer the rays of the level past MaxDepth,
+    // whose hit shades black, with an any-hit query; order camera rays in 8x4 pixel tiles
+    int anyhit_last = 1;
+    int primary_tiles = 1;
 };
 
 // Record a profiling event pair around one traversal launch.
@@ -137,7 +141,7 @@ size_t gbt_lbvh_scratch_bytes(uint32_t n);
 int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits);
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
                          const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s,
-                         unsigned long long *d_counters = nullptr);
+                         unsigned long long *d_counters = nullptr, bool any = false);
 // render.cu
 int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
                        float *d_rgb);

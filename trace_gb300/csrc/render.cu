@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) k_raygen(CamF cam, ShadeParams sp, uint32
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) counts[0] = count;
     if (i >= count) return;
-    uint32_t g = g0 + i;
+    uint32_t g = path_id(sp, g0 + i);
     float3 o, d;
     primary_ray(cam, sp, g, o, d);
     rays[2 * (size_t)i] = make_float4(o.x, o.y, o.z, 0.001f);
@@ -142,6 +142,8 @@ ShadeParams gbt_make_shade_params(const gbt_render_params *p, uint32_t n_tri) {
     sp.seed_lo = (uint32_t)p->seed;
     sp.seed_hi = (uint32_t)(p->seed >> 32);
     sp.n_tri = n_tri;
+    sp.tiles = 0;
+    sp.any_last = 0;
     return sp;
 }
 
@@ -210,6 +212,7 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
     gbt_scene *sc = bvh->scene;
     CamF cf = gbt_make_cam(cam);
     ShadeParams sp = gbt_make_shade_params(p, sc->n_tri);
+    sp.tiles = ctx->primary_tiles ? 1u : 0u;
     const int levels = p->max_depth + 2;  // surfaces at depth 0..MaxDepth+1 are traced
 
     GBT_CUDA(ctx, cudaMemsetAsync(rs.acc, 0, npix * 3 * sizeof(float), st));
@@ -224,7 +227,9 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
         for (int lv = 0; lv < levels; lv++) {
             int a = lv & 1;
             gbt_prof_begin(ctx);
-            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr);
+            // past MaxDepth a hit shades black, so only hit-or-miss matters there
+            const bool any = ctx->anyhit_last && lv == levels - 1;
+            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
             gbt_prof_end(ctx);
             k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],
                                             rs.aux[a ^ 1], rs.counts + lv + 1, bvh->d_prims, sc->d_prim_mat, sc->d_mats,

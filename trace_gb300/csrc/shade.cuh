@@ -28,6 +28,8 @@ struct ShadeParams {
     float3 miss_color;
     uint32_t seed_lo, seed_hi;
     uint32_t n_tri;
+    uint32_t tiles;     // 1: launch slots map to path ids tile by tile (path_id)
+    uint32_t any_last;  // 1: rays of level MaxDepth+1 take an any-hit query (batched kernel)
 };
 
 // Philox-2x32-10 (Salmon et al., "Parallel random numbers: as easy as 1, 2,
@@ -45,7 +47,25 @@ __device__ __forceinline__ uint2 philox2x32(uint32_t c0, uint32_t c1, uint32_t k
 }
 __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
-// Primary ray of path g (pixel g % npix).
+// Path launched in slot g.  Path ids select the pixel (id % npix) and the random
+// numbers, so the image depends only on the set of ids: with tiles the slots of
+// one warp (32 consecutive g) take the ids of an 8x4 pixel tile, which keeps the
+// rays of a warp coherent.  The map is a bijection on every run of npix slots:
+// full tiles first, then the right strip, then the bottom strip, in scan order.
+__device__ __forceinline__ uint32_t path_id(const ShadeParams &sp, uint32_t g) {
+    if (!sp.tiles) return g;
+    const uint32_t p = g % sp.npix, base = g - p;
+    const uint32_t w8 = sp.width & ~7u, h4 = sp.height & ~3u;
+    if (p >= w8 * h4) {
+        uint32_t q = p - w8 * h4, rw = sp.width - w8;
+        if (q < rw * h4) return base + (q / rw) * sp.width + w8 + q % rw;
+        return base + h4 * sp.width + (q - rw * h4);
+    }
+    const uint32_t t = p >> 5, l = p & 31u, tw = w8 >> 3;
+    return base + ((t / tw) * 4 + (l >> 3)) * sp.width + (t % tw) * 8 + (l & 7u);
+}
+
+// Primary ray of path id g (pixel g % npix).
 __device__ __forceinline__ void primary_ray(const CamF &cam, const ShadeParams &sp, uint32_t g, float3 &o, float3 &d) {
     uint32_t pix = g % sp.npix;
     uint32_t x = pix % sp.width, y = pix / sp.width;

@@ -17,6 +17,8 @@
 // tmin <= t <= tmax) and :56-86 (sphere, exclusive t bounds), in float32.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "gbt_internal.cuh"
 #include "traverse.cuh"
 
@@ -77,16 +79,36 @@ __device__ __forceinline__ uint32_t lane_lt() {
     return m;
 }
 
-template <int W, bool COUNT, int DYN>
-__global__ void __launch_bounds__(128) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+// Resident blocks per SM the register budget is sized for (64 registers a thread at 8).
+#ifndef GBT_PT_MINB
+#define GBT_PT_MINB 8
+#endif
+// Stack entries of each thread kept in shared memory (the bottom SH slots); 0: all local.
+#ifndef GBT_PT_SH
+#define GBT_PT_SH 12
+#endif
+
+// ANY: stop at the first hit found (for rays whose shading only needs hit or miss)
+template <int W, bool COUNT, int DYN, bool ANY>
+__global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                   const float4 *__restrict__ recs, const float4 *__restrict__ rays,
                                                   float4 *__restrict__ hits, uint32_t n,
                                                   const uint32_t *__restrict__ d_count, int out_mode, unsigned int *err,
                                                   unsigned long long *counters, uint32_t *fetch) {
     constexpr int STACK = W == 2 ? 64 : 96;
+    constexpr int SH = GBT_PT_SH;
     const uint32_t total = d_count ? *d_count : n;
     const uint32_t lane = threadIdx.x & 31;
-    gbt_dev::LocalStack<STACK> st;
+    using StackT = typename std::conditional<(SH > 0), gbt_dev::SharedTopStack<STACK, (SH > 0 ? SH : 1)>,
+                                             gbt_dev::LocalStack<STACK>>::type;
+    StackT st;
+    if constexpr (SH > 0) {
+        __shared__ int2 s_se[SH * 128];
+        __shared__ float s_st[SH * 128];
+        st.se = s_se + threadIdx.x;
+        st.st = s_st + threadIdx.x;
+        st.stride = 128;
+    }
     int sp = 0;
     int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
     gbt_dev::Ray r;
@@ -150,7 +172,11 @@ __global__ void __launch_bounds__(128) k_trace_pt(const BvhHeader *__restrict__ 
             while (leaf.y > 0) {
                 if (COUNT) w.prims += (uint32_t)leaf.y;
                 gbt_dev::leaf(recs, leaf.x, leaf.y, r, h);
-                if (node.y > 0) {
+                if (ANY && h.rec >= 0) {  // any hit ends the query
+                    node = make_int2(0, -1);
+                    leaf = make_int2(0, 0);
+                    sp = 0;
+                } else if (node.y > 0) {
                     leaf = node;
                     node = st.pop(sp, h.t);
                 } else {
@@ -163,13 +189,13 @@ __global__ void __launch_bounds__(128) k_trace_pt(const BvhHeader *__restrict__ 
     flush_work<COUNT>(w, counters);
 }
 
-template <int W, bool COUNT, int DYN>
+template <int W, bool COUNT, int DYN, bool ANY>
 void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
                cudaStream_t s) {
     static int per_sm = 0;  // resident blocks per SM of this instantiation
     if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN, ANY>, 128, 0);
         if (per_sm <= 0) per_sm = 1;
     }
     uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
@@ -177,22 +203,27 @@ void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const fl
     uint32_t grid = (uint32_t)(ctx->num_sms * per_sm);
     uint32_t need = (n + 127) / 128;
     if (need < grid) grid = need;
-    k_trace_pt<W, COUNT, DYN><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
+    k_trace_pt<W, COUNT, DYN, ANY><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
                                                   counters, fetch);
 }
 
 template <int W, int DYN>
 void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                    float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
-                   cudaStream_t s) {
-    if (counters) launch_pt<W, true, DYN>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
-    else launch_pt<W, false, DYN>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+                   cudaStream_t s, bool any) {
+    if (any) {
+        if (counters) launch_pt<W, true, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+    } else {
+        if (counters) launch_pt<W, true, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+    }
 }
 
 }  // namespace
 
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, const uint32_t *d_count,
-                         int out_mode, unsigned int *d_error, cudaStream_t s, unsigned long long *counters) {
+                         int out_mode, unsigned int *d_error, cudaStream_t s, unsigned long long *counters, bool any) {
     if (n == 0) return;
     uint32_t blocks = (n + 127) / 128;
     gbt_ctx *ctx = bvh->ctx;
@@ -202,11 +233,11 @@ void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, u
         const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
         const bool dyn = ctx->traversal == 0;
         if (four) {
-            if (dyn) launch_pt_any<4, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
-            else launch_pt_any<4, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+            if (dyn) launch_pt_any<4, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            else launch_pt_any<4, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
         } else {
-            if (dyn) launch_pt_any<2, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
-            else launch_pt_any<2, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s);
+            if (dyn) launch_pt_any<2, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            else launch_pt_any<2, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
         }
         return;
     }

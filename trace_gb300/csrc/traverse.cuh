@@ -53,6 +53,14 @@ __device__ __forceinline__ Ray load_ray(const float4 *__restrict__ rays, uint32_
 // Slab test against [tmin, tmax]; returns the entry distance.  The far
 // distance is widened by a few ulp so that a primitive lying on the box
 // boundary is never culled by float32 rounding.
+// Two float4 of a node in one 256-bit read-only load (sm_100 and later; p is
+// 32-byte aligned: node arrays come from cudaMalloc and nodes are 64 or 128 bytes).
+__device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, float hy, float hz, const Ray &r,
                                      float tmax, float &tenter) {
     float tx0 = fmaf(lx, r.inv.x, -r.oi.x), tx1 = fmaf(hx, r.inv.x, -r.oi.x);
@@ -141,8 +149,11 @@ __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *
         if (cur.y == 0) {
             if (COUNT) work->nodes++;
             const float4 *nd = nodes + 4 * (size_t)cur.x;
-            float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
-            int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+            float4 n0, n1, n2, n3f;
+            ldg256(nd, n0, n1);
+            ldg256(nd + 2, n2, n3f);
+            const int4 n3 = make_int4(__float_as_int(n3f.x), __float_as_int(n3f.y), __float_as_int(n3f.z),
+                                      __float_as_int(n3f.w));
             float t0, t1;
             bool h0 = n3.y >= 0 && slab(n0.x, n0.z, n2.x, n0.y, n0.w, n2.y, r, h.t, t0);
             bool h1 = n3.w >= 0 && slab(n1.x, n1.z, n2.z, n1.y, n1.w, n2.w, r, h.t, t1);
@@ -204,10 +215,15 @@ __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *
         if (cur.y == 0) {
             if (COUNT) work->nodes++;
             const float4 *nd = nodes + 8 * (size_t)cur.x;
-            float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
-            float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
-            int4 rf = __ldg(reinterpret_cast<const int4 *>(nd + 6));
-            int4 cn = __ldg(reinterpret_cast<const int4 *>(nd + 7));
+            float4 lx, hx, ly, hy, lz, hz, rff, cnf;
+            ldg256(nd, lx, hx);
+            ldg256(nd + 2, ly, hy);
+            ldg256(nd + 4, lz, hz);
+            ldg256(nd + 6, rff, cnf);
+            const int4 rf = make_int4(__float_as_int(rff.x), __float_as_int(rff.y), __float_as_int(rff.z),
+                                      __float_as_int(rff.w));
+            const int4 cn = make_int4(__float_as_int(cnf.x), __float_as_int(cnf.y), __float_as_int(cnf.z),
+                                      __float_as_int(cnf.w));
             float tc[4];
             int2 ch[4];
             int k = 0;
@@ -264,13 +280,11 @@ __device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *
 // Traversal stacks: entries (ref, cnt) with the entry distance used to skip
 // subtrees that lie beyond the current closest hit.
 template <int STACK>
-struct LocalStack {  // all entries in local memory
-    int2 e[STACK];
-    float t[STACK];
+struct LocalStack {  // all entries in local memory, one 16-byte word each (ref, cnt, t)
+    int4 e[STACK];
     __device__ __forceinline__ void push(int &sp, int2 v, float tv, unsigned int *err) {
         if (sp < STACK) {
-            e[sp] = v;
-            t[sp] = tv;
+            e[sp] = make_int4(v.x, v.y, __float_as_int(tv), 0);
             ++sp;
         } else {
             atomicOr(err, GBT_DEVERR_STACK);
@@ -279,29 +293,29 @@ struct LocalStack {  // all entries in local memory
     __device__ __forceinline__ int2 pop(int &sp, float tmax) {
         while (sp > 0) {
             --sp;
-            if (t[sp] <= tmax * 1.0000005f) return e[sp];
+            const int4 w = e[sp];
+            if (__int_as_float(w.z) <= tmax * 1.0000005f) return make_int2(w.x, w.y);
         }
         return make_int2(0, -1);
     }
 };
 
-// The top SH entries of each thread's stack in shared memory (column `lane`
-// of a [SH][stride] array), deeper entries in local memory.
+// The first SH slots of each thread's stack, where a shallow traversal does
+// all its pushes and pops, in shared memory (column `thread` of a [SH][stride]
+// array); deeper slots in local memory.
 template <int STACK, int SH>
 struct SharedTopStack {
     int2 *se;
     float *st;
     int stride;
-    int2 e[STACK - SH];
-    float t[STACK - SH];
+    int4 e[STACK - SH];
     __device__ __forceinline__ void push(int &sp, int2 v, float tv, unsigned int *err) {
         if (sp < SH) {
             se[sp * stride] = v;
             st[sp * stride] = tv;
             ++sp;
         } else if (sp < STACK) {
-            e[sp - SH] = v;
-            t[sp - SH] = tv;
+            e[sp - SH] = make_int4(v.x, v.y, __float_as_int(tv), 0);
             ++sp;
         } else {
             atomicOr(err, GBT_DEVERR_STACK);
@@ -310,8 +324,12 @@ struct SharedTopStack {
     __device__ __forceinline__ int2 pop(int &sp, float tmax) {
         while (sp > 0) {
             --sp;
-            float tv = sp < SH ? st[sp * stride] : t[sp - SH];
-            if (tv <= tmax * 1.0000005f) return sp < SH ? se[sp * stride] : e[sp - SH];
+            if (sp < SH) {
+                if (st[sp * stride] <= tmax * 1.0000005f) return se[sp * stride];
+            } else {
+                const int4 w = e[sp - SH];
+                if (__int_as_float(w.z) <= tmax * 1.0000005f) return make_int2(w.x, w.y);
+            }
         }
         return make_int2(0, -1);
     }
@@ -322,8 +340,10 @@ template <class StackT>
 __device__ __forceinline__ int2 step2(const float4 *__restrict__ nodes, int2 node, StackT &st, int &sp, const Ray &r,
                                       float tmax, unsigned int *err) {
     const float4 *nd = nodes + 4 * (size_t)node.x;
-    float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2);
-    int4 n3 = __ldg(reinterpret_cast<const int4 *>(nd + 3));
+    float4 n0, n1, n2, n3f;
+    ldg256(nd, n0, n1);
+    ldg256(nd + 2, n2, n3f);
+    const int4 n3 = make_int4(__float_as_int(n3f.x), __float_as_int(n3f.y), __float_as_int(n3f.z), __float_as_int(n3f.w));
     float t0, t1;
     bool h0 = n3.y >= 0 && slab(n0.x, n0.z, n2.x, n0.y, n0.w, n2.y, r, tmax, t0);
     bool h1 = n3.w >= 0 && slab(n1.x, n1.z, n2.z, n1.y, n1.w, n2.w, r, tmax, t1);
@@ -360,10 +380,13 @@ template <class StackT>
 __device__ __forceinline__ int2 step4(const float4 *__restrict__ nodes, int2 node, StackT &st, int &sp, const Ray &r,
                                       float tmax, unsigned int *err) {
     const float4 *nd = nodes + 8 * (size_t)node.x;
-    float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3);
-    float4 lz = __ldg(nd + 4), hz = __ldg(nd + 5);
-    int4 rf = __ldg(reinterpret_cast<const int4 *>(nd + 6));
-    int4 cn = __ldg(reinterpret_cast<const int4 *>(nd + 7));
+    float4 lx, hx, ly, hy, lz, hz, rff, cnf;
+    ldg256(nd, lx, hx);
+    ldg256(nd + 2, ly, hy);
+    ldg256(nd + 4, lz, hz);
+    ldg256(nd + 6, rff, cnf);
+    const int4 rf = make_int4(__float_as_int(rff.x), __float_as_int(rff.y), __float_as_int(rff.z), __float_as_int(rff.w));
+    const int4 cn = make_int4(__float_as_int(cnf.x), __float_as_int(cnf.y), __float_as_int(cnf.z), __float_as_int(cnf.w));
     const float MISS = __int_as_float(0x7f800000);
     Cand c0, c1, c2, c3;
     float t;

@@ -65,6 +65,12 @@ class Context:
     def sync(self):
         self.check(self.L.gbt_ctx_sync(self.h), "sync")
 
+    OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2}
+
+    def set_option(self, name, value):
+        """Execution option of later calls (gbt_ctx_set_option); results do not depend on it."""
+        self.check(self.L.gbt_ctx_set_option(self.h, self.OPTIONS[name], int(value)), "set_option")
+
     def close(self):
         if getattr(self, "h", None):
             kids = list(getattr(self, "_children", ()))
