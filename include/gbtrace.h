@@ -208,7 +208,7 @@ typedef struct {
 typedef struct {
     int32_t block;     /* threads per block: 64, 128 or 256 */
     int32_t fetch_min; /* 0: a warp refills only when all its lanes are idle; 16: when fewer than 16 are busy */
-    int32_t stack;     /* 0: traversal stack in local memory; 1: its top 8 entries in shared memory */
+    int32_t stack;     /* 0: traversal stack in local memory; 1: its first 12 entries in shared memory */
 } gbt_batch_config;
 
 /* All items in one persistent launch pulling (scene, path) work from a device

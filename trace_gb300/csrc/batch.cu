@@ -258,15 +258,15 @@ void launch_batch(const ItemDev *items, int n, uint32_t total, uint32_t *fetch, 
     k_batch<W, BLOCK, DYN, SH><<<grid, BLOCK, 0, s>>>(items, n, total, fetch, err, rays);
 }
 
-// config: block in {64,128,256} x fetch_min in {0,16} x stack in {local, top 8 entries in shared memory}
+// config: block in {64,128,256} x fetch_min in {0,16} x stack in {local, first 12 entries in shared memory}
 template <int W>
 Launcher pick(const gbt_batch_config &c) {
     const int b = c.block, d = c.fetch_min > 0 ? 1 : 0, s = c.stack ? 1 : 0;
 #define GBT_PICK(B, D, S) \
     if (b == B && d == (D > 0) && s == (S > 0)) return &launch_batch<W, B, D, S>;
-    GBT_PICK(64, 0, 0) GBT_PICK(64, 0, 8) GBT_PICK(64, 16, 0) GBT_PICK(64, 16, 8)
-    GBT_PICK(128, 0, 0) GBT_PICK(128, 0, 8) GBT_PICK(128, 16, 0) GBT_PICK(128, 16, 8)
-    GBT_PICK(256, 0, 0) GBT_PICK(256, 0, 8) GBT_PICK(256, 16, 0) GBT_PICK(256, 16, 8)
+    GBT_PICK(64, 0, 0) GBT_PICK(64, 0, 12) GBT_PICK(64, 16, 0) GBT_PICK(64, 16, 12)
+    GBT_PICK(128, 0, 0) GBT_PICK(128, 0, 12) GBT_PICK(128, 16, 0) GBT_PICK(128, 16, 12)
+    GBT_PICK(256, 0, 0) GBT_PICK(256, 0, 12) GBT_PICK(256, 16, 0) GBT_PICK(256, 16, 12)
 #undef GBT_PICK
     return nullptr;
 }
