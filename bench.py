@@ -324,21 +324,101 @@ def run_adjoint_workload(args):
     return 0
 
 
-def run_profile_case(args):
-    """The benchmark's scene, without timing: a case small enough for an ncu capture
-    (about 0.3 GB on the device).  `render`: 3 frames on the chosen tree;
-    `lbvh`: 3 LBVH builds."""
+def run_terrain_workload(args):
+    """The 2048x2048 fBm terrain (8,380,418 triangles plus a sun sphere): LBVH build
+    Mtri/s with its HBM roofline, the PHR grid optimiser and build, and Mrays/s of the
+    1920x1080, 64 spp, MaxDepth 4 render (constant sky 0.5) on the chosen PHR tree.
+    Inputs resident in HBM; the scene is far larger than L2."""
+    import torch
+
     from trace_gb300 import _lib, pt, scenes
 
     ctx = pt.Context(0)
-    s = scenes.soup(N_TRI, seed=1, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH)
+    t0 = time.perf_counter()
+    s = scenes.terrain(2048)
+    gen_s = time.perf_counter() - t0
+    n = s["verts"].shape[0] + s["spheres"].shape[0]
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    L, h = ctx.L, ctx.h
+    aux = pt.DefaultLBVH(ds)
+    steps = max(3, args.steps)
+    for _ in range(args.warmup):
+        ctx.check(L.gbt_lbvh_rebuild_async(h, aux.h), "rebuild")
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.check(L.gbt_lbvh_rebuild_async(h, aux.h), "rebuild")
+    e1.record(stream)
+    ctx.sync()
+    lb_ms = e0.elapsed_time(e1) / steps
+    hbm, peak_kind = peaks()
+    lb_bw = n * LBVH_BYTES_PER_TRI / (lb_ms * 1e-3) / 1e9
+    rd = s["render"]
+    # PHR parameters from the reference's grid optimiser (optimizer.go:44-94) over a grid that
+    # reaches deep enough cuts for this scene: the sun sphere inflates the root box, so the
+    # default grid's shallow cuts leave leaves of thousands of triangles
+    t0 = time.perf_counter()
+    opt = pt.NewGridOptimizer([0.4, 0.5, 0.55], [6, 8, 10, 12], rd["width"], rd["height"])
+    alpha, delta = opt.OptimizedPHRparams(aux, 2)
+    opt_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bvh = pt.NewPHRBuilder(alpha, delta, 2).BuildFromAuxilary(aux)
+    ctx.sync()
+    phr_s = time.perf_counter() - t0
+    cam = pt.make_camera(s["camera"])
+    rp = _lib.RenderParams(rd["width"], rd["height"], rd["spp"], rd["max_depth"], rd["miss_mode"],
+                           (C.c_float * 3)(*rd["miss_color"]), 7)
+    d_img = ctx.alloc(rd["width"] * rd["height"] * 3 * 4)
+    st = _lib.RenderStats()
+    ctx.check(L.gbt_render_async(h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+    ctx.sync()
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    frames = 2
+    e0.record(stream)
+    for _ in range(frames):
+        ctx.check(L.gbt_render_async(h, bvh.h, C.byref(cam), C.byref(rp), C.c_void_p(d_img)), "render")
+    e1.record(stream)
+    ctx.sync()
+    ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
+    ms = e0.elapsed_time(e1) / frames
+    img = np.empty((rd["height"], rd["width"], 3), np.float32)
+    ctx.d2h(img, d_img)
+    ctx.sync()
+    ctx.free(d_img)
+    line = {"metric": "Mrays/s (terrain)", "value": st.rays_traced / frames / ms / 1e3, "unit": "Mrays/s",
+            "workload": "terrain2048_1920x1080_spp64_depth4", "triangles": n, "ms_per_frame": ms,
+            "rays_per_frame": st.rays_traced / frames, "image_mean": float(img.mean()),
+            "lbvh": {"mtri_s": n / lb_ms / 1e3, "ms": lb_ms,
+                     "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
+                                  "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind}},
+            "phr": {"alpha": alpha, "delta": delta, "sah_cost": bvh.Cost(), "lbvh_sah_cost": aux.Cost(),
+                    "build_s_wall": phr_s, "optimizer_s_wall": opt_s,
+                    "grid": [{"alpha": a, "delta": d, "sah": c, "build_cost": b} for a, d, c, b in opt.evaluations]},
+            "scene_generation_s": gen_s}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile_case(args):
+    """The benchmark's scene, without timing: a case small enough for an ncu capture
+    (about 0.3 GB on the device for the soup, 3 GB for the terrain).  `render`: 3
+    frames on the chosen tree; `lbvh`: 3 LBVH builds (the first one allocates)."""
+    from trace_gb300 import _lib, pt, scenes
+
+    ctx = pt.Context(0)
+    if args.profile_scene == "terrain":
+        s = scenes.terrain(2048)
+    else:
+        s = scenes.soup(N_TRI, seed=1, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH)
     ds = pt.DeviceScene.from_dict(ctx, s)
     aux = pt.DefaultLBVH(ds)
     if args.profile == "lbvh":
         for _ in range(3):
             ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
         ctx.sync()
-        print("profile case lbvh: 3 builds of %d triangles" % N_TRI)
+        print("profile case lbvh: 3 builds of %d triangles" % s["verts"].shape[0])
         return 0
     bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux) if args.bvh == "phr" else aux
     ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, bvh.h, args.layout), "layout")
@@ -366,9 +446,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--profile", choices=["render", "lbvh"], default=None,
                     help="run a small fixed case for an ncu capture and exit: 3 frames (render) or 3 LBVH builds")
-    ap.add_argument("--workload", choices=["soup", "batch", "adjoint"], default="soup",
+    ap.add_argument("--profile-scene", choices=["soup", "terrain"], default="soup",
+                    help="scene of --profile lbvh: the 1M soup or the 8.4M-triangle terrain")
+    ap.add_argument("--workload", choices=["soup", "batch", "adjoint", "terrain"], default="soup",
                     help="soup: the headline 1M-triangle frame; batch: the 64-scene batched render; "
-                         "adjoint: forward+backward iteration of the differentiable render")
+                         "adjoint: forward+backward iteration of the differentiable render; "
+                         "terrain: LBVH/PHR builds and the 64 spp render of the 8.4M-triangle terrain")
     ap.add_argument("--batch-scenes", type=int, default=64)
     args = ap.parse_args()
     ws, rank, local = dist_env()
@@ -380,6 +463,8 @@ def main():
         return run_batch_workload(args)
     if args.workload == "adjoint":
         return run_adjoint_workload(args)
+    if args.workload == "terrain":
+        return run_terrain_workload(args)
     args.warmup = max(args.warmup, 3)
 
     import torch

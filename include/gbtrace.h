@@ -142,6 +142,19 @@ int gbt_scene_update_async(gbt_ctx *ctx, gbt_scene *scene, const float *d_verts)
 /* pkg/pt/phr.go:47-84 PhrBuilder.BuildFromAuxilary over an LBVH from
  * gbt_lbvh_build; alpha/delta/branching as NewPHRBuilder (phr.go:30-40). */
 int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out);
+/* pkg/pt/phr.go:154-192 PhrBuilder.BuildWithCost: the same tree plus the build
+ * cost, the initial cut's size plus the size of every cut handed to Split. */
+int gbt_phr_build_with_cost(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching,
+                            gbt_bvh **out, int64_t *build_cost);
+/* pkg/pt/optimizer.go:44-94 gridOptimizer.OptimizedPHRparams(aux, branching):
+ * builds every (alphas[i], deltas[j]) (alphas outer), scores each by
+ * build/max_build + omega^2 * sah/max_sah with omega = (prims/2e6)^2 *
+ * (width*height/2e5), and returns the first minimum.  evals (optional,
+ * 2*n_alpha*n_delta doubles) receives (SAH cost, build cost) per candidate.
+ * NewDefaultGridOptimizer's grid is alphas {0.4,0.45,0.5,0.55} x deltas {6,7,8,9}. */
+int gbt_phr_optimize_grid(gbt_ctx *ctx, gbt_bvh *aux, int32_t branching, const double *alphas, int32_t n_alpha,
+                          const double *deltas, int32_t n_delta, int32_t frame_width, int32_t frame_height,
+                          double *alpha, double *delta, double *evals);
 int gbt_bvh_destroy(gbt_bvh *bvh);
 /* Traversal layout of a binary tree: 4 (default after gbt_lbvh_build and a
  * branching-2 gbt_phr_build) traverses a 4-wide view collapsed from it; 2

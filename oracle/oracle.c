@@ -1233,6 +1233,7 @@ typedef struct {
     double *bc;     /* aux barycenters, 3 per node */
     int64_t max_cut;
     int64_t initial;
+    int64_t build_cost; /* BuildWithCost's count (phr.go:154-255) */
     /* scratch for minCost */
     double *rbox;
     double *rcost;
@@ -1482,6 +1483,7 @@ static int build_subtrees(phr_ctx *p, ocut initial) {
             for (int i = 0; i < nc; i++)
                 if (cuts[i].n > mx) { mx = cuts[i].n; mi = i; }
             if (mx <= 1) break;
+            p->build_cost += mx; /* buildSubTreeCost, phr.go:214 */
             ocut L, R;
             rc = sweep_sah(p, &cuts[mi], &L, &R);
             if (rc) break;
@@ -1576,7 +1578,7 @@ static int initial_cut(phr_ctx *p, ocut *c) {
 }
 
 /* PhrBuilder.BuildFromAuxilary (phr.go:47-84) */
-int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[4]) {
+int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[5]) {
     *out = NULL;
     if (bf < 2 || bf > ORC_MAX_ARITY) return ORC_E_ARG;
     orc_bvh *o = (orc_bvh *)calloc(1, sizeof(orc_bvh));
@@ -1613,6 +1615,7 @@ int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bv
     if (!rc) {
         p.initial = c0.n;
         p.max_cut = c0.n;
+        p.build_cost = c0.n; /* BuildWithCost, phr.go:159 */
         rc = build_subtrees(&p, c0);
     }
     free(p.bc);
@@ -1626,6 +1629,7 @@ int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bv
         stats[1] = p.max_cut;
         stats[2] = cnt[0];
         stats[3] = cnt[1];
+        stats[4] = p.build_cost;
     }
     *out = o;
     return ORC_OK;

@@ -97,7 +97,8 @@ int orc_adjoint(const orc_bvh *b, const orc_camera_desc *cam, const orc_render_d
                 const float *emission, const float *dimg, double *img, double *g_albedo, double *g_emission);
 
 /* ---- PHR ---- */
-int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[4]);
+/* stats: initial cut size, largest cut, nodes, leaves, BuildWithCost's build cost */
+int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[5]);
 
 #ifdef __cplusplus
 }

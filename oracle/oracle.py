@@ -230,12 +230,13 @@ class BVH:
 
     def phr(self, alpha=0.5, delta=6.0, bf=2):
         h = C.c_void_p()
-        stats = np.zeros(4, np.int64)
+        stats = np.zeros(5, np.int64)
         rc = lib().orc_phr_build(self.h, float(alpha), float(delta), int(bf), C.byref(h), _p(stats))
         if rc != 0:
             raise RuntimeError("oracle PHR failed: %d" % rc)
         b = BVH(h)
-        b.stats = dict(initial_cut=int(stats[0]), max_cut=int(stats[1]), nodes=int(stats[2]), leaves=int(stats[3]))
+        b.stats = dict(initial_cut=int(stats[0]), max_cut=int(stats[1]), nodes=int(stats[2]), leaves=int(stats[3]),
+                       build_cost=int(stats[4]))
         return b
 
 

@@ -69,8 +69,11 @@ def collect(n, acc):
             collect(k, acc)
 
 
-def phr(root, alpha, delta, bf):
+def phr(root, alpha, delta, bf, stats=None):
+    """stats, if a dict, receives build_cost: BuildWithCost's count (phr.go:154-255), the
+    initial cut's size plus the size of every cut handed to Split."""
     S = surface(root.box)
+    cost = [0]
 
     def thr(depth):  # DefaultThreshold
         return S / (2.0 ** (alpha * float(depth) + delta))
@@ -150,6 +153,7 @@ def phr(root, alpha, delta, bf):
                     mx, mi = len(c[0]), i
             if mx <= 1:
                 break
+            cost[0] += mx
             left, right = sweep(cuts[mi])
             if right is not None:
                 cuts[mi] = refined(left)
@@ -175,7 +179,11 @@ def phr(root, alpha, delta, bf):
                 q.extend(n.kids)
         else:
             cut.append(n)
-    return build((cut, root.box, 1))
+    cost[0] += len(cut)
+    out = build((cut, root.box, 1))
+    if stats is not None:
+        stats["build_cost"] = cost[0]
+    return out
 
 
 def export(root):

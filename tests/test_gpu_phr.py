@@ -54,3 +54,55 @@ def test_phr_1m_soup(ctx, alpha, delta, bf):
         alpha, delta, bf, o.cost(), (gp == op).mean(), len(near), len(hard)))
     assert len(hard) == 0
     assert (gp == op).mean() >= 0.9999 or len(near) <= 1e-4 * len(rays) + 2
+
+
+def oracle_grid(verts, spheres, alphas, deltas, bf, pixels):
+    """optimizer.go:44-94 (OptimizedPHRparams, omega, evalPHR) over oracle PHR builds."""
+    o = O.lbvh(verts, spheres)
+    evs = []
+    for a in alphas:
+        for d in deltas:
+            ph = o.phr(a, d, bf)
+            evs.append((ph.cost(), ph.stats["build_cost"], a, d))
+    max_b = max(e[1] for e in evs)
+    max_s = max(e[0] for e in evs)
+    n = verts.shape[0] + (0 if spheres is None else spheres.shape[0])
+    q = n / 2e6
+    om = (q * q) * (pixels / 2e5)
+    best, pick = float("inf"), None
+    for e in evs:
+        c = e[1] / max_b + (om * om) * (e[0] / max_s)
+        if c < best:
+            best, pick = c, (e[2], e[3])
+    return pick, evs
+
+
+GRID_CASES = [
+    ("soup20k_default_grid", lambda: (scenes.soup(20_000, seed=11)["verts"], None), None, None, 2, (1920, 1080)),
+    ("soup5k_bf4", lambda: (scenes.soup(5000, seed=12)["verts"], None), [0.4, 0.5], [3, 6, 9], 4, (640, 480)),
+    ("terrain129_sun_deep_grid", lambda: (scenes.terrain(129)["verts"], scenes.terrain(129)["spheres"]),
+     [0.4, 0.55], [6, 8, 10, 12], 2, (1920, 1080)),
+    # omega large enough for the SAH term to decide
+    ("terrain257_large_frame", lambda: (scenes.terrain_tris(257, seed=2), None), [0.45, 0.55], [6, 9], 2,
+     (40000, 40000)),
+]
+
+
+@pytest.mark.parametrize("name,make,alphas,deltas,bf,frame", GRID_CASES, ids=[c[0] for c in GRID_CASES])
+def test_grid_optimizer_matches_oracle(ctx, name, make, alphas, deltas, bf, frame):
+    verts, spheres = make()
+    verts = np.ascontiguousarray(verts, np.float32)
+    ds = pt.DeviceScene(ctx, verts, spheres=spheres)
+    aux = pt.DefaultLBVH(ds)
+    opt = pt.NewDefaultGridOptimizer(*frame) if alphas is None else pt.NewGridOptimizer(alphas, deltas, *frame)
+    got = opt.OptimizedPHRparams(aux, bf)
+    want, evs = oracle_grid(verts, spheres, opt.Alphas, opt.Deltas, bf, frame[0] * frame[1])
+    for (a, d, sah, build), (osah, obuild, oa, od) in zip(opt.evaluations, evs):
+        assert (a, d) == (oa, od)
+        assert build == obuild, (a, d, build, obuild)
+        assert sah == pytest.approx(osah, rel=1e-12), (a, d)
+    assert got == want, (got, want, opt.evaluations)
+    # BuildWithCost on the chosen parameters reports the same build cost
+    tree, cost = pt.NewPHRBuilder(got[0], got[1], bf).BuildWithCost(aux)
+    k = [(e[0], e[1]) for e in opt.evaluations].index(got)
+    assert cost == opt.evaluations[k][3] and tree.Cost() == pytest.approx(opt.evaluations[k][2], rel=1e-12)

@@ -214,9 +214,12 @@ def test_phr_matches_python_restatement(n, alpha, delta, bf):
     s = scenes.cornell() if n == 972 else scenes.soup(n, seed=n)
     b = O.lbvh(s["verts"])
     aux_tree = phr_py.parse(*b.export())
-    want = phr_py.export(phr_py.phr(aux_tree, alpha, delta, bf))
-    got = b.phr(alpha, delta, bf).export()
+    st = {}
+    want = phr_py.export(phr_py.phr(aux_tree, alpha, delta, bf, st))
+    ph = b.phr(alpha, delta, bf)
+    got = ph.export()
     assert canonical_equal(got, want), first_mismatch(got, want)
+    assert ph.stats["build_cost"] == st["build_cost"]  # BuildWithCost's count
 
 
 def test_phr_invariants():

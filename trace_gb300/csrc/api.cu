@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <cerrno>
+#include <cfloat>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -335,7 +336,8 @@ extern "C" int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width) {
     return gbt_check_device_error(ctx, "bvh_set_layout");
 }
 
-extern "C" int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out) {
+static int phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, bool view,
+                     gbt_bvh **out) {
     if (!ctx || !aux || !out) return GBT_EINVAL;
     *out = nullptr;
     if (aux->kind != GBT_BVH_LBVH) return gbt_fail(ctx, GBT_EINVAL, "phr_build: the auxiliary BVH must be an LBVH");
@@ -347,11 +349,23 @@ extern "C" int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double de
     b->arity = branching == 2 ? 2 : 4;
     int rc = gbt_phr_run(ctx, aux, alpha, delta, branching, b);
     if (!rc) rc = gbt_check_device_error(ctx, "phr_build");
-    if (!rc) rc = gbt_collapse4(ctx, b);
-    if (!rc) rc = gbt_check_device_error(ctx, "phr_build traversal view");
+    if (!rc && view) rc = gbt_collapse4(ctx, b);
+    if (!rc && view) rc = gbt_check_device_error(ctx, "phr_build traversal view");
     if (rc) { gbt_bvh_destroy(b); return rc; }
     *out = b;
     return GBT_OK;
+}
+
+extern "C" int gbt_phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, gbt_bvh **out) {
+    return phr_build(ctx, aux, alpha, delta, branching, true, out);
+}
+
+extern "C" int gbt_phr_build_with_cost(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching,
+                                       gbt_bvh **out, int64_t *build_cost) {
+    if (!build_cost) return GBT_EINVAL;
+    int rc = phr_build(ctx, aux, alpha, delta, branching, true, out);
+    *build_cost = rc ? 0 : (*out)->build_cost;
+    return rc;
 }
 
 // ---------------------------------------------------------------------------
@@ -505,6 +519,56 @@ extern "C" int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost) {
     GBT_TRY(export_tree(ctx, bvh, o));
     size_t i = 0;
     *cost = cost_at(o, i);
+    return GBT_OK;
+}
+
+// gridOptimizer.OptimizedPHRparams (optimizer.go:44-84) with omega and evalPHR
+// (optimizer.go:86-94): every (alpha, delta) of the grid, alphas outer, is built
+// on the device with its build cost; the SAH cost (bvh.go:226-239) is evaluated
+// on the downloaded tree; the first minimum of the normalised score wins.
+extern "C" int gbt_phr_optimize_grid(gbt_ctx *ctx, gbt_bvh *aux, int32_t branching, const double *alphas,
+                                     int32_t n_alpha, const double *deltas, int32_t n_delta, int32_t frame_width,
+                                     int32_t frame_height, double *alpha, double *delta, double *evals) {
+    if (!ctx || !aux || !alphas || !deltas || !alpha || !delta) return GBT_EINVAL;
+    if (n_alpha < 1 || n_delta < 1 || frame_width < 1 || frame_height < 1)
+        return gbt_fail(ctx, GBT_EINVAL, "phr_optimize_grid: empty grid or frame");
+    struct Eval { double sah; int64_t build; double a, d; };
+    std::vector<Eval> ev;
+    for (int32_t i = 0; i < n_alpha; i++) {
+        for (int32_t j = 0; j < n_delta; j++) {
+            gbt_bvh *b = nullptr;
+            GBT_TRY(phr_build(ctx, aux, alphas[i], deltas[j], branching, false, &b));
+            double sah = 0.0;
+            int rc = gbt_bvh_cost(ctx, b, &sah);
+            const int64_t bc = b->build_cost;
+            gbt_bvh_destroy(b);
+            if (rc) return rc;
+            ev.push_back({sah, bc, alphas[i], deltas[j]});
+        }
+    }
+    int64_t max_build = 0;
+    double max_sah = 0.0;
+    for (const Eval &e : ev) {
+        if (e.build > max_build) max_build = e.build;
+        if (e.sah > max_sah) max_sah = e.sah;
+    }
+    const double q = (double)aux->n_prim / 2000000.0;               // PRIM_THRESH
+    const double o = (q * q) * ((double)frame_width * (double)frame_height / 200000.0);  // RES_THRESH
+    double best = DBL_MAX;
+    size_t bi = 0;
+    for (size_t k = 0; k < ev.size(); k++) {
+        const double c = (double)ev[k].build / (double)max_build + (o * o) * (ev[k].sah / max_sah);
+        if (c < best) {
+            best = c;
+            bi = k;
+        }
+        if (evals) {
+            evals[2 * k] = ev[k].sah;
+            evals[2 * k + 1] = (double)ev[k].build;
+        }
+    }
+    *alpha = ev[bi].a;
+    *delta = ev[bi].d;
     return GBT_OK;
 }
 

@@ -105,6 +105,7 @@ struct gbt_bvh {
     int32_t *d_other = nullptr;     // emission hand-off words
     uint2 *d_range = nullptr;       // per inner node: distinct-code range [l, r]
     uint32_t n_nodes_host = 0;      // PHR: nodes allocated in d_nodes
+    int64_t build_cost = 0;         // PHR: BuildWithCost's count (phr.go:154-255)
     // 4-wide traversal view of a binary tree (collapse.cu); used by traversal when present
     float4 *d_nodes4 = nullptr;
     BvhHeader *d_hdr4 = nullptr;

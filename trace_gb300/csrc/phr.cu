@@ -55,6 +55,7 @@ struct PhrGlobals {
     int32_t root;
     uint32_t pad;
     uint32_t job_ctr[2], pool_ctr[2], max_n[2];
+    unsigned long long build_cost;  // sizes of the cuts handed to Split (phr.go:214)
 };
 
 // ---------------------------------------------------------------------------
@@ -588,6 +589,7 @@ __global__ void __launch_bounds__(PT) k_phr_level(LevelArgs A) {
             for (int i = 0; i < nc; i++)
                 if (s_cuts[i].n > mx) { mx = s_cuts[i].n; mi = i; }
             if (mx <= 1) break;
+            if (threadIdx.x == 0) atomicAdd(&A.g->build_cost, (unsigned long long)mx);
             const Cut cut = s_cuts[mi];
             const uint32_t n = cut.n;
             for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
@@ -903,6 +905,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
     uint32_t n_jobs = g.job_ctr[0], nmax = g.max_n[0];
+    const uint64_t initial_cut = g.pool_ctr[0];
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int parity = 0;
@@ -967,6 +970,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
     out->n_nodes_host = g.pnode_ctr;
+    out->build_cost = (int64_t)(initial_cut + g.build_cost);  // BuildWithCost (phr.go:154-192)
     if (scratch) cudaFree(scratch);
     cleanup();
     return GBT_OK;

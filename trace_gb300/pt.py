@@ -409,9 +409,52 @@ class PhrBuilder:
         out.aux = aux
         return out
 
+    def BuildWithCost(self, aux: BVH):
+        """phr.go:154-192: (tree, build cost = initial cut size + sizes of the cuts split)."""
+        ctx = aux.ctx
+        h = C.c_void_p()
+        cost = C.c_int64()
+        ctx.check(ctx.L.gbt_phr_build_with_cost(ctx.h, aux.h, float(self.Alpha), float(self.Delta),
+                                                int(self.BranchingFactor), C.byref(h), C.byref(cost)),
+                  "phr_build_with_cost")
+        return BVH(ctx, h, aux.scene, "phr"), int(cost.value)
+
 
 def NewPHRBuilder(alpha, delta, branching_factor):
     return PhrBuilder(alpha, delta, branching_factor)
+
+
+@dataclass
+class GridOptimizer:
+    """optimizer.go:19-94: exhaustive (alpha, delta) search scored by build cost and SAH cost."""
+    Alphas: list
+    Deltas: list
+    pixels: int
+    width: int = 0
+    height: int = 0
+
+    def OptimizedPHRparams(self, aux: BVH, branching: int = 2, threads: int = 0):
+        """(alpha, delta) of the best candidate; self.evaluations holds (alpha, delta, sah, build) per
+        candidate in grid order.  `threads` is accepted for the reference's signature."""
+        ctx = aux.ctx
+        al = np.ascontiguousarray(self.Alphas, np.float64)
+        de = np.ascontiguousarray(self.Deltas, np.float64)
+        ev = np.zeros((al.size * de.size, 2), np.float64)
+        a, d = C.c_double(), C.c_double()
+        w, h = (self.width, self.height) if self.width * self.height == self.pixels else (self.pixels, 1)
+        ctx.check(ctx.L.gbt_phr_optimize_grid(ctx.h, aux.h, int(branching), _p(al), al.size, _p(de), de.size, w, h,
+                                              C.byref(a), C.byref(d), _p(ev)), "phr_optimize_grid")
+        self.evaluations = [(float(x), float(y), float(ev[k, 0]), int(ev[k, 1]))
+                            for k, (x, y) in enumerate((x, y) for x in al for y in de)]
+        return a.value, d.value
+
+
+def NewGridOptimizer(alphas, deltas, frameWidth, frameHeight):
+    return GridOptimizer(list(alphas), list(deltas), frameWidth * frameHeight, frameWidth, frameHeight)
+
+
+def NewDefaultGridOptimizer(frameWidth, frameHeight):
+    return NewGridOptimizer([0.4, 0.45, 0.5, 0.55], [6, 7, 8, 9], frameWidth, frameHeight)  # optimizer.go:25-27
 
 
 def NewDefaultBuilder():
