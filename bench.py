@@ -401,6 +401,41 @@ def run_terrain_workload(args):
     return 0
 
 
+def run_lbvh_workload(args):
+    """LBVH build throughput alone: the 1M soup and the 8.4M-triangle terrain (with its
+    sun sphere), K timed rebuilds each after W warm-up builds, CUDA events on the
+    library's stream, inputs resident in HBM."""
+    import torch
+
+    from trace_gb300 import pt, scenes
+
+    ctx = pt.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    hbm, peak_kind = peaks()
+    out = {"metric": "LBVH Mtri/s", "unit": "Mtri/s", "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak": hbm,
+           "peak_source": peak_kind}
+    for name, s in (("soup1M", scenes.soup(N_TRI, seed=1)), ("terrain2048", scenes.terrain(2048))):
+        ds = pt.DeviceScene.from_dict(ctx, s)
+        n = ds.n_prim
+        aux = pt.DefaultLBVH(ds)
+        for _ in range(max(1, args.warmup)):
+            ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
+        e1.record(stream)
+        ctx.sync()
+        ms = e0.elapsed_time(e1) / args.steps
+        bw = n * LBVH_BYTES_PER_TRI / (ms * 1e-3) / 1e9
+        out[name] = {"triangles": n, "ms": ms, "mtri_s": n / ms / 1e3, "achieved_gbs": bw, "frac": bw / hbm}
+        aux.close()
+        ds.close()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_case(args):
     """The benchmark's scene, without timing: a case small enough for an ncu capture
     (about 0.3 GB on the device for the soup, 3 GB for the terrain).  `render`: 3
@@ -448,10 +483,11 @@ def main():
                     help="run a small fixed case for an ncu capture and exit: 3 frames (render) or 3 LBVH builds")
     ap.add_argument("--profile-scene", choices=["soup", "terrain"], default="soup",
                     help="scene of --profile lbvh: the 1M soup or the 8.4M-triangle terrain")
-    ap.add_argument("--workload", choices=["soup", "batch", "adjoint", "terrain"], default="soup",
+    ap.add_argument("--workload", choices=["soup", "batch", "adjoint", "terrain", "lbvh"], default="soup",
                     help="soup: the headline 1M-triangle frame; batch: the 64-scene batched render; "
                          "adjoint: forward+backward iteration of the differentiable render; "
-                         "terrain: LBVH/PHR builds and the 64 spp render of the 8.4M-triangle terrain")
+                         "terrain: LBVH/PHR builds and the 64 spp render of the 8.4M-triangle terrain; "
+                         "lbvh: LBVH build throughput on the soup and the terrain")
     ap.add_argument("--batch-scenes", type=int, default=64)
     args = ap.parse_args()
     ws, rank, local = dist_env()
@@ -465,6 +501,8 @@ def main():
         return run_adjoint_workload(args)
     if args.workload == "terrain":
         return run_terrain_workload(args)
+    if args.workload == "lbvh":
+        return run_lbvh_workload(args)
     args.warmup = max(args.warmup, 3)
 
     import torch

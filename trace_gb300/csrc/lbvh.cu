@@ -17,7 +17,12 @@
 namespace {
 
 constexpr int SORT_THREADS = 256;
-constexpr int SORT_ITEMS = 16;
+// Keys per thread of a sort tile; the register budget allows 2 * 16 / SORT_ITEMS
+// resident blocks per SM.
+#ifndef GBT_SORT_ITEMS
+#define GBT_SORT_ITEMS 16
+#endif
+constexpr int SORT_ITEMS = GBT_SORT_ITEMS;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_PREFIX = 2u << 30;
@@ -78,10 +83,38 @@ __device__ __forceinline__ void prim_box_f64(const float *__restrict__ verts, co
 // ---------------------------------------------------------------------------
 // scene bounds
 // ---------------------------------------------------------------------------
+// Triangle boxes are float32 values, so their fold is done in float32 (exact)
+// over the vertex array read as float4 triples: 12 floats hold 4 vertices with
+// the axis pattern x y z x | y z x y | z x y z.  Sphere boxes (c -+ r in
+// float64) are folded in float64.
 __global__ void __launch_bounds__(256) k_bounds(const float *__restrict__ verts, const float4 *__restrict__ sph,
                                                 uint32_t n_tri, uint32_t n, unsigned long long *acc) {
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float flo[3] = {INFINITY, INFINITY, INFINITY}, fhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const size_t nf = (size_t)n_tri * 9, nchunk = nf / 12;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const float4 *v4 = reinterpret_cast<const float4 *>(verts);
+    for (size_t c = tid; c < nchunk; c += stride) {
+        const float4 a = __ldg(v4 + 3 * c), b = __ldg(v4 + 3 * c + 1), d = __ldg(v4 + 3 * c + 2);
+        flo[0] = fminf(fminf(fminf(flo[0], a.x), fminf(a.w, b.z)), d.y);
+        fhi[0] = fmaxf(fmaxf(fmaxf(fhi[0], a.x), fmaxf(a.w, b.z)), d.y);
+        flo[1] = fminf(fminf(fminf(flo[1], a.y), fminf(b.x, b.w)), d.z);
+        fhi[1] = fmaxf(fmaxf(fmaxf(fhi[1], a.y), fmaxf(b.x, b.w)), d.z);
+        flo[2] = fminf(fminf(fminf(flo[2], a.z), fminf(b.y, d.x)), d.w);
+        fhi[2] = fmaxf(fmaxf(fmaxf(fhi[2], a.z), fmaxf(b.y, d.x)), d.w);
+    }
+    for (size_t f = nchunk * 12 + tid; f < nf; f += stride) {
+        const float x = __ldg(verts + f);
+        const int k = (int)(f % 3);
+        flo[k] = fminf(flo[k], x);
+        fhi[k] = fmaxf(fhi[k], x);
+    }
+    double lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        lo[k] = (double)flo[k];
+        hi[k] = (double)fhi[k];
+    }
+    for (uint32_t i = n_tri + (uint32_t)tid; i < n; i += (uint32_t)stride) {
         double a[3], b[3];
         prim_box_f64(verts, sph, n_tri, i, a, b);
 #pragma unroll
@@ -126,16 +159,43 @@ __device__ __forceinline__ uint64_t spread3(uint64_t a) {
     return x;
 }
 
+// float32 -> float64 by moving the exponent and mantissa fields (exact; the
+// fp64 pipe is the scarce unit here).  Zero, subnormal, Inf and NaN take the
+// ordinary conversion.
+__device__ __forceinline__ double widen(float x) {
+    const uint32_t b = __float_as_uint(x), e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const uint64_t d = ((uint64_t)(b & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                       ((uint64_t)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)d);
+}
+
+// x * 0.5 by decrementing the exponent field when the result stays normal (exact).
+__device__ __forceinline__ double halve(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x), e = (b >> 52) & 0x7ffu;
+    if (e > 1u && e < 0x7ffu) return __longlong_as_double((long long)(b - (1ull << 52)));
+    return __dmul_rn(x, 0.5);
+}
+
 // uint64(dx / step) exactly as the reference computes it: a correctly rounded
 // float64 division, truncated.  The product with the rounded reciprocal is
 // within a few ulp of the quotient, so its integer part is the answer unless
 // the quotient lies within 2^-26 of an integer; only then is the division done.
+// The integer and fractional parts of the product are read off its bits.
 __device__ __forceinline__ uint64_t quantise(double dx, double step, double rstep) {
-    double qa = __dmul_rn(dx, rstep);
-    if (qa >= 0.0 && qa < 4194304.0) {
-        double f = floor(qa);
-        double fr = qa - f;
-        if (fr > 0x1p-26 && fr < 1.0 - 0x1p-26) return (uint64_t)f;
+    const uint64_t b = (uint64_t)__double_as_longlong(__dmul_rn(dx, rstep));
+    // 0 <= qa < 2^22 (dx >= 0, rstep > 0; NaN and larger values have larger bit patterns)
+    if (b < 0x4150000000000000ull) {
+        const int E = (int)(b >> 52) - 1023;  // qa in [2^E, 2^(E+1)), or qa < 1
+        if (E < 0) {
+            // integer part 0, fraction qa: 2^-26 < qa < 1 - 2^-26
+            if (b > 0x3e50000000000000ull && b < 0x3feffffff8000000ull) return 0;
+        } else {
+            const uint64_t m = (b & 0xfffffffffffffull) | (1ull << 52);
+            const int fb = 52 - E;  // fraction bits, 31..52
+            const uint64_t frac = m & ((1ull << fb) - 1), lo = 1ull << (fb - 26);
+            if (frac > lo && frac < (1ull << fb) - lo) return m >> fb;
+        }
     }
     double q = __ddiv_rn(dx, step);
     if (!(q < 9223372036854775808.0) || q < 0.0) return 0;  // NaN (zero-extent axis) or out of domain
@@ -158,12 +218,22 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double lo[3], hi[3];
-        prim_box_f64(verts, sph, n_tri, i, lo, hi);
+        if (i < n_tri) {
+            const float *t = verts + (size_t)i * 9;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float a = __ldg(t + k), b = __ldg(t + 3 + k), c = __ldg(t + 6 + k);
+                lo[k] = widen(fminf(fminf(a, b), c));
+                hi[k] = widen(fmaxf(fmaxf(a, b), c));
+            }
+        } else {
+            prim_box_f64(verts, sph, n_tri, i, lo, hi);
+        }
         uint64_t q[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            double c = __dmul_rn(__dadd_rn(lo[k], hi[k]), 0.5);  // aabb barycenter
-            double dx = fabs(__dsub_rn(s_e[k], c));
+            const double c = halve(__dadd_rn(lo[k], hi[k]));  // aabb barycenter
+            const double dx = __longlong_as_double(__double_as_longlong(__dsub_rn(s_e[k], c)) & 0x7fffffffffffffffll);
             q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
         }
         codes[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
@@ -301,7 +371,7 @@ __device__ __forceinline__ uint32_t lookback_wait(const uint32_t *p, unsigned in
 // counts into warp-private shared histograms), publish the tile's digit
 // counts, look back over earlier tiles for the global offsets, stage the tile
 // in shared memory in digit order and write it out in runs.
-__global__ void __launch_bounds__(SORT_THREADS, 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
+__global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                               uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
                                                               unsigned int *err) {
     if (!plan->active[pass]) return;
