@@ -614,6 +614,12 @@ __device__ __forceinline__ int prefix_len(const uint64_t *__restrict__ ukey, uin
 // (the reference splits a range at the highest differing bit, lbvh.go:147-176,
 // so that boundary is its parent's split).  Inner node k is the split k|k+1.
 // The second child to arrive at a node folds both boxes and carries on.
+__device__ __forceinline__ int32_t exch_acq_rel(int32_t *p, int32_t v) {
+    int32_t old;
+    asm volatile("atom.acq_rel.gpu.global.exch.b32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
                                               const uint32_t *__restrict__ run, const uint64_t *__restrict__ ukey,
                                               const float4 *__restrict__ recs, float4 *nodes, int32_t *other,
@@ -650,10 +656,10 @@ __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader
         reinterpret_cast<float2 *>(nd + 2)[slot] = make_float2(lo.z, hi.z);
         reinterpret_cast<int2 *>(nd + 3)[slot] = make_int2(ref, cnt);
         if (cnt == 0) parent_of[ref] = (int32_t)p;
-        __threadfence();
-        int32_t o = atomicExch(&other[p], (int32_t)(left ? l : r));
+        // release: this child's slot is visible before the hand-off word; acquire: the
+        // sibling's slot, written before its own exchange, is read after this one
+        int32_t o = exch_acq_rel(&other[p], (int32_t)(left ? l : r));
         if (o < 0) return;  // first child here: the sibling finishes the node
-        __threadfence();
         float4 sb = __ldcg(nd + (slot ^ 1));
         float2 sz = __ldcg(reinterpret_cast<const float2 *>(nd + 2) + (slot ^ 1));
         int2 sr = __ldcg(reinterpret_cast<const int2 *>(nd + 3) + (slot ^ 1));
