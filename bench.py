@@ -517,10 +517,21 @@ def main():
     aux = pt.DefaultLBVH(ds)
     bvh_name = "lbvh"
     bvh = aux
+    phr_build = None
     if args.bvh == "phr":
         try:
             bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux)
             bvh_name = "phr(alpha=0.5,delta=6,bf=2)"
+            # PHR build time (host-driven, one launch per tree level): two more builds, wall clock
+            walls = []
+            for _ in range(2):
+                ctx.sync()
+                t0 = time.perf_counter()
+                extra = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux)
+                ctx.sync()
+                walls.append((time.perf_counter() - t0) * 1e3)
+                extra.close()
+            phr_build = {"ms": min(walls), "note": "wall clock of PhrBuilder.BuildFromAuxilary incl. its 4-wide view"}
         except _lib.GbtError as e:
             if e.code != -6:
                 raise
@@ -622,6 +633,8 @@ def main():
     lb_ms = sum(a.elapsed_time(b) for a, b in lb_ev) / args.steps
     lb_ms = dist.reduce(lb_ms, "max")
     lb_bw = N_TRI * LBVH_BYTES_PER_TRI / (lb_ms * 1e-3) / 1e9
+    if phr_build is not None:
+        phr_build["lbvh_plus_phr_mtri_s"] = N_TRI / (lb_ms + phr_build["ms"]) / 1e3
     lbvh = {"mtri_s": N_TRI / lb_ms / 1e3 * ws, "ms": lb_ms,
             "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
                          "bytes_per_tri": LBVH_BYTES_PER_TRI, "traffic": None, "kernel": "whole build (15 launches)"}}
@@ -642,7 +655,8 @@ def main():
                     "api": "gbt_render (C ABI), pinned host image"},
             "gpu_launches": int(timed["kernel_launches"]),
             "clocks": clk,
-            "lbvh": lbvh}
+            "lbvh": lbvh,
+            "phr_build": phr_build}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, seconds=args.cpu_seconds)
     if rank == 0:

@@ -28,6 +28,9 @@ namespace {
 
 constexpr uint32_t MAX_CUT_SIZE = 2500;  // phr.go:11
 constexpr int PT = 256;                  // threads per job block
+#ifndef PHR_SMALL_CUT
+#define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
+#endif
 constexpr int DEPTH_TABLE = 4096;
 
 struct AuxNode {
@@ -518,11 +521,15 @@ __device__ void attach(const LevelArgs &A, int32_t parent, int32_t slot, int32_t
     else A.pn[parent].child[slot] = child;
 }
 
-__global__ void __launch_bounds__(PT) k_phr_level(LevelArgs A) {
-    __shared__ BoxAgg s_tmp[PT / 32];
-    __shared__ BoxAgg s_rank[PT];
-    __shared__ double s_cost[PT];
-    __shared__ uint32_t s_idx[PT];
+// One block per job; BS threads per block.  Levels whose largest cut is small
+// run with one-warp blocks (BS = 32), so a job costs warp barriers only and 32
+// jobs are resident per SM.
+template <int BS>
+__global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
+    __shared__ BoxAgg s_tmp[BS / 32];
+    __shared__ BoxAgg s_rank[BS];
+    __shared__ double s_cost[BS];
+    __shared__ uint32_t s_idx[BS];
     __shared__ uint32_t s_u[32];
     __shared__ Cut s_cuts[4];
     __shared__ int32_t s_branch, s_ncuts;
@@ -909,10 +916,12 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int parity = 0;
-    const int max_grid = ctx->num_sms * 4;
+    const int max_grid = ctx->num_sms * 4;         // 256-thread blocks
+    const int max_grid_small = ctx->num_sms * 16;  // one-warp blocks (about 18 resident per SM)
     int levels = 0;
     while (n_jobs > 0) {
-        uint32_t grid = std::min<uint32_t>(n_jobs, (uint32_t)max_grid);
+        const bool small = nmax <= PHR_SMALL_CUT;
+        uint32_t grid = std::min<uint32_t>(n_jobs, (uint32_t)(small ? max_grid_small : max_grid));
         size_t per_block = gbt_align(scratch_bytes_for(nmax));
         size_t need = per_block * grid;
         if (need > scratch_bytes) {
@@ -952,7 +961,8 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         A.bf = bf;
         A.n_prim = N;
         A.err = ctx->d_error;
-        k_phr_level<<<grid, PT, 0, st>>>(A);
+        if (small) k_phr_level<32><<<grid, 32, 0, st>>>(A);
+        else k_phr_level<PT><<<grid, PT, 0, st>>>(A);
         GBT_CUDA(ctx, cudaGetLastError());
         GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaStreamSynchronize(st));
