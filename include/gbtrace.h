@@ -202,6 +202,17 @@ int gbt_trace_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t 
 /* ---- renderer (render.go:91-129 ImageRenderer.RenderToBuffer) -------- */
 /* rgb: width*height*3 floats, row y=0 is the bottom row (buffer.go:47-49
  * order); each pixel is the mean of spp samples. */
+/* pkg/pt/render.go:137-197 HeatMapRenderer.RenderToBuffer: per pixel the
+ * pixel-centre ray's BVH.traversalSteps (bvh.go:21-44: inner nodes whose box
+ * is intersected, children popped last-first, culled by the closest hit so
+ * far) coloured by DefaultTraversalCountShader (render.go:250-257) with
+ * `threshold` (NewHeatMapRenderer, render.go:145-153).  Counted on the tree
+ * as built (binary LBVH or PHR nodes).  rgb: width*height*3 floats, row y = 0
+ * first; counts (optional): width*height int32. */
+int gbt_heatmap(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, int32_t width, int32_t height, int32_t threshold,
+                float *rgb, int32_t *counts);
+int gbt_heatmap_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, int32_t width, int32_t height,
+                      int32_t threshold, float *d_rgb, int32_t *d_counts);
 int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
                float *rgb, gbt_render_stats *stats);
 /* Same into a device buffer; enqueue only; stats are read by gbt_render_last_stats. */

@@ -19,6 +19,7 @@
  */
 #include "oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdatomic.h>
@@ -894,6 +895,46 @@ void orc_camera_rays(const orc_camera_desc *cam, int32_t width, int32_t height,
         dirs[3 * i + 1] = d.y;
         dirs[3 * i + 2] = d.z;
     }
+}
+
+/* HeatMapRenderer.RenderToBuffer (render.go:167-197): pixel-centre rays
+ * (u = x/(w-1), v = y/(h-1)), BVH.traversalSteps from 0.001 to MaxFloat64
+ * (bvh.go:21-44) and DefaultTraversalCountShader (render.go:250-257).
+ * rgb: width*height*3 (row y = 0 first); counts optional. */
+typedef struct {
+    const orc_bvh *b;
+    ocam k;
+    int32_t w, h, thr;
+    double *rgb;
+    int32_t *counts;
+} heat_ctx;
+
+static void heat_job(void *c, int64_t y) {
+    heat_ctx *x = (heat_ctx *)c;
+    for (int32_t xx = 0; xx < x->w; xx++) {
+        double u = (double)xx / (double)(x->w - 1), v = (double)y / (double)(x->h - 1);
+        oray r = make_ray(x->k.origin, cam_dir(&x->k, u, v));
+        int32_t cnt = traversal_steps(x->b, &r, 0.001, DBL_MAX);
+        int64_t p = y * x->w + xx;
+        double *o = x->rgb + 3 * p;
+        if (cnt > x->thr) {
+            o[0] = (double)cnt / (double)x->thr * 2;
+            o[1] = 0;
+            o[2] = 0;
+        } else {
+            double f = (double)cnt / ((double)x->thr * 1.25);
+            o[0] = 0;
+            o[1] = f;
+            o[2] = 1 - f;
+        }
+        if (x->counts) x->counts[p] = cnt;
+    }
+}
+
+void orc_heatmap(const orc_bvh *b, const orc_camera_desc *cam, int32_t width, int32_t height, int32_t threshold,
+                 int threads, double *rgb, int32_t *counts) {
+    heat_ctx x = {b, make_camera(cam), width, height, threshold, rgb, counts};
+    orc_parallel(threads, height, heat_job, &x);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -96,6 +96,11 @@ void orc_camera_rays(const orc_camera_desc *cam, int32_t width, int32_t height,
 int orc_adjoint(const orc_bvh *b, const orc_camera_desc *cam, const orc_render_desc *rd, const float *albedo,
                 const float *emission, const float *dimg, double *img, double *g_albedo, double *g_emission);
 
+/* HeatMapRenderer.RenderToBuffer with traversalSteps and DefaultTraversalCountShader
+ * (render.go:137-197,250-257, bvh.go:21-44): rgb width*height*3, counts optional. */
+void orc_heatmap(const orc_bvh *b, const orc_camera_desc *cam, int32_t width, int32_t height, int32_t threshold,
+                 int threads, double *rgb, int32_t *counts);
+
 /* ---- PHR ---- */
 /* stats: initial cut size, largest cut, nodes, leaves, BuildWithCost's build cost */
 int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[5]);

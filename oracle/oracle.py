@@ -61,6 +61,7 @@ def lib():
         L.orc_render.argtypes = [P, P, P, P, P, P, P]
         L.orc_adjoint.restype = C.c_int
         L.orc_adjoint.argtypes = [P, P, P, P, P, P, P, P, P]
+        L.orc_heatmap.argtypes = [P, P, i32, i32, i32, C.c_int, P, P]
         L.orc_phr_build.restype = C.c_int
         L.orc_phr_build.argtypes = [P, d, d, C.c_int, C.POINTER(P), P]
         _lib = L
@@ -227,6 +228,20 @@ class BVH:
         if rc != 0:
             raise RuntimeError("oracle adjoint failed: %d" % rc)
         return img, ga, ge
+
+    def heatmap(self, camera, width, height, threshold, threads=None):
+        """(rgb float64 (h, w, 3), counts int32 (h, w)) of the reference's heat-map renderer."""
+        cd = CameraDesc()
+        cd.look_from[:] = camera["look_from"]
+        cd.look_at[:] = camera["look_at"]
+        cd.up[:] = camera["up"]
+        cd.aspect = camera["aspect"]
+        cd.fov_deg = camera["fov"]
+        rgb = np.empty((height, width, 3), np.float64)
+        counts = np.empty((height, width), np.int32)
+        lib().orc_heatmap(self.h, C.byref(cd), width, height, threshold, threads or (os.cpu_count() or 1), _p(rgb),
+                          _p(counts))
+        return rgb, counts
 
     def phr(self, alpha=0.5, delta=6.0, bf=2):
         h = C.c_void_p()

@@ -106,3 +106,16 @@ def test_grid_optimizer_matches_oracle(ctx, name, make, alphas, deltas, bf, fram
     tree, cost = pt.NewPHRBuilder(got[0], got[1], bf).BuildWithCost(aux)
     k = [(e[0], e[1]) for e in opt.evaluations].index(got)
     assert cost == opt.evaluations[k][3] and tree.Cost() == pytest.approx(opt.evaluations[k][2], rel=1e-12)
+
+
+@pytest.mark.parametrize("alpha,delta,bf", [(0.5, 9.0, 3), (0.55, 9.0, 4), (0.5, 12.0, 3)])
+def test_phr_terrain_with_sun_matches_oracle(ctx, alpha, delta, bf):
+    """Branching 3 and 4 split refined cuts of a job again inside the same block: those cuts
+    can be up to 2^(bf-2) times the job's own cut, which the per-block scratch must hold."""
+    s = scenes.terrain(129)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.NewPHRBuilder(alpha, delta, bf).BuildFromAuxilary(pt.DefaultLBVH(ds))
+    o = O.lbvh(s["verts"], s["spheres"]).phr(alpha, delta, bf)
+    ge, oe = g.export(), o.export()
+    assert canonical_equal(ge, oe), first_mismatch(ge, oe)
+    assert g.Cost() == pytest.approx(o.cost(), rel=1e-12)

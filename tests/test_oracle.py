@@ -243,3 +243,22 @@ def test_render_light_only_sees_emission():
               render=dict(width=8, height=8, spp=2, max_depth=0, miss_mode=0, miss_color=(0, 0, 0)))
     img = b.render(sc)
     np.testing.assert_allclose(img, 10.0)
+
+
+def test_heatmap_matches_python_restatement():
+    """The oracle's heat map (render.go:137-197, bvh.go:21-44) against tests/heat_py.py on the
+    Cornell box, LBVH and PHR trees: identical step counts and colours."""
+    from tests import heat_py
+
+    s = scenes.cornell()
+    w, h, thr = 24, 18, 20
+    cam = dict(s["camera"], aspect=w / h)
+    tris = [tuple(float(x) for x in t) for t in s["verts"]]
+    b = O.lbvh(s["verts"])
+    for tree in (b, b.phr(0.5, 6, 2), b.phr(0.55, 9, 4)):
+        root = phr_py.parse(*tree.export())
+        want_c, want_rgb = heat_py.heatmap(root, tris, cam, w, h, thr)
+        rgb, counts = tree.heatmap(cam, w, h, thr)
+        assert counts.ravel().tolist() == want_c
+        np.testing.assert_array_equal(rgb.reshape(-1, 3), np.array(want_rgb))
+        assert counts.max() > 0

@@ -20,7 +20,7 @@ EXPORTS = [
     "gbt_ctx_create", "gbt_ctx_destroy", "gbt_last_error", "gbt_ctx_stream", "gbt_ctx_sync",
     "gbt_ctx_set_profiling", "gbt_ctx_set_option", "gbt_host_alloc", "gbt_host_free",
     "gbt_scene_upload", "gbt_scene_destroy", "gbt_obj_parse",
-    "gbt_lbvh_build", "gbt_lbvh_rebuild_async", "gbt_scene_update_async", "gbt_phr_build", "gbt_phr_build_with_cost", "gbt_phr_optimize_grid", "gbt_bvh_destroy",
+    "gbt_lbvh_build", "gbt_lbvh_rebuild_async", "gbt_scene_update_async", "gbt_heatmap", "gbt_heatmap_async", "gbt_phr_build", "gbt_phr_build_with_cost", "gbt_phr_optimize_grid", "gbt_bvh_destroy",
     "gbt_bvh_cost", "gbt_bvh_size", "gbt_bvh_counts", "gbt_bvh_export", "gbt_lbvh_sorted",
     "gbt_trace", "gbt_trace_async", "gbt_render", "gbt_render_async", "gbt_render_last_stats",
     "gbt_device_alloc", "gbt_device_free", "gbt_copy_h2d_async", "gbt_copy_d2h_async",
@@ -96,6 +96,8 @@ def load():
         "gbt_scene_update_async": ([P, P, P], C.c_int),
         "gbt_phr_build": ([P, P, d, d, i32, PP], C.c_int),
         "gbt_phr_build_with_cost": ([P, P, d, d, i32, PP, P], C.c_int),
+        "gbt_heatmap": ([P, P, P, i32, i32, i32, P, P], C.c_int),
+        "gbt_heatmap_async": ([P, P, P, i32, i32, i32, P, P], C.c_int),
         "gbt_phr_optimize_grid": ([P, P, i32, P, i32, P, i32, i32, i32, P, P, P], C.c_int),
         "gbt_bvh_destroy": ([P], C.c_int),
         "gbt_bvh_cost": ([P, P, C.POINTER(d)], C.c_int),

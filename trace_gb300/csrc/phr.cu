@@ -500,6 +500,7 @@ struct LevelArgs {
     PhrGlobals *g;
     int parity;
     uint32_t pool_cap, job_cap, pnode_cap, nmax;
+    uint32_t cap;  // per-block scratch capacity in cut nodes: nmax * 2^(bf-2)
     unsigned char *scratch;
     size_t scratch_per_block;
     int bf;
@@ -536,7 +537,7 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
     __shared__ uint32_t s_off;
     const int in = A.parity, out = A.parity ^ 1;
     const uint32_t n_jobs = A.g->job_ctr[in];
-    Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.nmax);
+    Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
     for (uint32_t j = blockIdx.x; j < n_jobs; j += gridDim.x) {
         const PJob job = A.jobs_in[j];
         if (job.n > A.nmax) {
@@ -599,6 +600,11 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
             if (threadIdx.x == 0) atomicAdd(&A.g->build_cost, (unsigned long long)mx);
             const Cut cut = s_cuts[mi];
             const uint32_t n = cut.n;
+            // a refined cut of this job can be larger than the job's own cut (bf > 2)
+            if (n > A.cap) {
+                if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+                break;
+            }
             for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
             __syncthreads();
             // SweepSAH: x from the cut order, y from the x order
@@ -922,7 +928,15 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     while (n_jobs > 0) {
         const bool small = nmax <= PHR_SMALL_CUT;
         uint32_t grid = std::min<uint32_t>(n_jobs, (uint32_t)(small ? max_grid_small : max_grid));
-        size_t per_block = gbt_align(scratch_bytes_for(nmax));
+        // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
+        // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
+        if (nmax > (1u << 28)) {
+            if (scratch) cudaFree(scratch);
+            cleanup();
+            return gbt_fail(ctx, GBT_ENOMEM, "phr: cut too large");
+        }
+        const uint32_t cap = nmax << (bf > 2 ? bf - 2 : 0);
+        size_t per_block = gbt_align(scratch_bytes_for(cap));
         size_t need = per_block * grid;
         if (need > scratch_bytes) {
             if (scratch) {
@@ -956,6 +970,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         A.job_cap = job_cap;
         A.pnode_cap = pnode_cap;
         A.nmax = nmax;
+        A.cap = cap;
         A.scratch = static_cast<unsigned char *>(scratch);
         A.scratch_per_block = per_block;
         A.bf = bf;

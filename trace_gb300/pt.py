@@ -540,6 +540,40 @@ def NewBenchmarkRenderer(bvh, camera):
     return ImageRenderer(bvh, camera, MaxDepth=5, Spp=1, Miss=MISS_WHITE)  # render.go:60-72
 
 
+@dataclass
+class HeatMapRenderer:
+    """pkg/pt/render.go:137-197: per pixel the traversal-step count of the pixel-centre ray,
+    coloured by DefaultTraversalCountShader (render.go:250-257)."""
+    Bvh: BVH
+    Camera: Camera
+    Threshold: int
+    last_counts: np.ndarray = field(default=None, repr=False)
+
+    def RenderToBuffer(self, buff: PixelBuffer):
+        ctx = self.Bvh.ctx
+        cam = make_camera(self.Camera.desc() if isinstance(self.Camera, Camera) else self.Camera)
+        rgb = np.empty((buff.height, buff.width, 3), np.float32)
+        counts = np.empty((buff.height, buff.width), np.int32)
+        ctx.check(ctx.L.gbt_heatmap(ctx.h, self.Bvh.h, C.byref(cam), buff.width, buff.height, int(self.Threshold),
+                                    _p(rgb), _p(counts)), "heatmap")
+        buff.data[...] = rgb
+        self.last_counts = counts
+        return buff
+
+    def GetBvh(self):
+        return self.Bvh
+
+    def SetBvh(self, bvh):
+        self.Bvh = bvh
+
+    def GetCamera(self):
+        return self.Camera
+
+
+def NewHeatMapRenderer(bvh, camera, threshold):
+    return HeatMapRenderer(bvh, camera, threshold)  # render.go:145-153
+
+
 def ParseFromPath(path):
     """pkg/pt/obj.go:10-17 -> (verts (n,9) float32, normals (n,9) float32 or None)."""
     L = _lib.load()
