@@ -43,11 +43,14 @@ typedef struct {
     float radius;
 } gbt_sphere; /* pkg/pt/primitive.go:25-40 Sphere */
 
-#define GBT_MAT_DIFFUSE 0 /* pkg/pt/material.go:25-42 Diffuse{Albedo} */
-#define GBT_MAT_LIGHT 1   /* pkg/pt/material.go:13-23 Light{Color} */
+#define GBT_MAT_DIFFUSE 0    /* pkg/pt/material.go:25-42 Diffuse{Albedo} */
+#define GBT_MAT_LIGHT 1      /* pkg/pt/material.go:13-23 Light{Color} */
+#define GBT_MAT_REFLECTIVE 2 /* pkg/pt/material.go:44-57 Reflective{Albedo, Diffusion} */
+#define GBT_MAT_REFRACTIVE 3 /* pkg/pt/material.go:59-106 Refractive{Albedo, Ratio} */
 typedef struct {
     int32_t type;
-    float color[3];
+    float color[3]; /* Albedo (Diffuse, Reflective, Refractive) or Color (Light) */
+    float param;    /* Reflective.Diffusion or Refractive.Ratio; unused otherwise */
 } gbt_material;
 
 typedef struct {

@@ -984,7 +984,7 @@ static v3 random_unit_vector(xrng *r) {
 typedef struct {
     const orc_bvh *b;
     const int32_t *prim_mat, *mat_type;
-    const double *mat_color;
+    const double *mat_color, *mat_param;
     const orc_render_desc *rd;
     ocam cam;
     double *acc; /* running mean per pixel (PixelBuffer) */
@@ -1007,18 +1007,49 @@ static v3 miss_color(const render_ctx *x, const oray *r) { /* render.go:228-246 
     }
 }
 
-/* DefaultClosestHitShader (render.go:209-224) with Diffuse.scatter
- * (material.go:29-38) and Light (material.go:13-23). */
+/* reflect, refract, reflectance (Schlick): material.go:88-106 */
+static v3 reflect_v(v3 v, v3 n) { return vsub(v, vmul(n, vdot(v, n) * 2)); }
+static v3 refract_v(v3 uv, v3 n, double eta) {
+    double c = fmin(vdot(vmul(uv, -1), n), 1.0);
+    v3 perp = vmul(vadd(uv, vmul(n, c)), eta);
+    v3 par = vmul(n, -sqrt(fabs(1.0 - vdot(perp, perp))));
+    return vadd(perp, par);
+}
+static double reflectance(double cosine, double ratio) {
+    double r0 = (1 - ratio) / (1 + ratio);
+    r0 = r0 * r0;
+    return r0 + (1 - r0) * pow(1 - cosine, 5);
+}
+
+/* DefaultClosestHitShader (render.go:209-224) with Light (material.go:13-23),
+ * Diffuse (:29-38), Reflective (:49-53) and Refractive (:63-86) scatter. */
 static v3 shade(const render_ctx *x, oray r, ohit h, int depth, xrng *g) {
     if (depth > x->rd->max_depth) return mk(0, 0, 0);
     depth++;
     int m = x->prim_mat[h.prim];
     v3 col = mk(x->mat_color[3 * m], x->mat_color[3 * m + 1], x->mat_color[3 * m + 2]);
-    if (x->mat_type[m] == 1) return col; /* Light: emits, does not scatter */
+    int type = x->mat_type[m];
+    if (type == 1) return col; /* Light: emits, does not scatter */
     v3 light = mk(0, 0, 0);
-    v3 sd = vadd(h.normal, random_unit_vector(g));
-    if (fabs(sd.x) <= ORC_APPROX_THRESH && fabs(sd.y) <= ORC_APPROX_THRESH && fabs(sd.z) <= ORC_APPROX_THRESH)
-        sd = h.normal;
+    v3 sd;
+    if (type == 2) { /* Reflective */
+        v3 refl = reflect_v(vunit(r.d), h.normal);
+        sd = vadd(refl, vmul(random_unit_vector(g), x->mat_param ? x->mat_param[m] : 0.0));
+        if (!(vdot(refl, h.normal) > 0)) return light;
+    } else if (type == 3) { /* Refractive */
+        double ratio = x->mat_param ? x->mat_param[m] : 1.0;
+        if (h.front) ratio = 1 / ratio;
+        v3 ud = vunit(r.d);
+        double ct = fmin(vdot(vmul(ud, -1), h.normal), 1.0);
+        double st = sqrt(1.0 - ct * ct);
+        int cannot = ratio * st > 1.0;
+        if (cannot || reflectance(ct, ratio) > xf64(g)) sd = reflect_v(ud, h.normal);
+        else sd = refract_v(ud, h.normal, ratio);
+    } else { /* Diffuse */
+        sd = vadd(h.normal, random_unit_vector(g));
+        if (fabs(sd.x) <= ORC_APPROX_THRESH && fabs(sd.y) <= ORC_APPROX_THRESH && fabs(sd.z) <= ORC_APPROX_THRESH)
+            sd = h.normal;
+    }
     oray r2 = make_ray(h.point, sd);
     ohit h2;
     memset(&h2, 0, sizeof(h2));
@@ -1068,13 +1099,14 @@ static void pass_row(void *c, int64_t y) {
 }
 
 int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_type, const double *mat_color,
-               const orc_camera_desc *cam, orc_render_desc *rd, double *rgb) {
+               const double *mat_param, const orc_camera_desc *cam, orc_render_desc *rd, double *rgb) {
     if (rd->width < 2 || rd->height < 2) return ORC_E_ARG;
     render_ctx x;
     x.b = b;
     x.prim_mat = prim_mat;
     x.mat_type = mat_type;
     x.mat_color = mat_color;
+    x.mat_param = mat_param;
     x.rd = rd;
     x.cam = make_camera(cam);
     x.acc = rgb;

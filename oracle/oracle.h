@@ -82,8 +82,10 @@ typedef struct {
 } orc_render_desc;
 
 /* materials: mat_type[m] 0 = Diffuse(albedo), 1 = Light(color); mat_color[m*3] */
+/* mat_type 0 Diffuse, 1 Light, 2 Reflective, 3 Refractive; mat_param (may be
+ * NULL) is Reflective.Diffusion or Refractive.Ratio per material. */
 int orc_render(const orc_bvh *b, const int32_t *prim_mat, const int32_t *mat_type, const double *mat_color,
-               const orc_camera_desc *cam, orc_render_desc *rd, double *rgb);
+               const double *mat_param, const orc_camera_desc *cam, orc_render_desc *rd, double *rgb);
 void orc_camera_rays(const orc_camera_desc *cam, int32_t width, int32_t height,
                      const double *su, const double *sv, int64_t n, double *dirs, double origin[3]);
 

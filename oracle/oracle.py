@@ -58,7 +58,7 @@ def lib():
         L.orc_prim_intersect.argtypes = [P, i32, P, P, P, P, P]
         L.orc_traversal_steps.argtypes = [P, P, i64, C.c_int, P]
         L.orc_render.restype = C.c_int
-        L.orc_render.argtypes = [P, P, P, P, P, P, P]
+        L.orc_render.argtypes = [P, P, P, P, P, P, P, P]
         L.orc_adjoint.restype = C.c_int
         L.orc_adjoint.argtypes = [P, P, P, P, P, P, P, P, P]
         L.orc_heatmap.argtypes = [P, P, i32, i32, i32, C.c_int, P, P]
@@ -198,7 +198,9 @@ class BVH:
         pm = np.ascontiguousarray(scene["prim_mat"], np.int32)
         mt = np.ascontiguousarray(scene["mat_type"], np.int32)
         mc = np.ascontiguousarray(scene["mat_color"], np.float64)
-        rc = lib().orc_render(self.h, _p(pm), _p(mt), _p(mc), C.byref(cd), C.byref(r), _p(img))
+        mp = scene.get("mat_param")
+        mp = np.ascontiguousarray(mp if mp is not None else np.zeros(len(mt)), np.float64)
+        rc = lib().orc_render(self.h, _p(pm), _p(mt), _p(mc), _p(mp), C.byref(cd), C.byref(r), _p(img))
         if rc != 0:
             raise RuntimeError("oracle render failed: %d" % rc)
         self.last_rays = int(r.rays_traced)

@@ -57,3 +57,32 @@ def first_mismatch(a, b):
         return "node count %d vs %d" % (len(ka), len(kb))
     m = np.nonzero(pa != pb)[0]
     return "prims differ at %s" % m[:5] if len(m) else "equal"
+
+
+def _quad(c, a, b):
+    c, a, b = (np.asarray(x, np.float64) for x in (c, a, b))
+    p0, p1, p2, p3 = c, c + a, c + a + b, c + b
+    return [np.concatenate([p0, p1, p2]), np.concatenate([p0, p2, p3])]
+
+
+def mirror_scene(albedo=(0.8, 0.6, 0.4), le=5.0):
+    """A Reflective mirror (diffusion 0) at z = -1 facing a camera at the origin; a Light
+    plane at z = +1 behind the camera: every camera ray reflects into the light, so each
+    pixel is albedo * Le exactly (MaxDepth >= 1)."""
+    tris = _quad([-10, -10, -1], [20, 0, 0], [0, 20, 0]) + _quad([-10, -10, 1], [0, 20, 0], [20, 0, 0])
+    return dict(verts=np.asarray(tris, np.float32), spheres=np.zeros((0, 4), np.float32),
+                prim_mat=np.array([0, 0, 1, 1], np.int32), mat_type=np.array([2, 1], np.int32),
+                mat_color=np.array([albedo, [le, le, le]]), mat_param=np.array([0.0, 0.0]),
+                camera=dict(look_from=(0, 0, 0), look_at=(0, 0, -1), up=(0, 1, 0), fov=10.0, aspect=1.0))
+
+
+def clear_glass_scene(albedo=(0.9, 0.8, 0.7), le=5.0):
+    """A Refractive slab of ratio 1 (faces at z = -1 and z = -1.2) in front of a Light plane
+    at z = -3: near-normal rays pass straight through both faces (Schlick reflectance
+    (1 - cos)^5 ~ 0), so each pixel is albedo^2 * Le (MaxDepth >= 2)."""
+    tris = (_quad([-10, -10, -1], [20, 0, 0], [0, 20, 0]) + _quad([-10, -10, -1.2], [0, 20, 0], [20, 0, 0])
+            + _quad([-10, -10, -3], [20, 0, 0], [0, 20, 0]))
+    return dict(verts=np.asarray(tris, np.float32), spheres=np.zeros((0, 4), np.float32),
+                prim_mat=np.array([0, 0, 0, 0, 1, 1], np.int32), mat_type=np.array([3, 1], np.int32),
+                mat_color=np.array([albedo, [le, le, le]]), mat_param=np.array([1.0, 0.0]),
+                camera=dict(look_from=(0, 0, 0), look_at=(0, 0, -1), up=(0, 1, 0), fov=10.0, aspect=1.0))

@@ -108,3 +108,24 @@ def test_execution_options_leave_images_identical(ctx, kind):
         ctx.set_option("traversal", 0)
         ctx.set_option("anyhit_last", 1)
         ctx.set_option("primary_tiles", 1)
+
+
+def test_render_cornell_reflective_refractive(ctx):
+    """Glass UV sphere (Refractive, triangles) and a brushed-metal sphere primitive
+    (Reflective): statistical parity with the oracle's renderer."""
+    # caustics through the glass are noisy: more samples for the converged and high-spp images
+    run(ctx, scenes.cornell_materials(), 96, 96, spp_eq=16, spp_conv=2048, spp_hi=2048)
+
+
+@pytest.mark.parametrize("kind", ["mirror", "glass"])
+def test_render_reflective_and_refractive_exact(ctx, kind):
+    from tests.helpers import clear_glass_scene, mirror_scene
+
+    s = mirror_scene() if kind == "mirror" else clear_glass_scene()
+    g = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s))
+    img, st = g.render(s["camera"], 16, 16, 4, 3)
+    a, le = np.asarray(s["mat_color"][0]), s["mat_color"][1][0]
+    want = a * le if kind == "mirror" else a * a * le
+    np.testing.assert_allclose(img.reshape(-1, 3), np.broadcast_to(want, (256, 3)), rtol=1e-5)
+    # mirror: camera ray + reflected ray; glass: camera ray + two refracted rays
+    assert st["rays_traced"] == 16 * 16 * 4 * (2 if kind == "mirror" else 3)

@@ -262,3 +262,18 @@ def test_heatmap_matches_python_restatement():
         assert counts.ravel().tolist() == want_c
         np.testing.assert_array_equal(rgb.reshape(-1, 3), np.array(want_rgb))
         assert counts.max() > 0
+
+
+@pytest.mark.parametrize("kind", ["mirror", "glass"])
+def test_render_reflective_and_refractive_exact(kind):
+    """Reflective (material.go:44-57) and Refractive (:59-106) in the oracle renderer on
+    scenes whose every path is known: albedo * Le after a mirror, albedo^2 * Le through a
+    ratio-1 slab."""
+    from tests.helpers import clear_glass_scene, mirror_scene
+
+    s = mirror_scene() if kind == "mirror" else clear_glass_scene()
+    s["render"] = dict(width=16, height=16, spp=4, max_depth=3, miss_mode=0, miss_color=(0.0, 0.0, 0.0))
+    img = O.lbvh(s["verts"]).render(s)
+    a, le = np.asarray(s["mat_color"][0]), s["mat_color"][1][0]
+    want = a * le if kind == "mirror" else a * a * le
+    np.testing.assert_allclose(img.reshape(-1, 3), np.broadcast_to(want, (256, 3)), rtol=1e-9)

@@ -36,7 +36,7 @@ class Sphere(C.Structure):
 
 
 class Material(C.Structure):
-    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3)]
+    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("param", C.c_float)]
 
 
 class Camera(C.Structure):

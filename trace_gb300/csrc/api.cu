@@ -197,14 +197,18 @@ extern "C" int gbt_scene_upload(gbt_ctx *ctx, const float *verts, const float *n
     }
     std::vector<gbt_material> mv;
     if (mats && n_mat) mv.assign(mats, mats + n_mat);
-    else mv.push_back(gbt_material{GBT_MAT_DIFFUSE, {0.5f, 0.5f, 0.5f}});
-    std::vector<float4> mf(mv.size());
+    else mv.push_back(gbt_material{GBT_MAT_DIFFUSE, {0.5f, 0.5f, 0.5f}, 0.f});
+    // two float4 per material: (color.rgb, type), (param, 0, 0, 0)
+    std::vector<float4> mf(2 * mv.size());
     for (size_t i = 0; i < mv.size(); i++) {
-        if (mv[i].type != GBT_MAT_DIFFUSE && mv[i].type != GBT_MAT_LIGHT)
-            return gbt_fail(ctx, GBT_EUNSUPPORTED, "scene_upload: only Diffuse and Light materials run on the device");
+        if (mv[i].type < GBT_MAT_DIFFUSE || mv[i].type > GBT_MAT_REFRACTIVE)
+            return gbt_fail(ctx, GBT_EINVAL, "scene_upload: unknown material type " + std::to_string(mv[i].type));
+        if (mv[i].type == GBT_MAT_REFRACTIVE && !(mv[i].param > 0.f))
+            return gbt_fail(ctx, GBT_EINVAL, "scene_upload: Refractive.Ratio must be > 0");
         float tf;
         std::memcpy(&tf, &mv[i].type, sizeof(tf));
-        mf[i] = make_float4(mv[i].color[0], mv[i].color[1], mv[i].color[2], tf);
+        mf[2 * i] = make_float4(mv[i].color[0], mv[i].color[1], mv[i].color[2], tf);
+        mf[2 * i + 1] = make_float4(mv[i].param, 0.f, 0.f, 0.f);
     }
     gbt_scene *s = new gbt_scene();
     s->ctx = ctx;

@@ -66,7 +66,7 @@ struct gbt_scene {
     float *d_normals = nullptr;    // n_tri*9 or null
     float4 *d_sph = nullptr;       // n_sph (center, radius)
     uint32_t *d_prim_mat = nullptr;
-    float4 *d_mats = nullptr;      // (color.rgb, type)
+    float4 *d_mats = nullptr;      // 2 per material: (color.rgb, type), (param, 0, 0, 0)
     std::vector<gbt_material> mats;
 };
 

@@ -29,7 +29,7 @@ import numpy as np
 from . import _lib
 from ._lib import GbtError
 
-DIFFUSE, LIGHT = 0, 1
+DIFFUSE, LIGHT, REFLECTIVE, REFRACTIVE = 0, 1, 2, 3
 MISS_BLACK, MISS_WHITE, MISS_SKY, MISS_CONSTANT = 0, 1, 2, 3
 
 
@@ -112,7 +112,8 @@ class Context:
 class DeviceScene:
     """Flattened primitives resident on the device (gbt_scene)."""
 
-    def __init__(self, ctx, verts, normals=None, spheres=None, prim_mat=None, mat_type=None, mat_color=None):
+    def __init__(self, ctx, verts, normals=None, spheres=None, prim_mat=None, mat_type=None, mat_color=None,
+                 mat_param=None):
         self.ctx = ctx
         self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 9)
         self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
@@ -123,9 +124,11 @@ class DeviceScene:
         mt = np.array([DIFFUSE], np.int32) if mat_type is None else np.asarray(mat_type, np.int32)
         mc = np.array([[0.5, 0.5, 0.5]]) if mat_color is None else np.asarray(mat_color, np.float64).reshape(-1, 3)
         mats = (_lib.Material * len(mt))()
+        mp = np.zeros(len(mt)) if mat_param is None else np.asarray(mat_param, np.float64).reshape(-1)
         for i in range(len(mt)):
             mats[i].type = int(mt[i])
             mats[i].color[:] = [float(x) for x in mc[i]]
+            mats[i].param = float(mp[i])
         sarr = (_lib.Sphere * max(1, sph.shape[0]))()
         for i in range(sph.shape[0]):
             sarr[i].center[:] = [float(x) for x in sph[i, :3]]
@@ -141,7 +144,7 @@ class DeviceScene:
     @classmethod
     def from_dict(cls, ctx, s):
         return cls(ctx, s["verts"], s.get("normals"), s.get("spheres"), s.get("prim_mat"), s.get("mat_type"),
-                   s.get("mat_color"))
+                   s.get("mat_color"), s.get("mat_param"))
 
     def close(self):
         if getattr(self, "h", None):

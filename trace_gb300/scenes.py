@@ -27,7 +27,7 @@ from __future__ import annotations
 
 import numpy as np
 
-DIFFUSE, LIGHT = 0, 1
+DIFFUSE, LIGHT, REFLECTIVE, REFRACTIVE = 0, 1, 2, 3
 MISS_BLACK, MISS_WHITE, MISS_SKY, MISS_CONSTANT = 0, 1, 2, 3
 
 
@@ -93,6 +93,26 @@ def cornell(sphere_u=32, sphere_v=16, width=256, height=256, spp=16, max_depth=5
         render=dict(width=width, height=height, spp=spp, max_depth=max_depth,
                     miss_mode=MISS_BLACK, miss_color=(0.0, 0.0, 0.0)),
     )
+
+
+def cornell_materials(width=256, height=256, spp=16, max_depth=5):
+    """The Cornell box with a glass UV sphere (Refractive, ratio 1.5) and a small
+    brushed-metal analytic sphere (Reflective, diffusion 0.15): the materials of
+    material.go:44-106 on triangles and on a sphere primitive."""
+    s = cornell(width=width, height=height, spp=spp, max_depth=max_depth)
+    n = s["verts"].shape[0]
+    pm = s["prim_mat"].copy()
+    pm[n - len(list(uv_sphere([0.0, 0.3, 0.0], 0.3, 32, 16))):] = 4  # the UV sphere's triangles (added last)
+    s.update(
+        name="cornell_materials",
+        spheres=np.array([[-0.28, 0.14, 0.22, 0.14]], np.float32),
+        prim_mat=np.concatenate([pm, np.array([5], np.int32)]),
+        mat_type=np.array([DIFFUSE, DIFFUSE, DIFFUSE, LIGHT, REFRACTIVE, REFLECTIVE], np.int32),
+        mat_color=np.array([[0.7, 0.7, 0.7], [0.7, 0.1, 0.1], [0.1, 0.7, 0.1], [10.0, 10.0, 10.0],
+                            [0.95, 0.95, 0.95], [0.8, 0.8, 0.8]]),
+        mat_param=np.array([0.0, 0.0, 0.0, 0.0, 1.5, 0.15]),
+    )
+    return s
 
 
 def soup(n=1_000_000, seed=1, width=1920, height=1080, spp=1, max_depth=0):
