@@ -54,7 +54,8 @@ f 7/1/6 1/1/6 3/1/6 5/1/6
 def test_obj_parse_fan_triangulation_and_negative_indices(tmp_path):
     p = tmp_path / "cube.obj"
     p.write_text(CUBE)
-    verts, normals = pt.ParseFromPath(p)
+    g = pt.ParseFromPath(p)
+    verts, normals = g.verts, (g.normals if g.has_normals else None)
     assert verts.shape == (12, 9)  # 6 quads, fan-triangulated (obj.go:193-203)
     assert normals is not None
     # first face: (v1, v2, v4), (v1, v4, v3)
@@ -71,7 +72,8 @@ def test_obj_parse_fan_triangulation_and_negative_indices(tmp_path):
 def test_obj_parse_without_normals_and_errors(tmp_path):
     p = tmp_path / "tri.obj"
     p.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
-    verts, normals = pt.ParseFromPath(p)
+    g = pt.ParseFromPath(p)
+    verts, normals = g.verts, (g.normals if g.has_normals else None)
     assert verts.shape == (1, 9) and normals is None
     bad = tmp_path / "bad.obj"
     bad.write_text("v 0 0 x\n")

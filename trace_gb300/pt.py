@@ -6,8 +6,11 @@ entry points:
   Go (pkg/pt)                                   here
   ------------------------------------------    -----------------------------------------
   ParseFromPath (obj.go:10-17)                  ParseFromPath(path) -> Geometry
+  NewScene / NewSceneNode / NewMesh (scene.go)  the same names; node transforms of transformation.go
   Scene.CompileLBVH (scene.go:27-30)            Scene.CompileLBVH(ctx) / DefaultLBVH(scene)
   Scene.Compile / CompilePHR (scene.go:21-36)   Scene.Compile(ctx) / Scene.CompilePHR(ctx, a, d, bf)
+  HeatMapRenderer (render.go:137-197)           NewHeatMapRenderer(bvh, camera, threshold)
+  gridOptimizer (optimizer.go:19-94)            NewGridOptimizer(...).OptimizedPHRparams(aux, bf)
   NewPHRBuilder + BuildFromAuxilary (phr.go)    NewPHRBuilder(alpha, delta, bf).BuildFromAuxilary(aux)
   BVH.Cost / BVH.Size (bvh.go:46-52)            BVH.Cost() / BVH.Size()
   NewCamera (camera.go:53-59)                   NewCamera(aspect, fov, CameraTransformation)
@@ -28,6 +31,10 @@ import numpy as np
 
 from . import _lib
 from ._lib import GbtError
+from .scenegraph import (Diffuse, Geometry, IdentityMatrix, Light, Mesh, NewColor, NewMesh,  # noqa: F401
+                         NewSceneNode, NewSphere, NewTriangle, NewTriangleWithoutNormals, NewVector3, Reflective,
+                         Refractive, Rotate, Scale, ScaleUniform, SceneNode, Translate)
+from .scenegraph import flatten as _flatten
 
 DIFFUSE, LIGHT, REFLECTIVE, REFRACTIVE = 0, 1, 2, 3
 MISS_BLACK, MISS_WHITE, MISS_SKY, MISS_CONSTANT = 0, 1, 2, 3
@@ -578,7 +585,9 @@ def NewHeatMapRenderer(bvh, camera, threshold):
 
 
 def ParseFromPath(path):
-    """pkg/pt/obj.go:10-17 -> (verts (n,9) float32, normals (n,9) float32 or None)."""
+    """pkg/pt/obj.go:10-17 -> Geometry: triangles (n, 9) with per-vertex normals (n, 9); faces
+    without normal indices get calcNormal normals (obj.go:93-110).  has_normals tells whether
+    the file gave any."""
     L = _lib.load()
     n = C.c_uint32(0)
     hn = C.c_int32(0)
@@ -590,4 +599,41 @@ def ParseFromPath(path):
     rc = L.gbt_obj_parse(str(path).encode(), _p(verts), _p(normals), C.byref(n), C.byref(hn))
     if rc != 0:
         raise GbtError(rc, "ParseFromPath(%s)" % path)
-    return verts, (normals if hn.value else None)
+    g = Geometry(verts.astype(np.float64), normals.astype(np.float64), np.zeros((0, 4)))
+    g.has_normals = bool(hn.value)
+    return g
+
+
+class Scene:
+    """pkg/pt/scene.go:7-36: a scene graph compiled into a device scene and a BVH."""
+
+    def __init__(self):
+        self.root = NewSceneNode(None)
+
+    def Add(self, node):
+        self.root.Add(node)
+
+    def tracables(self):
+        """collectTracables from the identity (scene.go:21-36), flattened for upload."""
+        return _flatten(self.root.collect(IdentityMatrix(), []))
+
+    def UntransformedTracables(self):
+        return _flatten(self.root.collect_raw([]))
+
+    def upload(self, ctx):
+        d = self.tracables()
+        return DeviceScene(ctx, d["verts"], d["normals"] if d["verts"].shape[0] else None, d["spheres"],
+                           d["prim_mat"], d["mat_type"], d["mat_color"], d["mat_param"])
+
+    def Compile(self, ctx):
+        return NewDefaultBuilder().Build(self.upload(ctx))
+
+    def CompileLBVH(self, ctx):
+        return DefaultLBVH(self.upload(ctx))
+
+    def CompilePHR(self, ctx, alpha, delta, branchingFactor):
+        return NewPHRBuilder(alpha, delta, branchingFactor).Build(self.upload(ctx))
+
+
+def NewScene():
+    return Scene()
