@@ -62,6 +62,14 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def replica_throughput(dist, rays, ms):
+    """Whole-job Mrays/s of N independent replicas: rays summed over ranks divided by the
+    slowest rank's device time.  Returns (Mrays/s, max ms, total rays)."""
+    ms_max = dist.reduce(ms, "max")
+    rays_all = dist.reduce(rays, "sum")
+    return rays_all / ms_max / 1e3, ms_max, rays_all
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -578,9 +586,7 @@ def main():
     ctx.check(L.gbt_render_last_stats(h, C.byref(st)))
     timed = st.as_dict()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    ms_max = dist.reduce(ms, "max")
-    rays_all = dist.reduce(timed["rays_traced"], "sum")
-    value = rays_all / ms_max / 1e3  # Mrays/s
+    value, ms_max, rays_all = replica_throughput(dist, timed["rays_traced"], ms)  # Mrays/s
     # roofline of the traversal kernels
     hbm, peak_kind = peaks()
     rays_per_frame = count_stats["rays_traced"]
