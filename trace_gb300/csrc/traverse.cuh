@@ -93,6 +93,9 @@ __device__ __forceinline__ void test_record(const float4 *__restrict__ recs, int
         if (v < 0.f || u + v > 1.f) return;
         float t = dot3(e2, qv) * inv;
         if (t < r.tmin || t > h.t) return;
+        // an exact tie with the current hit goes to the lower record, whatever the visiting order
+        // (the reference keeps the last one its own order finds)
+        if (t == h.t && h.rec >= 0 && s > h.rec) return;
         h.t = t;
         h.u = u;
         h.v = v;
