@@ -411,7 +411,13 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
         uint32_t d = ok ? (uint32_t)((k[i] >> shift) & 255u) : 256u;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        // lanes with the same digit, from one vote per digit bit (valid lanes only)
+        uint32_t peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const uint32_t vb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? vb : ~vb;
+        }
         uint32_t base = ok ? wh[d] : 0u;
         __syncwarp();
         if (ok && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = base + __popc(peers);
