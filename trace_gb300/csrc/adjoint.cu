@@ -30,17 +30,30 @@ namespace {
 
 constexpr int MAXV = 16;  // path vertices kept for replay (max_depth <= 14)
 
+constexpr int SH = 12;  // traversal stack entries per thread kept in shared memory (4-wide trees)
+using Stack4 = SharedTopStack<96, SH>;
+
 template <int W>
 __device__ __forceinline__ Hit closest(const BvhHeader &hdr, const float4 *nodes, const float4 *recs, float3 o,
-                                       float3 d, float tmin, unsigned int *err) {
+                                       float3 d, float tmin, unsigned int *err, Stack4 &st) {
     Ray r;
     r.o = o;
     r.d = d;
     r.tmin = tmin;
     r.tmax = __int_as_float(0x7f800000);
     finish_ray(r);
-    return W == 2 ? closest_hit2<64>(hdr, nodes, recs, r, err) : closest_hit4<96>(hdr, nodes, recs, r, err);
+    if constexpr (W == 2) return closest_hit2<64>(hdr, nodes, recs, r, err);
+    else return closest_hit4_with<false>(hdr, nodes, recs, r, err, nullptr, st);
 }
+
+// the per-thread shared-memory bottom of the traversal stack (blocks of 128 threads)
+#define ADJ_STACK(st)                          \
+    __shared__ int2 s_se_[SH * 128];           \
+    __shared__ float s_st_[SH * 128];          \
+    Stack4 st;                                 \
+    st.se = s_se_ + threadIdx.x;               \
+    st.st = s_st_ + threadIdx.x;               \
+    st.stride = 128
 
 struct Vertex {
     int tri;
@@ -54,7 +67,8 @@ template <int W>
 __device__ __forceinline__ int trace_path(const BvhHeader &hdr, const float4 *nodes, const float4 *recs,
                                           const float *normals, const CamF &cam, const ShadeParams &sp,
                                           const float *__restrict__ albedo, const float *__restrict__ emission,
-                                          uint32_t g, Vertex *vx, float3 &L, float3 &miss, unsigned int *err) {
+                                          uint32_t g, Vertex *vx, float3 &L, float3 &miss, unsigned int *err,
+                                          Stack4 &st) {
     float3 o, d;
     primary_ray(cam, sp, g, o, d);
     float tmin = 0.001f;
@@ -63,7 +77,7 @@ __device__ __forceinline__ int trace_path(const BvhHeader &hdr, const float4 *no
     miss = f3(0.f, 0.f, 0.f);
     int nv = 0;
     for (int level = 0;; level++) {
-        Hit h = closest<W>(hdr, nodes, recs, o, d, tmin, err);
+        Hit h = closest<W>(hdr, nodes, recs, o, d, tmin, err, st);
         if (h.rec < 0) {
             miss = miss_colour(sp, d);
             L = add3(L, emul3(T, miss));
@@ -97,12 +111,13 @@ __global__ void __launch_bounds__(128) k_adj_forward(const BvhHeader *__restrict
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const BvhHeader H = *hdr;
     unsigned long long nr = 0;
+    ADJ_STACK(st);
     if (pix < sp.npix) {
         double s0 = 0, s1 = 0, s2 = 0;
         Vertex vx[MAXV];
         for (uint32_t s = 0; s < sp.spp; s++) {
             float3 L, m;
-            int nv = trace_path<W>(H, nodes, recs, normals, cam, sp, albedo, emission, s * sp.npix + pix, vx, L, m, err);
+            int nv = trace_path<W>(H, nodes, recs, normals, cam, sp, albedo, emission, s * sp.npix + pix, vx, L, m, err, st);
             nr += (unsigned long long)nv + 1;
             s0 += L.x;
             s1 += L.y;
@@ -147,6 +162,7 @@ __global__ void __launch_bounds__(128) k_adj_backward(const BvhHeader *__restric
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = pix < sp.npix;
     const BvhHeader H = *hdr;
+    ADJ_STACK(st);
     const float inv = 1.f / (float)sp.spp;
     float3 delta = f3(0.f, 0.f, 0.f);
     if (live) delta = f3(dimg[3 * (size_t)pix] * inv, dimg[3 * (size_t)pix + 1] * inv, dimg[3 * (size_t)pix + 2] * inv);
@@ -157,7 +173,7 @@ __global__ void __launch_bounds__(128) k_adj_backward(const BvhHeader *__restric
         int nv = 0;
         if (live) {
             float3 L, m;
-            nv = trace_path<W>(H, nodes, recs, normals, cam, sp, albedo, emission, s * sp.npix + pix, vx, L, m, err);
+            nv = trace_path<W>(H, nodes, recs, normals, cam, sp, albedo, emission, s * sp.npix + pix, vx, L, m, err, st);
             // S_i: radiance beyond vertex i per unit throughput leaving it; S_{K-1} = M
             float3 acc = m;
             for (int i = nv - 1; i >= 0; i--) {

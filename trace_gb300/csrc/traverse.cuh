@@ -199,79 +199,6 @@ __device__ __forceinline__ Hit closest_hit2(const BvhHeader &hdr, const float4 *
     return h;
 }
 
-template <int STACK, bool COUNT = false>
-__device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *__restrict__ nodes,
-                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
-                                            Work *work = nullptr) {
-    Hit h;
-    h.t = r.tmax;
-    h.u = h.v = 0.f;
-    h.rec = -1;
-    float te;
-    if (!slab(hdr.root_lo[0], hdr.root_lo[1], hdr.root_lo[2], hdr.root_hi[0], hdr.root_hi[1], hdr.root_hi[2], r, h.t, te))
-        return h;
-    int2 stack[STACK];
-    float stack_t[STACK];
-    int sp = 0;
-    int2 cur = make_int2(hdr.root_ref, hdr.root_cnt);
-    for (;;) {
-        if (cur.y == 0) {
-            if (COUNT) work->nodes++;
-            const float4 *nd = nodes + 8 * (size_t)cur.x;
-            float4 lx, hx, ly, hy, lz, hz, rff, cnf;
-            ldg256(nd, lx, hx);
-            ldg256(nd + 2, ly, hy);
-            ldg256(nd + 4, lz, hz);
-            ldg256(nd + 6, rff, cnf);
-            const int4 rf = make_int4(__float_as_int(rff.x), __float_as_int(rff.y), __float_as_int(rff.z),
-                                      __float_as_int(rff.w));
-            const int4 cn = make_int4(__float_as_int(cnf.x), __float_as_int(cnf.y), __float_as_int(cnf.z),
-                                      __float_as_int(cnf.w));
-            float tc[4];
-            int2 ch[4];
-            int k = 0;
-            float t;
-            if (cn.x >= 0 && slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.x, cn.x); }
-            if (cn.y >= 0 && slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.y, cn.y); }
-            if (cn.z >= 0 && slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.z, cn.z); }
-            if (cn.w >= 0 && slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) { tc[k] = t; ch[k++] = make_int2(rf.w, cn.w); }
-            if (k > 0) {
-                // order by entry distance, far first onto the stack
-                for (int a = 1; a < k; ++a)
-                    for (int b = a; b > 0 && tc[b] > tc[b - 1]; --b) {
-                        float tt = tc[b]; tc[b] = tc[b - 1]; tc[b - 1] = tt;
-                        int2 cc = ch[b]; ch[b] = ch[b - 1]; ch[b - 1] = cc;
-                    }
-                for (int a = 0; a < k - 1; ++a) {
-                    if (sp < STACK) {
-                        stack[sp] = ch[a];
-                        stack_t[sp] = tc[a];
-                        ++sp;
-                    } else {
-                        atomicOr(err, GBT_DEVERR_STACK);
-                    }
-                }
-                cur = ch[k - 1];
-                continue;
-            }
-        } else if (cur.y > 0) {
-            if (COUNT) work->prims += (uint32_t)cur.y;
-            leaf(recs, cur.x, cur.y, r, h);
-        }
-        bool found = false;
-        while (sp > 0) {
-            --sp;
-            if (stack_t[sp] <= h.t * 1.0000005f) {
-                cur = stack[sp];
-                found = true;
-                break;
-            }
-        }
-        if (!found) break;
-    }
-    return h;
-}
-
 // ---------------------------------------------------------------------------
 // Persistent traversal: each warp keeps its lanes busy by fetching new rays as
 // old ones finish, and runs inner-node steps until every busy lane holds a leaf
@@ -411,6 +338,44 @@ __device__ __forceinline__ int2 step4(const float4 *__restrict__ nodes, int2 nod
     if (c2.t != MISS) st.push(sp, c2.e, c2.t, err);
     if (c1.t != MISS) st.push(sp, c1.e, c1.t, err);
     return c0.e;
+}
+
+// One ray through a 4-wide tree: the sorting-network step with the given stack.
+template <bool COUNT, class StackT>
+__device__ __forceinline__ Hit closest_hit4_with(const BvhHeader &hdr, const float4 *__restrict__ nodes,
+                                                 const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
+                                                 Work *work, StackT &st) {
+    Hit h;
+    h.t = r.tmax;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    float te;
+    if (!slab(hdr.root_lo[0], hdr.root_lo[1], hdr.root_lo[2], hdr.root_hi[0], hdr.root_hi[1], hdr.root_hi[2], r, h.t, te))
+        return h;
+    int sp = 0;
+    int2 node = make_int2(hdr.root_ref, hdr.root_cnt);
+    for (;;) {
+        if (node.y == 0) {
+            if (COUNT) work->nodes++;
+            node = step4(nodes, node, st, sp, r, h.t, err);
+        } else if (node.y > 0) {
+            if (COUNT) work->prims += (uint32_t)node.y;
+            leaf(recs, node.x, node.y, r, h);
+            node = st.pop(sp, h.t);
+        } else {
+            break;
+        }
+    }
+    return h;
+}
+
+// ... with a local-memory stack
+template <int STACK, bool COUNT = false>
+__device__ __forceinline__ Hit closest_hit4(const BvhHeader &hdr, const float4 *__restrict__ nodes,
+                                            const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
+                                            Work *work = nullptr) {
+    LocalStack<STACK> st;
+    return closest_hit4_with<COUNT>(hdr, nodes, recs, r, err, work, st);
 }
 
 // out_mode 0: gbt_hit (primitive id, t, u, v); 1: (t, u, v, record) for the renderer
