@@ -24,6 +24,12 @@
 #include "gbt_internal.cuh"
 #include "shade.cuh"
 
+#define GBT_TRY_ADJ(x)       \
+    do {                     \
+        int rc_ = (x);       \
+        if (rc_) return rc_; \
+    } while (0)
+
 using namespace gbt_dev;
 
 namespace {
@@ -106,16 +112,18 @@ template <int W>
 __global__ void __launch_bounds__(128) k_adj_forward(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                      const float4 *__restrict__ recs, const float *__restrict__ normals,
                                                      CamF cam, ShadeParams sp, const float *__restrict__ albedo,
-                                                     const float *__restrict__ emission, float *__restrict__ img,
+                                                     const float *__restrict__ emission, double *__restrict__ part,
                                                      unsigned int *err, unsigned long long *rays) {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t c = blockIdx.y, nc = gridDim.y;  // this thread's chunk of the pixel's samples
+    const uint32_t s_lo = (uint32_t)((uint64_t)sp.spp * c / nc), s_hi = (uint32_t)((uint64_t)sp.spp * (c + 1) / nc);
     const BvhHeader H = *hdr;
     unsigned long long nr = 0;
     ADJ_STACK(st);
     if (pix < sp.npix) {
         double s0 = 0, s1 = 0, s2 = 0;
         Vertex vx[MAXV];
-        for (uint32_t s = 0; s < sp.spp; s++) {
+        for (uint32_t s = s_lo; s < s_hi; s++) {
             float3 L, m;
             int nv = trace_path<W>(H, nodes, recs, normals, cam, sp, albedo, emission, s * sp.npix + pix, vx, L, m, err, st);
             nr += (unsigned long long)nv + 1;
@@ -123,9 +131,10 @@ __global__ void __launch_bounds__(128) k_adj_forward(const BvhHeader *__restrict
             s1 += L.y;
             s2 += L.z;
         }
-        img[3 * (size_t)pix] = (float)(s0 / sp.spp);
-        img[3 * (size_t)pix + 1] = (float)(s1 / sp.spp);
-        img[3 * (size_t)pix + 2] = (float)(s2 / sp.spp);
+        double *o = part + 3 * ((size_t)c * sp.npix + pix);
+        o[0] = s0;
+        o[1] = s1;
+        o[2] = s2;
     }
     __syncwarp();
 #pragma unroll
@@ -133,20 +142,38 @@ __global__ void __launch_bounds__(128) k_adj_forward(const BvhHeader *__restrict
     if ((threadIdx.x & 31) == 0) atomicAdd(rays, nr);
 }
 
-// Sum four floats over the lanes of `peers`, result valid in every lane of the group.
+// The pixel's chunk sums in chunk order, divided by spp (a fixed order: the
+// image is bitwise reproducible).
+__global__ void k_adj_combine(const double *__restrict__ part, uint32_t npix, uint32_t nc, uint32_t spp,
+                              float *__restrict__ img) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * npix) return;
+    double acc = 0.0;
+    for (uint32_t c = 0; c < nc; c++) acc += part[(size_t)c * 3 * npix + i];
+    img[i] = (float)(acc / spp);
+}
+
+// Sum four floats over the lanes of `peers` (own value first, then the other
+// peers in lane order); valid in every lane of the group.  The loop runs the
+// largest group's size - 1 times: not at all when every lane's triangle differs.
 __device__ __forceinline__ float4 group_sum(uint32_t peers, float4 v) {
-    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int src = 0; src < 32; src++) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t m = peers & ~(1u << lane);
+    float4 s = v;
+    const int iters = (int)__reduce_max_sync(0xffffffffu, (uint32_t)__popc(peers)) - 1;
+    for (int it = 0; it < iters; it++) {
+        const int src = m ? __ffs(m) - 1 : (int)lane;
         float4 x;
         x.x = __shfl_sync(0xffffffffu, v.x, src);
         x.y = __shfl_sync(0xffffffffu, v.y, src);
         x.z = __shfl_sync(0xffffffffu, v.z, src);
         x.w = __shfl_sync(0xffffffffu, v.w, src);
-        if ((peers >> src) & 1u) {
+        if (m) {
             s.x += x.x;
             s.y += x.y;
             s.z += x.z;
             s.w += x.w;
+            m &= m - 1;
         }
     }
     return s;
@@ -167,9 +194,11 @@ __global__ void __launch_bounds__(128) k_adj_backward(const BvhHeader *__restric
     float3 delta = f3(0.f, 0.f, 0.f);
     if (live) delta = f3(dimg[3 * (size_t)pix] * inv, dimg[3 * (size_t)pix + 1] * inv, dimg[3 * (size_t)pix + 2] * inv);
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t c = blockIdx.y, nc = gridDim.y;  // this thread's chunk of the pixel's samples
+    const uint32_t s_lo = (uint32_t)((uint64_t)sp.spp * c / nc), s_hi = (uint32_t)((uint64_t)sp.spp * (c + 1) / nc);
     Vertex vx[MAXV];
     float3 S[MAXV];
-    for (uint32_t s = 0; s < sp.spp; s++) {  // warp-uniform loop
+    for (uint32_t s = s_lo; s < s_hi; s++) {  // warp-uniform loop
         int nv = 0;
         if (live) {
             float3 L, m;
@@ -235,6 +264,20 @@ int check(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_render_params *p) {
     return GBT_OK;
 }
 
+// Sample chunks per pixel: enough 128-thread blocks for about eight waves of
+// the resident blocks, so the last wave's idle SMs cost little.
+template <class K>
+uint32_t sample_chunks(gbt_ctx *ctx, K kernel, uint32_t npix, uint32_t spp) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    if (per_sm <= 0) per_sm = 1;
+    const uint64_t want = 8ull * (uint64_t)ctx->num_sms * per_sm, have = (npix + 127) / 128;
+    uint64_t c = (want + have - 1) / have;
+    if (c > spp) c = spp;
+    if (c > 64) c = 64;
+    return (uint32_t)(c < 1 ? 1 : c);
+}
+
 }  // namespace
 
 extern "C" int gbt_adjoint_forward_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
@@ -248,14 +291,21 @@ extern "C" int gbt_adjoint_forward_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_c
     const bool four = bvh->has_nodes4 || bvh->arity == 4;
     const BvhHeader *hd = bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr;
     const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
+    const uint32_t nc = four ? sample_chunks(ctx, k_adj_forward<4>, sp.npix, sp.spp)
+                             : sample_chunks(ctx, k_adj_forward<2>, sp.npix, sp.spp);
+    void *scr = nullptr;
+    GBT_TRY_ADJ(gbt_scratch(ctx, (size_t)nc * sp.npix * 3 * sizeof(double), &scr));
+    double *part = static_cast<double *>(scr);
+    const dim3 grid(blocks, nc);
     if (four)
-        k_adj_forward<4><<<blocks, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
-                                                          d_emission, d_img, ctx->d_error, ctx->d_counters + 2);
+        k_adj_forward<4><<<grid, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
+                                                        d_emission, part, ctx->d_error, ctx->d_counters + 2);
     else
-        k_adj_forward<2><<<blocks, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
-                                                          d_emission, d_img, ctx->d_error, ctx->d_counters + 2);
+        k_adj_forward<2><<<grid, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
+                                                        d_emission, part, ctx->d_error, ctx->d_counters + 2);
+    k_adj_combine<<<(3 * sp.npix + 255) / 256, 256, 0, ctx->stream>>>(part, sp.npix, nc, sp.spp, d_img);
     GBT_CUDA(ctx, cudaGetLastError());
-    ctx->last_stats.kernel_launches += 1;
+    ctx->last_stats.kernel_launches += 2;
     ctx->last_stats.paths += (uint64_t)sp.npix * sp.spp;
     return GBT_OK;
 }
@@ -276,12 +326,15 @@ extern "C" int gbt_adjoint_backward_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_
     const bool four = bvh->has_nodes4 || bvh->arity == 4;
     const BvhHeader *hd = bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr;
     const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
+    const uint32_t nc = four ? sample_chunks(ctx, k_adj_backward<4>, sp.npix, sp.spp)
+                             : sample_chunks(ctx, k_adj_backward<2>, sp.npix, sp.spp);
+    const dim3 grid(blocks, nc);
     if (four)
-        k_adj_backward<4><<<blocks, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
-                                                           d_emission, d_dimg, d_galbedo, d_gemission, ctx->d_error);
+        k_adj_backward<4><<<grid, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
+                                                         d_emission, d_dimg, d_galbedo, d_gemission, ctx->d_error);
     else
-        k_adj_backward<2><<<blocks, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
-                                                           d_emission, d_dimg, d_galbedo, d_gemission, ctx->d_error);
+        k_adj_backward<2><<<grid, 128, 0, ctx->stream>>>(hd, nd, bvh->d_prims, bvh->scene->d_normals, cf, sp, d_albedo,
+                                                         d_emission, d_dimg, d_galbedo, d_gemission, ctx->d_error);
     GBT_CUDA(ctx, cudaGetLastError());
     ctx->last_stats.kernel_launches += 1;
     return GBT_OK;
