@@ -80,6 +80,10 @@ __device__ __forceinline__ uint32_t lane_lt() {
 }
 
 // Resident blocks per SM the register budget is sized for (64 registers a thread at 8).
+// A warp refills its idle lanes with new rays once fewer than this many are busy.
+#ifndef GBT_PT_DYN
+#define GBT_PT_DYN 16
+#endif
 #ifndef GBT_PT_MINB
 #define GBT_PT_MINB 8
 #endif
@@ -233,10 +237,10 @@ void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, u
         const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
         const bool dyn = ctx->traversal == 0;
         if (four) {
-            if (dyn) launch_pt_any<4, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            if (dyn) launch_pt_any<4, GBT_PT_DYN>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
             else launch_pt_any<4, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
         } else {
-            if (dyn) launch_pt_any<2, 16>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            if (dyn) launch_pt_any<2, GBT_PT_DYN>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
             else launch_pt_any<2, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
         }
         return;
