@@ -603,7 +603,8 @@ def main():
             "traversal_ms_per_frame": trav_ms_frame, "traversal_share": timed["ms_traverse"] / ms,
             "nodes_per_ray": count_stats["nodes_visited"] / rays_per_frame,
             "prims_per_ray": count_stats["prims_tested"] / rays_per_frame,
-            "note": "bytes counted at the node/record level; most are L1/L2 hits, so frac can exceed 1"}
+            "note": "bytes counted at the node/record level; most are L1/L2 hits, so frac can exceed 1; "
+                    "camera rays run as 32-ray packets whose node and record fetches count once per warp"}
     ctx.check(L.gbt_ctx_set_profiling(h, 0))
 
     # e2e: the C-ABI call with a pinned host image, device->host copy inside the timed region

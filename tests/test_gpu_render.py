@@ -80,7 +80,7 @@ def test_render_emitter_exact(ctx):
 
 @pytest.mark.parametrize("kind", ["cornell", "soup"])
 def test_execution_options_leave_images_identical(ctx, kind):
-    """Any-hit past MaxDepth, tiled camera rays and the traversal kernel change the
+    """Any-hit past MaxDepth, tiled camera rays, packet tracing and the traversal kernel change the
     order of work only: with spp 2 (two deposits per pixel add commutatively) the
     images and ray counts are bitwise equal under every setting.  The frame size is
     no multiple of the 8x4 tile, so the right and bottom strips are covered too."""
@@ -93,21 +93,23 @@ def test_execution_options_leave_images_identical(ctx, kind):
     try:
         for trav in (0, 1, 2):
             for anyhit in (0, 1):
-                for tiles in (0, 1):
+                for tiles, packets in ((0, 0), (1, 0), (1, 1)):
                     ctx.set_option("traversal", trav)
                     ctx.set_option("anyhit_last", anyhit)
                     ctx.set_option("primary_tiles", tiles)
+                    ctx.set_option("primary_packets", packets)
                     img, st = g.render(cam, w, h, spp, md, rd["miss_mode"], rd["miss_color"], seed=5)
                     if ref is None:
                         ref = (img, st["rays_traced"])
                         assert img.mean() > 0
                     else:
-                        assert st["rays_traced"] == ref[1], (trav, anyhit, tiles)
-                        assert np.array_equal(img, ref[0]), (trav, anyhit, tiles, np.abs(img - ref[0]).max())
+                        assert st["rays_traced"] == ref[1], (trav, anyhit, tiles, packets)
+                        assert np.array_equal(img, ref[0]), (trav, anyhit, tiles, packets, np.abs(img - ref[0]).max())
     finally:
         ctx.set_option("traversal", 0)
         ctx.set_option("anyhit_last", 1)
         ctx.set_option("primary_tiles", 1)
+        ctx.set_option("primary_packets", 1)
 
 
 def test_render_cornell_reflective_refractive(ctx):

@@ -106,6 +106,7 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
         c->traversal = std::strcmp(t, "simple") == 0 ? 1 : std::strcmp(t, "ww") == 0 ? 2 : 0;
     if (const char *t = std::getenv("GBT_ANYHIT_LAST")) c->anyhit_last = std::strcmp(t, "0") != 0;
     if (const char *t = std::getenv("GBT_PRIMARY_TILES")) c->primary_tiles = std::strcmp(t, "0") != 0;
+    if (const char *t = std::getenv("GBT_PRIMARY_PACKETS")) c->primary_packets = std::strcmp(t, "0") != 0;
     *out = c;
     return GBT_OK;
 }
@@ -151,8 +152,10 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
         return GBT_OK;
     case GBT_OPT_ANYHIT_LAST:
     case GBT_OPT_PRIMARY_TILES:
+    case GBT_OPT_PRIMARY_PACKETS:
         if (value < 0 || value > 1) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 0 or 1");
-        (option == GBT_OPT_ANYHIT_LAST ? ctx->anyhit_last : ctx->primary_tiles) = value;
+        (option == GBT_OPT_ANYHIT_LAST ? ctx->anyhit_last
+                                       : option == GBT_OPT_PRIMARY_TILES ? ctx->primary_tiles : ctx->primary_packets) = value;
         return GBT_OK;
     default:
         return gbt_fail(ctx, GBT_EINVAL, "set_option: unknown option " + std::to_string(option));

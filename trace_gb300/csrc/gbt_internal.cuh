@@ -53,6 +53,7 @@ struct gbt_ctx {
     // whose hit shades black, with an any-hit query; order camera rays in 8x4 pixel tiles
     int anyhit_last = 1;
     int primary_tiles = 1;
+    int primary_packets = 1;  // camera rays of a tiled frame traced as 32-ray packets
 };
 
 // Record a profiling event pair around one traversal launch.
@@ -143,6 +144,9 @@ int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, u
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
                          const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s,
                          unsigned long long *d_counters = nullptr, bool any = false);
+// 32-ray packets per warp (coherent camera rays) over a 4-wide tree; false when the tree has no 4-wide nodes
+bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,
+                                 unsigned int *d_error, cudaStream_t s, unsigned long long *d_counters);
 // render.cu
 int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
                        float *d_rgb);

@@ -229,7 +229,10 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
             gbt_prof_begin(ctx);
             // past MaxDepth a hit shades black, so only hit-or-miss matters there
             const bool any = ctx->anyhit_last && lv == levels - 1;
-            gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
+            // camera rays of a tiled frame: one coherent 8x4 tile per warp, traced as a packet
+            const bool packets = lv == 0 && ctx->primary_packets && ctx->primary_tiles &&
+                                 gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, ctr);
+            if (!packets) gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
             gbt_prof_end(ctx);
             k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],
                                             rs.aux[a ^ 1], rs.counts + lv + 1, bvh->d_prims, sc->d_prim_mat, sc->d_mats,

@@ -73,6 +73,117 @@ __global__ void __launch_bounds__(128) k_trace4(const BvhHeader *__restrict__ hd
     flush_work<COUNT>(w, counters);
 }
 
+// Packet traversal of a 4-wide tree for coherent rays (camera rays of one 8x4
+// pixel tile per warp): the warp walks one node sequence with a stack in shared
+// memory; each lane tests every child box against its own ray and closest hit,
+// the children that any lane hits are taken nearest first by the warp's
+// smallest entry distance, and a popped entry is skipped when no lane can
+// still reach it.  Control flow is uniform across the warp.  Each lane keeps
+// its own closest hit, so the hits equal the single-ray kernels' (exact ties
+// go to the lower record whatever the order).  Counters (profiling level 2)
+// count the warp's node fetches and leaf visits.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restrict__ hdr,
+                                                       const float4 *__restrict__ nodes, const float4 *__restrict__ recs,
+                                                       const float4 *__restrict__ rays, float4 *__restrict__ hits,
+                                                       uint32_t n, int out_mode, unsigned int *err,
+                                                       unsigned long long *counters) {
+    constexpr int PSTACK = 96;
+    constexpr uint32_t FULL = 0xffffffffu;
+    __shared__ int2 s_e[4][PSTACK];
+    __shared__ float s_t[4][PSTACK];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t id = blockIdx.x * 128 + threadIdx.x;
+    const bool live = id < n;
+    gbt_dev::Work w;
+    gbt_dev::Ray r;
+    if (live) {
+        r = gbt_dev::load_ray(rays, id);
+    } else {  // a ray that hits nothing keeps the lane in step
+        r.o = make_float3(0.f, 0.f, 0.f);
+        r.d = make_float3(1.f, 1.f, 1.f);
+        r.tmin = 1.f;
+        r.tmax = 0.f;
+        gbt_dev::finish_ray(r);
+    }
+    gbt_dev::Hit h;
+    h.t = r.tmax;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    const float MISS = __int_as_float(0x7f800000);
+    float te;
+    const bool root_hit = gbt_dev::slab(hdr->root_lo[0], hdr->root_lo[1], hdr->root_lo[2], hdr->root_hi[0],
+                                        hdr->root_hi[1], hdr->root_hi[2], r, h.t, te);
+    int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
+    int sp = 0;
+    auto pop = [&]() -> int2 {
+        while (sp > 0) {
+            --sp;
+            const float t = s_t[wp][sp];
+            const int2 e = s_e[wp][sp];
+            if (__any_sync(FULL, t <= h.t * 1.0000005f)) return e;
+        }
+        return make_int2(0, -1);
+    };
+    for (;;) {
+        if (node.y == 0) {
+            if (COUNT && lane == 0) w.nodes++;
+            const float4 *nd = nodes + 8 * (size_t)node.x;
+            float4 lx, hx, ly, hy, lz, hz, rff, cnf;
+            gbt_dev::ldg256(nd, lx, hx);
+            gbt_dev::ldg256(nd + 2, ly, hy);
+            gbt_dev::ldg256(nd + 4, lz, hz);
+            gbt_dev::ldg256(nd + 6, rff, cnf);
+            float t;
+            // per lane entry distance (+0 for -0, so that unsigned min orders them), MISS if missed
+            const float t0 = (__float_as_int(cnf.x) >= 0 && gbt_dev::slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) ? t + 0.f : MISS;
+            const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
+            const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
+            const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
+            gbt_dev::Cand c0, c1, c2, c3;
+            c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
+            c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
+            c2.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t2)));
+            c3.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t3)));
+            c0.e = make_int2(__float_as_int(rff.x), __float_as_int(cnf.x));
+            c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
+            c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
+            c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
+            gbt_dev::cx(c0, c1);
+            gbt_dev::cx(c2, c3);
+            gbt_dev::cx(c0, c2);
+            gbt_dev::cx(c1, c3);
+            gbt_dev::cx(c1, c2);
+            if (c0.t == MISS) {
+                node = pop();
+                continue;
+            }
+            const int np = (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
+            if (sp + np > PSTACK) {
+                if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
+            } else {
+                if (lane == 0) {
+                    int q = sp;
+                    if (c3.t != MISS) { s_e[wp][q] = c3.e; s_t[wp][q] = c3.t; ++q; }
+                    if (c2.t != MISS) { s_e[wp][q] = c2.e; s_t[wp][q] = c2.t; ++q; }
+                    if (c1.t != MISS) { s_e[wp][q] = c1.e; s_t[wp][q] = c1.t; ++q; }
+                }
+                sp += np;
+                __syncwarp();
+            }
+            node = c0.e;
+        } else if (node.y > 0) {
+            if (COUNT && lane == 0) w.prims += (uint32_t)node.y;
+            gbt_dev::leaf(recs, node.x, node.y, r, h);
+            node = pop();
+        } else {
+            break;
+        }
+    }
+    if (live) gbt_dev::store_hit(hits, id, h, recs, out_mode);
+    flush_work<COUNT>(w, counters);
+}
+
 __device__ __forceinline__ uint32_t lane_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -262,6 +373,20 @@ void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, u
         else
             k_trace2<false><<<blocks, 128, 0, s>>>(bvh->d_hdr, bvh->d_nodes, bvh->d_prims, rays, hits, n, d_count, out_mode, d_error, nullptr);
     }
+}
+
+bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,
+                                 unsigned int *d_error, cudaStream_t s, unsigned long long *counters) {
+    if (!(bvh->has_nodes4 || bvh->arity == 4)) return false;
+    if (n == 0) return true;
+    const BvhHeader *hd = bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr;
+    const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
+    const uint32_t blocks = (n + 127) / 128;
+    if (counters)
+        k_trace_packet4<true><<<blocks, 128, 0, s>>>(hd, nd, bvh->d_prims, rays, hits, n, out_mode, d_error, counters);
+    else
+        k_trace_packet4<false><<<blocks, 128, 0, s>>>(hd, nd, bvh->d_prims, rays, hits, n, out_mode, d_error, nullptr);
+    return true;
 }
 
 int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits) {
