@@ -111,12 +111,15 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
  *                          the first hit found
  *   GBT_OPT_PRIMARY_TILES  1 (default): the 32 camera rays of a warp cover an
  *                          8x4 pixel tile instead of 32 pixels of one row
- *   GBT_OPT_PRIMARY_PACKETS 1 (default): with tiles, the camera rays of a warp
- *                          are traced as one packet (a shared node sequence,
- *                          each lane testing its own ray)
+ *   GBT_OPT_PRIMARY_PACKETS with tiles, the camera rays of a warp traced as
+ *                          one packet (a shared node sequence, each lane testing
+ *                          its own ray): 0 never, 1 always, 2 (default) when
+ *                          the first render on a tree measures the packet
+ *                          kernel faster on its camera rays (that render traces
+ *                          them with both kernels and synchronises once)
  * The environment variables GBT_TRAVERSAL (persistent|simple|ww),
- * GBT_ANYHIT_LAST, GBT_PRIMARY_TILES and GBT_PRIMARY_PACKETS (0|1) set the
- * initial values.
+ * GBT_ANYHIT_LAST, GBT_PRIMARY_TILES (0|1) and GBT_PRIMARY_PACKETS (0|1|2) set
+ * the initial values.
  * No counterpart in the reference. */
 #define GBT_OPT_TRAVERSAL 0
 #define GBT_OPT_ANYHIT_LAST 1

@@ -93,7 +93,7 @@ def test_execution_options_leave_images_identical(ctx, kind):
     try:
         for trav in (0, 1, 2):
             for anyhit in (0, 1):
-                for tiles, packets in ((0, 0), (1, 0), (1, 1)):
+                for tiles, packets in ((0, 0), (1, 0), (1, 1), (1, 2)):
                     ctx.set_option("traversal", trav)
                     ctx.set_option("anyhit_last", anyhit)
                     ctx.set_option("primary_tiles", tiles)
@@ -109,7 +109,7 @@ def test_execution_options_leave_images_identical(ctx, kind):
         ctx.set_option("traversal", 0)
         ctx.set_option("anyhit_last", 1)
         ctx.set_option("primary_tiles", 1)
-        ctx.set_option("primary_packets", 1)
+        ctx.set_option("primary_packets", 2)
 
 
 def test_render_cornell_reflective_refractive(ctx):
@@ -131,3 +131,22 @@ def test_render_reflective_and_refractive_exact(ctx, kind):
     np.testing.assert_allclose(img.reshape(-1, 3), np.broadcast_to(want, (256, 3)), rtol=1e-5)
     # mirror: camera ray + reflected ray; glass: camera ray + two refracted rays
     assert st["rays_traced"] == 16 * 16 * 4 * (2 if kind == "mirror" else 3)
+
+
+def test_measured_packet_choice_keeps_the_image(ctx):
+    """GBT_OPT_PRIMARY_PACKETS = 2: the first render on a tree traces its camera rays with both
+    kernels and keeps the faster; the image equals the one without packets, then and after."""
+    s = scenes.cornell()
+    rd = s["render"]
+    cam = dict(s["camera"], aspect=1.0)
+    g = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s))
+    try:
+        ctx.set_option("primary_packets", 0)
+        ref, st0 = g.render(cam, 256, 256, 1, 3, rd["miss_mode"], rd["miss_color"], seed=9)
+        ctx.set_option("primary_packets", 2)
+        first, st1 = g.render(cam, 256, 256, 1, 3, rd["miss_mode"], rd["miss_color"], seed=9)  # measures
+        again, st2 = g.render(cam, 256, 256, 1, 3, rd["miss_mode"], rd["miss_color"], seed=9)  # uses the choice
+        assert np.array_equal(first, ref) and np.array_equal(again, ref)
+        assert st0["rays_traced"] == st1["rays_traced"] == st2["rays_traced"]
+    finally:
+        ctx.set_option("primary_packets", 2)

@@ -102,11 +102,12 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
         return GBT_ECUDA;
     }
     for (auto &e : c->ev) cudaEventCreate(&e);
+    for (auto &e : c->tune_ev) cudaEventCreate(&e);
     if (const char *t = std::getenv("GBT_TRAVERSAL"))
         c->traversal = std::strcmp(t, "simple") == 0 ? 1 : std::strcmp(t, "ww") == 0 ? 2 : 0;
     if (const char *t = std::getenv("GBT_ANYHIT_LAST")) c->anyhit_last = std::strcmp(t, "0") != 0;
     if (const char *t = std::getenv("GBT_PRIMARY_TILES")) c->primary_tiles = std::strcmp(t, "0") != 0;
-    if (const char *t = std::getenv("GBT_PRIMARY_PACKETS")) c->primary_packets = std::strcmp(t, "0") != 0;
+    if (const char *t = std::getenv("GBT_PRIMARY_PACKETS")) c->primary_packets = std::atoi(t) < 0 ? 0 : std::atoi(t) > 2 ? 2 : std::atoi(t);
     *out = c;
     return GBT_OK;
 }
@@ -123,6 +124,8 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     if (ctx->bstate) cudaFree(ctx->bstate);
     for (auto &e : ctx->prof_ev) cudaEventDestroy(e);
     for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : ctx->tune_ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -152,10 +155,12 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
         return GBT_OK;
     case GBT_OPT_ANYHIT_LAST:
     case GBT_OPT_PRIMARY_TILES:
-    case GBT_OPT_PRIMARY_PACKETS:
         if (value < 0 || value > 1) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 0 or 1");
-        (option == GBT_OPT_ANYHIT_LAST ? ctx->anyhit_last
-                                       : option == GBT_OPT_PRIMARY_TILES ? ctx->primary_tiles : ctx->primary_packets) = value;
+        (option == GBT_OPT_ANYHIT_LAST ? ctx->anyhit_last : ctx->primary_tiles) = value;
+        return GBT_OK;
+    case GBT_OPT_PRIMARY_PACKETS:
+        if (value < 0 || value > 2) return gbt_fail(ctx, GBT_EINVAL, "set_option: packets must be 0, 1 or 2");
+        ctx->primary_packets = value;
         return GBT_OK;
     default:
         return gbt_fail(ctx, GBT_EINVAL, "set_option: unknown option " + std::to_string(option));
@@ -330,6 +335,7 @@ extern "C" int gbt_lbvh_build(gbt_ctx *ctx, gbt_scene *scene, gbt_bvh **out) {
 extern "C" int gbt_lbvh_rebuild_async(gbt_ctx *ctx, gbt_bvh *bvh) {
     if (!ctx || !bvh || bvh->kind != GBT_BVH_LBVH) return gbt_fail(ctx, GBT_EINVAL, "rebuild: not an LBVH");
     bvh->has_nodes4 = 0;  // traversal uses the rebuilt binary nodes until gbt_bvh_set_layout(.., 4)
+    bvh->packet_choice = 0;
     return gbt_lbvh_enqueue(ctx, bvh);
 }
 
@@ -337,9 +343,11 @@ extern "C" int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width) {
     if (!ctx || !bvh || (width != 2 && width != 4)) return GBT_EINVAL;
     if (width == 2) {
         bvh->has_nodes4 = 0;
+        bvh->packet_choice = 0;
         return GBT_OK;
     }
     GBT_TRY(gbt_collapse4(ctx, bvh));
+    bvh->packet_choice = 0;
     return gbt_check_device_error(ctx, "bvh_set_layout");
 }
 

@@ -53,7 +53,10 @@ struct gbt_ctx {
     // whose hit shades black, with an any-hit query; order camera rays in 8x4 pixel tiles
     int anyhit_last = 1;
     int primary_tiles = 1;
-    int primary_packets = 1;  // camera rays of a tiled frame traced as 32-ray packets
+    // camera rays of a tiled frame as 32-ray packets: 0 never, 1 always, 2 (default) whichever
+    // kernel the first render on a BVH measures faster for its camera rays
+    int primary_packets = 2;
+    cudaEvent_t tune_ev[3] = {nullptr, nullptr, nullptr};
 };
 
 // Record a profiling event pair around one traversal launch.
@@ -112,6 +115,7 @@ struct gbt_bvh {
     BvhHeader *d_hdr4 = nullptr;
     uint32_t nodes4_cap = 0;
     int has_nodes4 = 0;
+    int packet_choice = 0;          // camera-ray kernel measured for this tree: 0 not yet, 1 packets, 2 single rays
 };
 
 // collapse.cu

@@ -229,10 +229,34 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
             gbt_prof_begin(ctx);
             // past MaxDepth a hit shades black, so only hit-or-miss matters there
             const bool any = ctx->anyhit_last && lv == levels - 1;
-            // camera rays of a tiled frame: one coherent 8x4 tile per warp, traced as a packet
-            const bool packets = lv == 0 && ctx->primary_packets && ctx->primary_tiles &&
-                                 gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, ctr);
-            if (!packets) gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
+            // camera rays of a tiled frame: one coherent 8x4 tile per warp, traced as a packet when
+            // that is faster for this tree and view (both kernels give the same hits)
+            const bool four = bvh->has_nodes4 || bvh->arity == 4;
+            bool packets = false, done = false;
+            if (lv == 0 && ctx->primary_tiles && four && ctx->primary_packets) {
+                if (ctx->primary_packets == 2 && bvh->packet_choice == 0 && ctx->profiling == 0 && count >= (1u << 16)) {
+                    // first render on this tree: time both kernels on this wave's camera rays
+                    cudaEventRecord(ctx->tune_ev[0], st);
+                    gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, nullptr);
+                    cudaEventRecord(ctx->tune_ev[1], st);
+                    gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, nullptr);
+                    cudaEventRecord(ctx->tune_ev[2], st);
+                    float tp = 0.f, ts = 0.f;
+                    if (cudaEventSynchronize(ctx->tune_ev[2]) == cudaSuccess &&
+                        cudaEventElapsedTime(&tp, ctx->tune_ev[0], ctx->tune_ev[1]) == cudaSuccess &&
+                        cudaEventElapsedTime(&ts, ctx->tune_ev[1], ctx->tune_ev[2]) == cudaSuccess)
+                        bvh->packet_choice = tp < ts ? 1 : 2;
+                    else
+                        bvh->packet_choice = 2;
+                    done = true;
+                    launches += 1;
+                }
+                packets = ctx->primary_packets == 1 || bvh->packet_choice == 1;
+            }
+            if (!done) {
+                if (packets) gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, ctr);
+                else gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
+            }
             gbt_prof_end(ctx);
             k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],
                                             rs.aux[a ^ 1], rs.counts + lv + 1, bvh->d_prims, sc->d_prim_mat, sc->d_mats,
