@@ -675,7 +675,7 @@ def main():
 
 # DRAM bytes of one frame's two traversal launches (dram__bytes_read.sum + dram__bytes_write.sum,
 # closest hit + any-hit) from the ncu capture summarised in
-# profiles/traversal_k_trace_pt_soup1M_phr.md; the LBVH tree was not captured.
+# profiles/traversal_kernels_soup1M_phr.md; the LBVH tree was not captured.
 TRAVERSAL_TRAFFIC = {"lbvh": None, "phr": (148.699136 + 22.645248 + 152.854272 + 17.515776) * 1e6}
 
 if __name__ == "__main__":
