@@ -673,10 +673,11 @@ def main():
     return 0
 
 
-# DRAM bytes of one frame's two traversal launches (dram__bytes_read.sum + dram__bytes_write.sum,
-# closest hit + any-hit) from the ncu capture summarised in
-# profiles/traversal_kernels_soup1M_phr.md; the LBVH tree was not captured.
-TRAVERSAL_TRAFFIC = {"lbvh": None, "phr": (148.699136 + 22.645248 + 152.854272 + 17.515776) * 1e6}
+# DRAM bytes of one headline frame's two traversal launches on the PHR tree
+# (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full capture each:
+# the camera rays' packet kernel and the any-hit kernel past MaxDepth); the LBVH
+# tree was not captured.
+TRAVERSAL_TRAFFIC = {"lbvh": None, "phr": (147.453184 + 21.7536 + 152.9536 + 17.157376) * 1e6}
 
 if __name__ == "__main__":
     sys.exit(main())
