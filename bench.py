@@ -31,6 +31,7 @@ import ctypes as C
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -116,8 +117,9 @@ class ClockSampler:
 
     def __init__(self, gpu_index):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/gbt_clocks.csv"
+        # raw samples go to a temporary file (GBT_CLOCKS_CSV keeps them at a chosen path)
+        self.path = os.environ.get("GBT_CLOCKS_CSV") or os.path.join(tempfile.gettempdir(),
+                                                                     "gbt_clocks_%d.csv" % os.getpid())
         try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
