@@ -510,37 +510,15 @@ extern "C" int gbt_bvh_export(gbt_ctx *ctx, gbt_bvh *bvh, int8_t *kind, int32_t 
     return GBT_OK;
 }
 
-// cost (bvh.go:226-239) over the exported pre-order arrays
-static double cost_at(const ExportOut &o, size_t &i) {
-    size_t me = i++;
-    if (o.kind[me]) return 1.0 * (double)o.count[me];
-    auto surf = [&](size_t n) {
-        const double *b = &o.box[6 * n];
-        double w = b[3] - b[0], h = b[4] - b[1], d = b[5] - b[2];
-        return 2 * w * h + 2 * w * d + 2 * h * d;
-    };
-    double sn = surf(me), acc = 0.0;
-    for (int c = 0; c < o.count[me]; c++) {
-        size_t ci = i;
-        double cc = cost_at(o, i);
-        if (sn != 0) acc += surf(ci) / sn * cc;
-    }
-    return 2.0 + acc;
-}
-
 extern "C" int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost) {
     if (!ctx || !bvh || !cost) return GBT_EINVAL;
-    ExportOut o;
-    GBT_TRY(export_tree(ctx, bvh, o));
-    size_t i = 0;
-    *cost = cost_at(o, i);
-    return GBT_OK;
+    return gbt_cost_device(ctx, bvh, cost);  // bvh.go:226-239, evaluated on the device (cost.cu)
 }
 
 // gridOptimizer.OptimizedPHRparams (optimizer.go:44-84) with omega and evalPHR
 // (optimizer.go:86-94): every (alpha, delta) of the grid, alphas outer, is built
-// on the device with its build cost; the SAH cost (bvh.go:226-239) is evaluated
-// on the downloaded tree; the first minimum of the normalised score wins.
+// on the device with its build cost and its SAH cost (bvh.go:226-239, also on
+// the device); the first minimum of the normalised score wins.
 extern "C" int gbt_phr_optimize_grid(gbt_ctx *ctx, gbt_bvh *aux, int32_t branching, const double *alphas,
                                      int32_t n_alpha, const double *deltas, int32_t n_delta, int32_t frame_width,
                                      int32_t frame_height, double *alpha, double *delta, double *evals) {

@@ -120,6 +120,8 @@ struct gbt_bvh {
 
 // collapse.cu
 int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh);
+// cost.cu: BVH.Cost of the tree as built
+int gbt_cost_device(gbt_ctx *ctx, gbt_bvh *bvh, double *out);
 
 // ---------------------------------------------------------------------------
 // helpers

@@ -779,8 +779,10 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
 // ---------------------------------------------------------------------------
 // traversal nodes
 // ---------------------------------------------------------------------------
+// Also the parent of every inner node (-1 for the root) and -2 for the entries
+// of leaves, which hold no node.
 __global__ void k_phr_finalize(const PNode *__restrict__ pn, const PhrGlobals *__restrict__ g, float4 *nodes, int arity,
-                               BvhHeader *hdr, uint32_t n_prim, unsigned int *err) {
+                               BvhHeader *hdr, uint32_t n_prim, int32_t *__restrict__ parent, unsigned int *err) {
     const uint32_t count = g->pnode_ctr;
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
@@ -802,7 +804,15 @@ __global__ void k_phr_finalize(const PNode *__restrict__ pn, const PhrGlobals *_
     }
     if (i >= count) return;
     const PNode &b = pn[i];
-    if (b.leaf) return;
+    if (b.leaf) {
+        parent[i] = -2;
+        return;
+    }
+    if ((int32_t)i == g->root) parent[i] = -1;
+    for (int c = 0; c < b.nchild && c < 4; c++) {
+        const int32_t ci = b.child[c];
+        if (ci >= 0 && (uint32_t)ci < count && !pn[ci].leaf) parent[ci] = (int32_t)i;
+    }
     float lo[4][3], hi[4][3];
     int32_t ref[4], cnt[4];
     for (int c = 0; c < 4; c++) {
@@ -874,6 +884,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     const uint32_t pnode_cap = 2 * n_aux + 2;
     if (cudaMalloc(&out->d_prims, (size_t)N * 3 * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&out->d_nodes, (size_t)pnode_cap * per_node * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&out->d_parent, (size_t)pnode_cap * sizeof(int32_t)) != cudaSuccess ||
         cudaMalloc(&out->d_hdr, sizeof(BvhHeader)) != cudaSuccess) {
         cudaGetLastError();
         return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
@@ -990,6 +1001,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         levels++;
     }
     k_phr_finalize<<<(pnode_cap + 255) / 256, 256, 0, st>>>(d_pn, d_g, out->d_nodes, bf == 2 ? 2 : 4, out->d_hdr, N,
+                                                            out->d_parent,
                                                             ctx->d_error);
     GBT_CUDA(ctx, cudaGetLastError());
     GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
