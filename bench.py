@@ -262,6 +262,10 @@ def run_batch_workload(args):
     steps = max(2, args.steps // 2)
     ms_plain, rays_plain = timed("plain", steps)
     plain = [b.read(i) for i in range(b.n)]
+    forms = {}
+    for name, mode in (("wavefront", _lib.BATCH_WAVEFRONT), ("megakernel", _lib.BATCH_MEGAKERNEL)):
+        ms_f, rays_f = timed("batched", steps, _lib.BatchConfig(128, 16, 0, mode))
+        forms[name] = {"value": rays_f / ms_f / 1e3, "ms_per_frame": ms_f}
     cfg, tune_ms = b.autotune()
     ms_batch, rays_batch = timed("batched", steps, cfg)
     batched = [b.read(i) for i in range(b.n)]
@@ -273,8 +277,10 @@ def run_batch_workload(args):
             "triangles_total": tris, "scenes": count,
             "plain": {"value": rays_plain / ms_plain / 1e3, "ms_per_frame": ms_plain, "rays": rays_plain},
             "batched": {"value": rays_batch / ms_batch / 1e3, "ms_per_frame": ms_batch, "rays": rays_batch,
-                        "config": {"block": cfg.block, "fetch_min": cfg.fetch_min, "stack": cfg.stack},
+                        "config": {"mode": ["megakernel", "wavefront"][cfg.mode], "block": cfg.block,
+                                   "fetch_min": cfg.fetch_min, "stack": cfg.stack},
                         "autotune_best_ms": tune_ms},
+            "forms": forms,
             "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},
             "speedup_batched_vs_plain": (rays_batch / ms_batch) / (rays_plain / ms_plain),
             "images": {"max_abs_diff_batched_vs_plain": diff, "rmse_batched_vs_plain": rmse},

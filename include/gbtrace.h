@@ -240,29 +240,38 @@ typedef struct {
     float *d_rgb;              /* device image, width*height*3 floats */
 } gbt_batch_item;
 
+#define GBT_BATCH_MEGAKERNEL 0 /* one persistent launch; each lane runs whole paths from a device queue */
+#define GBT_BATCH_WAVEFRONT 1  /* per bounce level one shading and one multi-tree traversal launch over all items */
+
 typedef struct {
-    int32_t block;     /* threads per block: 64, 128 or 256 */
-    int32_t fetch_min; /* 0: a warp refills only when all its lanes are idle; 16: when fewer than 16 are busy */
-    int32_t stack;     /* 0: traversal stack in local memory; 1: its first 12 entries in shared memory */
+    int32_t block;     /* megakernel: threads per block, 64, 128 or 256 */
+    int32_t fetch_min; /* megakernel: 0, a warp refills only when all its lanes are idle; 16, when fewer than 16 are busy */
+    int32_t stack;     /* megakernel: 0, traversal stack in local memory; 1, its first 12 entries in shared memory */
+    int32_t mode;      /* GBT_BATCH_MEGAKERNEL or GBT_BATCH_WAVEFRONT (which ignores the three fields above) */
 } gbt_batch_config;
 
-/* All items in one persistent launch pulling (scene, path) work from a device
- * queue; each path runs to completion in one lane.  Images equal those of
- * gbt_render_async per item up to float summation order.  cfg NULL: the
- * autotuned choice of this context, else block 128 / fetch_min 16 / local
- * stack.  All BVHs must share a traversal layout (gbt_bvh_set_layout).
- * Enqueue only; the first call may grow the context's batch state. */
+/* All items as one frame: either one persistent launch pulling (scene, path)
+ * work from a device queue, each path running to completion in one lane, or
+ * the wavefront over all items (two launches per bounce level).  Images equal
+ * those of gbt_render_async per item up to float summation order.  cfg NULL:
+ * the autotuned choice of this context, else the wavefront form.  All BVHs
+ * must share a traversal layout (gbt_bvh_set_layout).  Enqueue only; the
+ * first call may grow the context's batch state and path buffers. */
 int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, const gbt_batch_config *cfg);
 /* The baseline: the same items as one gbt_render_async per item. */
 int gbt_render_batch_plain_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n);
-/* Times every configuration on these items (one warm frame, best of two
- * timed frames), keeps the fastest for this context and returns it. */
+/* Times the wavefront form and every megakernel configuration on these items
+ * (one warm frame, best of two timed frames), keeps the fastest for this
+ * context and returns it. */
 int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, gbt_batch_config *best,
                        double *best_ms);
 /* A CUDA graph of one batched frame: optionally the in-place LBVH rebuild of
  * every item (which switches their traversal to the binary nodes), then the
- * accumulator clear, the persistent launch and the resolve.  Items, outputs
- * and BVHs must outlive the graph. */
+ * accumulator clear, the frame in form cfg and the resolve.  The graph owns
+ * its descriptors, accumulators and path buffers; with rebuilds it also holds
+ * the context's scratch, which cannot grow (larger builds fail with
+ * GBT_EINVAL) until the graph is destroyed.  Outputs and BVHs must outlive the
+ * graph, and the graph must be destroyed before its context. */
 typedef struct gbt_graph gbt_graph;
 int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, const gbt_batch_config *cfg,
                            int32_t rebuild_lbvh, gbt_graph **out);

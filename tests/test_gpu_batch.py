@@ -7,7 +7,7 @@ form must therefore have the same image RMSE against a converged image.
 import numpy as np
 import pytest
 
-from trace_gb300 import pt, scenes
+from trace_gb300 import _lib, pt, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -25,30 +25,84 @@ def make_batch(ctx, count=6, lo=1_000, hi=60_000, w=96, h=64, spp=4, depth=3):
     return ss, pt.Batch(ctx, bvhs, cams, params)
 
 
-def test_batched_equals_plain(ctx):
+MEGA = _lib.BatchConfig(128, 16, 0, _lib.BATCH_MEGAKERNEL)
+WAVE = _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT)
+
+
+@pytest.mark.parametrize("cfg", [None, MEGA, WAVE, _lib.BatchConfig(256, 0, 1, _lib.BATCH_MEGAKERNEL)],
+                         ids=["default", "megakernel", "wavefront", "megakernel_b256_shared"])
+def test_batched_equals_plain(ctx, cfg):
     ss, b = make_batch(ctx)
     try:
         b.render("plain")
         plain = [b.read(i) for i in range(b.n)]
-        b.render("batched")
+        b.render("batched", cfg)
         batched = [b.read(i) for i in range(b.n)]
         for p, q in zip(plain, batched):
             assert np.all(np.isfinite(q))
             np.testing.assert_allclose(q, p, rtol=1e-4, atol=1e-5)
-        # the autotuner returns one of the supported configurations and it renders the same
+    finally:
+        b.close()
+
+
+def test_autotune_choice_renders_the_same(ctx):
+    ss, b = make_batch(ctx)
+    try:
+        b.render("plain")
+        plain = [b.read(i) for i in range(b.n)]
         cfg, ms = b.autotune()
-        assert cfg.block in (64, 128, 256) and cfg.fetch_min in (0, 16) and cfg.stack in (0, 1) and ms > 0
+        assert ms > 0 and cfg.mode in (_lib.BATCH_MEGAKERNEL, _lib.BATCH_WAVEFRONT)
+        if cfg.mode == _lib.BATCH_MEGAKERNEL:
+            assert cfg.block in (64, 128, 256) and cfg.fetch_min in (0, 16) and cfg.stack in (0, 1)
         b.render("batched", cfg)
+        for i, p in enumerate(plain):
+            np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
+        b.render("batched")  # the tuned choice is now the context's default
         for i, p in enumerate(plain):
             np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
     finally:
         b.close()
 
 
-def test_batch_graph_with_rebuild(ctx):
+def test_mixed_depths_and_sizes(ctx):
+    """Items of different depth, size and spp in one frame: the wavefront runs the deepest
+    item's levels, and shallower items' paths end at their own depth."""
+    ss = scenes.batch(count=3, lo=2_000, hi=20_000, seed=5, width=64, height=48, spp=2, max_depth=1)
+    bvhs, cams, params = [], [], []
+    for k, s in enumerate(ss):
+        bvhs.append(pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s)))
+        cams.append(s["camera"])
+        p = dict(s["render"])
+        p.update(seed=7 + k, max_depth=[0, 5, 2][k], width=[64, 40, 33][k], height=[48, 30, 17][k], spp=[2, 3, 1][k])
+        params.append(p)
+    b = pt.Batch(ctx, bvhs, cams, params)
+    try:
+        b.render("plain")
+        plain = [b.read(i) for i in range(b.n)]
+        for cfg in (WAVE, MEGA):
+            b.render("batched", cfg)
+            for i, p in enumerate(plain):
+                np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
+    finally:
+        b.close()
+
+
+def test_bad_config_is_rejected(ctx):
+    ss, b = make_batch(ctx, count=2)
+    try:
+        with pytest.raises(pt.GbtError):
+            b.render("batched", _lib.BatchConfig(96, 16, 0, _lib.BATCH_MEGAKERNEL))
+        with pytest.raises(pt.GbtError):
+            b.render("batched", _lib.BatchConfig(128, 16, 0, 7))
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("cfg", [WAVE, MEGA], ids=["wavefront", "megakernel"])
+def test_batch_graph_with_rebuild(ctx, cfg):
     ss, b = make_batch(ctx, count=4)
     try:
-        b.make_graph(rebuild=True)
+        b.make_graph(rebuild=True, cfg=cfg)
         b.render("graph")
         g1 = [b.read(i) for i in range(b.n)]
         b.render("graph")  # a replay rebuilds and renders again: same result
@@ -58,5 +112,24 @@ def test_batch_graph_with_rebuild(ctx):
         for x, y, p in zip(g1, g2, plain):
             np.testing.assert_allclose(x, y, rtol=1e-4, atol=1e-5)
             np.testing.assert_allclose(x, p, rtol=1e-4, atol=1e-5)
+    finally:
+        b.close()
+
+
+def test_graph_owns_its_buffers(ctx):
+    """A plain render after graph creation reuses and may regrow the context's path buffers;
+    the graph's replays must not be affected."""
+    ss, b = make_batch(ctx, count=2)
+    try:
+        b.make_graph(rebuild=False, cfg=WAVE)
+        b.render("graph")
+        g1 = [b.read(i) for i in range(b.n)]
+        s = scenes.batch(count=1, lo=2_000, hi=2_001, seed=9, width=256, height=256, spp=8, max_depth=2)[0]
+        big = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s))
+        big.render(s["camera"], 256, 256, 8, 2)
+        b.render("graph")
+        g2 = [b.read(i) for i in range(b.n)]
+        for x, y in zip(g1, g2):
+            np.testing.assert_allclose(x, y, rtol=1e-4, atol=1e-5)
     finally:
         b.close()

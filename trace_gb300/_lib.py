@@ -53,8 +53,11 @@ class BatchItem(C.Structure):
     _fields_ = [("bvh", C.c_void_p), ("camera", Camera), ("params", RenderParams), ("d_rgb", C.c_void_p)]
 
 
+BATCH_MEGAKERNEL, BATCH_WAVEFRONT = 0, 1
+
+
 class BatchConfig(C.Structure):
-    _fields_ = [("block", C.c_int32), ("fetch_min", C.c_int32), ("stack", C.c_int32)]
+    _fields_ = [("block", C.c_int32), ("fetch_min", C.c_int32), ("stack", C.c_int32), ("mode", C.c_int32)]
 
 
 class RenderStats(C.Structure):

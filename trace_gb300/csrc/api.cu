@@ -43,6 +43,9 @@ int gbt_check_device_error(gbt_ctx *ctx, const char *what) {
 
 int gbt_scratch(gbt_ctx *ctx, size_t bytes, void **out) {
     if (ctx->scratch_bytes < bytes) {
+        if (ctx->scratch_pins > 0)
+            return gbt_fail(ctx, GBT_EINVAL, "scratch: a live graph's rebuilds use the context's scratch, which "
+                                             "cannot grow until the graph is destroyed");
         if (ctx->scratch) {
             GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             cudaFree(ctx->scratch);

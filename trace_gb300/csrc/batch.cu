@@ -1,15 +1,21 @@
-// Batched rendering: many scenes and many independent renders in one
-// persistent launch.
+// Batched rendering: many scenes and many independent renders as one frame.
 //
-// Every (scene, path) pair of the batch is one entry of a device work queue
-// (a counter over the concatenated path ranges of the items).  Each lane of a
-// resident warp pulls a path, runs it to completion -- camera ray, closest
-// hit, shading, next bounce (shade.cuh) -- and pulls the next one; lanes are
-// refilled with warp-aggregated atomics.  The paths are the ones the per-scene
-// wavefront renderer traces (same Philox counters), so the images agree up to
-// the order of float additions.  The per-frame sequence (accumulator clear,
-// the persistent kernel, the resolve) can be captured in a CUDA graph together
-// with in-place LBVH rebuilds.  Launch parameters come from a small autotuner.
+// Every (scene, path) pair of the batch is one entry of a work range (the
+// concatenated path ranges of the items).  Two forms trace it:
+//   megakernel  one persistent launch; each lane of a resident warp pulls a
+//               path from a device queue, runs it to completion -- camera ray,
+//               closest hit, shading, next bounce (shade.cuh) -- and pulls the
+//               next one; lanes are refilled with warp-aggregated atomics;
+//   wavefront   the per-scene wavefront over all items at once: per bounce
+//               level one camera/shading kernel over the live paths of every
+//               item and one persistent traversal over all their trees
+//               (k_trace_multi), so each level is two launches whatever the
+//               number of items.
+// The paths are the ones the per-scene wavefront renderer traces (same
+// Philox counters), so the images agree up to the order of float additions.
+// The per-frame sequence can be captured in a CUDA graph together with
+// in-place LBVH rebuilds.  The form and its launch parameters come from a
+// small autotuner.
 //
 // The reference renders one scene at a time (render.go:91-129); batching has
 // no counterpart there.
@@ -30,9 +36,7 @@ namespace {
 constexpr int MAX_ITEMS = 1024;
 
 struct ItemDev {
-    const BvhHeader *hdr;
-    const float4 *nodes;
-    const float4 *recs;
+    TreeRef tree;  // first member: the item table doubles as the traversal's tree table
     const uint32_t *prim_mat;
     const float4 *mats;
     const float *normals;
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
                 sp = 0;
                 leaf = make_int2(0, 0);
                 float te;
-                const BvhHeader *hd = it.hdr;
+                const BvhHeader *hd = it.tree.hdr;
                 node = slab(hd->root_lo[0], hd->root_lo[1], hd->root_lo[2], hd->root_hi[0], hd->root_hi[1],
                             hd->root_hi[2], r, h.t, te)
                            ? make_int2(hd->root_ref, hd->root_cnt)
@@ -146,8 +150,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
                     item = find_item(s_base, n_items, q);
                     const ItemDev &it = items[item];
                     g = path_id(it.sp, q - it.path_base);
-                    nodes = it.nodes;
-                    recs = it.recs;
+                    nodes = it.tree.nodes;
+                    recs = it.tree.recs;
                     level = 0;
                     any = false;
                     T = f3(1.f, 1.f, 1.f);
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const ItemDev *__restrict__ ite
                     sp = 0;
                     leaf = make_int2(0, 0);
                     float te;
-                    const BvhHeader *hd = it.hdr;
+                    const BvhHeader *hd = it.tree.hdr;
                     node = slab(hd->root_lo[0], hd->root_lo[1], hd->root_lo[2], hd->root_hi[0], hd->root_hi[1],
                                 hd->root_hi[2], r, h.t, te)
                                ? make_int2(hd->root_ref, hd->root_cnt)
@@ -225,6 +229,83 @@ __global__ void k_resolve_batch(const ItemDev *__restrict__ items, int n_items, 
     }
 }
 
+// wavefront form: camera rays of queue entries [g0, g0 + count); the item index rides in aux[2 i + 1].w
+__global__ void __launch_bounds__(256) k_raygen_batch(const ItemDev *__restrict__ items, int n_items, uint32_t g0,
+                                                      uint32_t count, float4 *__restrict__ rays,
+                                                      float4 *__restrict__ aux, uint32_t *counts) {
+    __shared__ uint32_t s_base[MAX_ITEMS];
+    for (int k = threadIdx.x; k < n_items; k += blockDim.x) s_base[k] = items[k].path_base;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) counts[0] = count;
+    if (i >= count) return;
+    const uint32_t q = g0 + i;
+    const int item = find_item(s_base, n_items, q);
+    const ItemDev &it = items[item];
+    const uint32_t g = path_id(it.sp, q - it.path_base);
+    float3 o, d;
+    primary_ray(it.cam, it.sp, g, o, d);
+    rays[2 * (size_t)i] = make_float4(o.x, o.y, o.z, 0.001f);
+    rays[2 * (size_t)i + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
+    aux[2 * (size_t)i] = make_float4(1.f, 1.f, 1.f, __int_as_float((int)g));
+    aux[2 * (size_t)i + 1] = make_float4(0.f, 0.f, 0.f, __int_as_float(item));
+}
+
+// wavefront form: shade the level's hits of every item, compact the live paths into the next level
+__global__ void __launch_bounds__(256) k_shade_batch(const ItemDev *__restrict__ items, int level,
+                                                     const float4 *__restrict__ rays_in,
+                                                     const float4 *__restrict__ aux_in, const float4 *__restrict__ hits,
+                                                     const uint32_t *__restrict__ count_in,
+                                                     float4 *__restrict__ rays_out, float4 *__restrict__ aux_out,
+                                                     uint32_t *count_out, uint32_t cap) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *count_in;
+    bool alive = false;
+    float4 out_r0, out_r1, out_a0, out_a1;
+    if (i < n) {
+        const float4 a0 = aux_in[2 * (size_t)i], a1 = aux_in[2 * (size_t)i + 1];
+        const ItemDev &it = items[__float_as_int(a1.w)];
+        float3 T = f3(a0.x, a0.y, a0.z), L = f3(a1.x, a1.y, a1.z);
+        const uint32_t g = (uint32_t)__float_as_int(a0.w);
+        const float4 h = hits[i];
+        const float4 ro = rays_in[2 * (size_t)i], rd = rays_in[2 * (size_t)i + 1];
+        float3 o = f3(ro.x, ro.y, ro.z), d = f3(rd.x, rd.y, rd.z), no, nd;
+        alive = shade_step(it.sp, level, g, o, d, h.x, h.y, h.z, __float_as_int(h.w), it.tree.recs, it.prim_mat,
+                           it.mats, it.normals, T, L, no, nd);
+        if (alive) {
+            out_r0 = make_float4(no.x, no.y, no.z, 0.0001f);
+            out_r1 = make_float4(nd.x, nd.y, nd.z, __int_as_float(0x7f800000));
+            out_a0 = make_float4(T.x, T.y, T.z, a0.w);
+            out_a1 = make_float4(L.x, L.y, L.z, a1.w);
+        } else {
+            deposit(it.acc, g % it.sp.npix, L);
+        }
+    }
+    const uint32_t ball = __ballot_sync(0xffffffffu, alive);
+    if (ball == 0) return;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == (uint32_t)(__ffs(ball) - 1)) base = atomicAdd(count_out, (uint32_t)__popc(ball));
+    base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
+    if (alive) {
+        const uint32_t slot = base + __popc(ball & lane_lt_mask());
+        if (slot < cap) {
+            rays_out[2 * (size_t)slot] = out_r0;
+            rays_out[2 * (size_t)slot + 1] = out_r1;
+            aux_out[2 * (size_t)slot] = out_a0;
+            aux_out[2 * (size_t)slot + 1] = out_a1;
+        }
+    }
+}
+
+__global__ void k_sum_levels(const uint32_t *counts, int levels, unsigned long long *total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int i = 0; i < levels; i++) s += counts[i];
+        *total += s;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -235,6 +316,8 @@ struct gbt_graph {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     void *pinned_items = nullptr;  // page-locked source of the graph's descriptor upload
+    void *state = nullptr;         // the graph's own descriptors, accumulators and path buffers
+    int pins_scratch = 0;          // its rebuilds use the context's scratch
     uint64_t paths = 0;
 };
 
@@ -258,7 +341,7 @@ void launch_batch(const ItemDev *items, int n, uint32_t total, uint32_t *fetch, 
     k_batch<W, BLOCK, DYN, SH><<<grid, BLOCK, 0, s>>>(items, n, total, fetch, err, rays);
 }
 
-// config: block in {64,128,256} x fetch_min in {0,16} x stack in {local, first 12 entries in shared memory}
+// megakernel config: block in {64,128,256} x fetch_min in {0,16} x stack in {local, first 12 entries in shared memory}
 template <int W>
 Launcher pick(const gbt_batch_config &c) {
     const int b = c.block, d = c.fetch_min > 0 ? 1 : 0, s = c.stack ? 1 : 0;
@@ -291,21 +374,31 @@ int check_items(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, int *widt
     return GBT_OK;
 }
 
-// Per-context batch state: item descriptors, accumulators, queue counter.
-int prepare(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<ItemDev> &hi, uint64_t *total_paths,
-            size_t *acc_floats) {
+int check_config(gbt_ctx *ctx, const gbt_batch_config &c, int width) {
+    if (c.mode == GBT_BATCH_WAVEFRONT) return GBT_OK;
+    if (c.mode != GBT_BATCH_MEGAKERNEL || !(width == 4 ? pick<4>(c) : pick<2>(c)))
+        return gbt_fail(ctx, GBT_EINVAL, "batch: unsupported configuration");
+    return GBT_OK;
+}
+
+// Item descriptors of one frame; acc pointers are set by place().
+int describe(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<ItemDev> &hi, uint64_t *total_paths,
+             size_t *acc_floats) {
     hi.resize(n);
     uint64_t paths = 0, pix = 0;
     for (uint32_t i = 0; i < n; i++) {
         const gbt_batch_item &it = items[i];
         const gbt_bvh *b = it.bvh;
         ItemDev &d = hi[i];
-        d.hdr = b->has_nodes4 ? b->d_hdr4 : b->d_hdr;
-        d.nodes = b->has_nodes4 ? b->d_nodes4 : b->d_nodes;
-        d.recs = b->d_prims;
+        d.tree.hdr = b->has_nodes4 ? b->d_hdr4 : b->d_hdr;
+        d.tree.nodes = b->has_nodes4 ? b->d_nodes4 : b->d_nodes;
+        d.tree.recs = b->d_prims;
+        d.tree.any_level = ctx->anyhit_last ? it.params.max_depth + 1 : -1;
+        d.tree.pad = 0;
         d.prim_mat = b->scene->d_prim_mat;
         d.mats = b->scene->d_mats;
         d.normals = b->scene->d_normals;
+        d.acc = nullptr;
         d.out = it.d_rgb;
         d.cam = gbt_make_cam(&it.camera);
         d.sp = gbt_make_shade_params(&it.params, b->scene->n_tri);
@@ -321,7 +414,33 @@ int prepare(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<I
     *total_paths = paths;
     *acc_floats = pix * 3;
     if (pix * 3 >= (1ull << 32)) return gbt_fail(ctx, GBT_EINVAL, "batch: too many pixels");
-    size_t need = gbt_align(n * sizeof(ItemDev)) + gbt_align(*acc_floats * sizeof(float)) + 256;
+    return GBT_OK;
+}
+
+// Device buffers of one frame: descriptors, accumulators and, for the wavefront form, the path buffers.
+struct FrameBufs {
+    ItemDev *items = nullptr;
+    float *acc = nullptr;
+    RenderState rs{};  // rs.cap == 0: no path buffers
+};
+
+size_t head_bytes(size_t n, size_t acc_floats) {
+    return gbt_align(n * sizeof(ItemDev)) + gbt_align(acc_floats * sizeof(float));
+}
+
+void bind_head(void *base, size_t n, FrameBufs *fb) {
+    unsigned char *b = static_cast<unsigned char *>(base);
+    fb->items = reinterpret_cast<ItemDev *>(b);
+    fb->acc = reinterpret_cast<float *>(b + gbt_align(n * sizeof(ItemDev)));
+}
+
+void place(std::vector<ItemDev> &hi, float *acc) {
+    for (auto &d : hi) d.acc = acc + (size_t)d.pix_base * 3;
+}
+
+// the context's batch state (grow-only) and, for the wavefront form, its render path buffers
+int context_bufs(gbt_ctx *ctx, size_t n, size_t acc_floats, uint64_t paths, bool waves, FrameBufs *fb) {
+    const size_t need = head_bytes(n, acc_floats);
     if (ctx->bstate_bytes < need) {
         if (ctx->bstate) {
             cudaStreamSynchronize(ctx->stream);
@@ -335,29 +454,57 @@ int prepare(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<I
         }
         ctx->bstate_bytes = need;
     }
-    unsigned char *base = static_cast<unsigned char *>(ctx->bstate);
-    float *acc = reinterpret_cast<float *>(base + gbt_align(n * sizeof(ItemDev)));
-    for (uint32_t i = 0; i < n; i++) hi[i].acc = acc + (size_t)hi[i].pix_base * 3;
+    bind_head(ctx->bstate, n, fb);
+    fb->rs = RenderState{};
+    if (waves) return gbt_render_buffers(ctx, paths, 0, &fb->rs);
     return GBT_OK;
 }
 
-int enqueue_frame(gbt_ctx *ctx, const ItemDev *h_items, size_t n_items, uint64_t paths, size_t acc_floats,
-                  const gbt_batch_config &cfg, int width) {
+int enqueue_frame(gbt_ctx *ctx, const FrameBufs &fb, const ItemDev *h_items, size_t n_items, uint64_t paths,
+                  size_t acc_floats, const gbt_batch_config &cfg, int width) {
     cudaStream_t st = ctx->stream;
-    unsigned char *base = static_cast<unsigned char *>(ctx->bstate);
-    ItemDev *d_items = reinterpret_cast<ItemDev *>(base);
-    float *acc = reinterpret_cast<float *>(base + gbt_align(n_items * sizeof(ItemDev)));
-    uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
-    Launcher f = width == 4 ? pick<4>(cfg) : pick<2>(cfg);
-    if (!f) return gbt_fail(ctx, GBT_EINVAL, "batch: unsupported configuration");
-    GBT_CUDA(ctx, cudaMemcpyAsync(d_items, h_items, n_items * sizeof(ItemDev), cudaMemcpyHostToDevice, st));
-    GBT_CUDA(ctx, cudaMemsetAsync(acc, 0, acc_floats * sizeof(float), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st));
-    f(d_items, (int)n_items, (uint32_t)paths, fetch, ctx->d_error, ctx->d_counters + 2, ctx->num_sms, st);
-    k_resolve_batch<<<ctx->num_sms * 4, 256, 0, st>>>(d_items, (int)n_items, (uint32_t)acc_floats);
+    GBT_CUDA(ctx, cudaMemcpyAsync(fb.items, h_items, n_items * sizeof(ItemDev), cudaMemcpyHostToDevice, st));
+    GBT_CUDA(ctx, cudaMemsetAsync(fb.acc, 0, acc_floats * sizeof(float), st));
+    uint64_t launches = 0, trav = 0;
+    if (cfg.mode == GBT_BATCH_MEGAKERNEL) {
+        Launcher f = width == 4 ? pick<4>(cfg) : pick<2>(cfg);
+        if (!f) return gbt_fail(ctx, GBT_EINVAL, "batch: unsupported configuration");
+        uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
+        GBT_CUDA(ctx, cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st));
+        f(fb.items, (int)n_items, (uint32_t)paths, fetch, ctx->d_error, ctx->d_counters + 2, ctx->num_sms, st);
+        launches++;
+    } else {
+        const RenderState &rs = fb.rs;
+        if (rs.cap == 0) return gbt_fail(ctx, GBT_EINVAL, "batch: wavefront form without path buffers");
+        int levels = 0;  // surfaces at depth 0..MaxDepth+1 of the deepest item
+        for (size_t i = 0; i < n_items; i++) levels = std::max(levels, h_items[i].sp.max_depth + 2);
+        for (uint64_t g0 = 0; g0 < paths; g0 += rs.cap) {
+            const uint32_t count = (uint32_t)std::min<uint64_t>(paths - g0, rs.cap);
+            const uint32_t blocks = (count + 255) / 256;
+            GBT_CUDA(ctx, cudaMemsetAsync(rs.counts, 0, 64 * sizeof(uint32_t), st));
+            k_raygen_batch<<<blocks, 256, 0, st>>>(fb.items, (int)n_items, (uint32_t)g0, count, rs.rays[0], rs.aux[0],
+                                                   rs.counts);
+            launches++;
+            for (int lv = 0; lv < levels; lv++) {
+                const int a = lv & 1;
+                gbt_launch_traverse_multi(ctx, &fb.items->tree, sizeof(ItemDev), width, rs.rays[a], rs.aux[a], rs.hits,
+                                          count, rs.counts + lv, lv, st);
+                k_shade_batch<<<blocks, 256, 0, st>>>(fb.items, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv,
+                                                      rs.rays[a ^ 1], rs.aux[a ^ 1], rs.counts + lv + 1,
+                                                      (uint32_t)rs.cap);
+                launches += 2;
+                trav++;
+            }
+            k_sum_levels<<<1, 32, 0, st>>>(rs.counts, levels, ctx->d_counters + 2);
+            launches++;
+        }
+    }
+    k_resolve_batch<<<ctx->num_sms * 4, 256, 0, st>>>(fb.items, (int)n_items, (uint32_t)acc_floats);
+    launches++;
     GBT_CUDA(ctx, cudaGetLastError());
     ctx->last_stats.paths += paths;
-    ctx->last_stats.kernel_launches += 2;
+    ctx->last_stats.kernel_launches += launches;
+    ctx->last_stats.traverse_launches += trav;
     return GBT_OK;
 }
 
@@ -367,7 +514,19 @@ gbt_batch_config default_config(const gbt_ctx *ctx) {
     c.block = 128;
     c.fetch_min = 16;
     c.stack = 0;
+    c.mode = GBT_BATCH_WAVEFRONT;
     return c;
+}
+
+// descriptors and the context's buffers for one frame in form cfg
+int setup(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, bool waves, std::vector<ItemDev> &hi,
+          uint64_t *paths, size_t *accf, FrameBufs *fb) {
+    int rc = describe(ctx, items, n, hi, paths, accf);
+    if (rc) return rc;
+    rc = context_bufs(ctx, n, *accf, *paths, waves, fb);
+    if (rc) return rc;
+    place(hi, fb->acc);
+    return GBT_OK;
 }
 
 }  // namespace
@@ -378,13 +537,17 @@ extern "C" int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items,
     int width;
     int rc = check_items(ctx, items, n, &width);
     if (rc) return rc;
+    const gbt_batch_config c = cfg ? *cfg : default_config(ctx);
+    rc = check_config(ctx, c, width);
+    if (rc) return rc;
     std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;
-    rc = prepare(ctx, items, n, hi, &paths, &accf);
+    FrameBufs fb;
+    rc = setup(ctx, items, n, c.mode == GBT_BATCH_WAVEFRONT, hi, &paths, &accf, &fb);
     if (rc) return rc;
     // a copy from pageable memory is staged before cudaMemcpyAsync returns, so hi may go
-    return enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, cfg ? *cfg : default_config(ctx), width);
+    return enqueue_frame(ctx, fb, hi.data(), hi.size(), paths, accf, c, width);
 }
 
 extern "C" int gbt_render_batch_plain_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n) {
@@ -408,34 +571,36 @@ extern "C" int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uin
     std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;
-    rc = prepare(ctx, items, n, hi, &paths, &accf);
+    FrameBufs fb;
+    rc = setup(ctx, items, n, true, hi, &paths, &accf, &fb);
     if (rc) return rc;
-    const int blocks[3] = {64, 128, 256}, fetches[2] = {0, 16}, stacks[2] = {0, 1};
+    std::vector<gbt_batch_config> cands;
+    cands.push_back(gbt_batch_config{128, 16, 0, GBT_BATCH_WAVEFRONT});
+    for (int b : {64, 128, 256})
+        for (int f : {0, 16})
+            for (int s : {0, 1}) cands.push_back(gbt_batch_config{b, f, s, GBT_BATCH_MEGAKERNEL});
     double bms = 1e30;
-    gbt_batch_config bc{128, 16, 0};
-    for (int b : blocks)
-        for (int f : fetches)
-            for (int s : stacks) {
-                gbt_batch_config c{b, f, s};
-                // one untimed frame, then the best of two timed frames
-                rc = enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, c, width);
-                if (rc) return rc;
-                double m = 1e30;
-                for (int rep = 0; rep < 2; rep++) {
-                    GBT_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
-                    rc = enqueue_frame(ctx, hi.data(), hi.size(), paths, accf, c, width);
-                    if (rc) return rc;
-                    GBT_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
-                    GBT_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
-                    float ms = 0.f;
-                    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
-                    m = std::min(m, (double)ms);
-                }
-                if (m < bms) {
-                    bms = m;
-                    bc = c;
-                }
-            }
+    gbt_batch_config bc = cands[0];
+    for (const gbt_batch_config &c : cands) {
+        // one untimed frame, then the best of two timed frames
+        rc = enqueue_frame(ctx, fb, hi.data(), hi.size(), paths, accf, c, width);
+        if (rc) return rc;
+        double m = 1e30;
+        for (int rep = 0; rep < 2; rep++) {
+            GBT_CUDA(ctx, cudaEventRecord(ctx->ev[2], ctx->stream));
+            rc = enqueue_frame(ctx, fb, hi.data(), hi.size(), paths, accf, c, width);
+            if (rc) return rc;
+            GBT_CUDA(ctx, cudaEventRecord(ctx->ev[3], ctx->stream));
+            GBT_CUDA(ctx, cudaEventSynchronize(ctx->ev[3]));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+            m = std::min(m, (double)ms);
+        }
+        if (m < bms) {
+            bms = m;
+            bc = c;
+        }
+    }
     rc = gbt_check_device_error(ctx, "batch_autotune");
     if (rc) return rc;
     ctx->batch_cfg = bc;
@@ -460,51 +625,59 @@ extern "C" int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items,
         for (uint32_t i = 0; i < n; i++) items[i].bvh->has_nodes4 = 0;
         width = 2;
     }
-    gbt_graph *g = new gbt_graph();
-    g->ctx = ctx;
+    const gbt_batch_config c = cfg ? *cfg : default_config(ctx);
+    rc = check_config(ctx, c, width);
+    if (rc) return rc;
+    const bool waves = c.mode == GBT_BATCH_WAVEFRONT;
+    std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;
-    std::vector<ItemDev> hi;
-    rc = prepare(ctx, items, n, hi, &paths, &accf);
-    if (rc) { delete g; return rc; }
+    rc = describe(ctx, items, n, hi, &paths, &accf);
+    if (rc) return rc;
+    gbt_graph *g = new gbt_graph();
+    g->ctx = ctx;
     g->paths = paths;
-    if (cudaMallocHost(&g->pinned_items, hi.size() * sizeof(ItemDev)) != cudaSuccess) {
-        cudaGetLastError();
+    auto fail = [&](int code) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        if (g->graph) cudaGraphDestroy(g->graph);
+        if (g->pinned_items) cudaFreeHost(g->pinned_items);
+        if (g->state) cudaFree(g->state);
         delete g;
-        return gbt_fail(ctx, GBT_ENOMEM, "batch graph: pinned descriptors");
-    }
+        cudaGetLastError();
+        return code;
+    };
+    // the graph owns its buffers, so later work on the context cannot move them
+    const size_t head = head_bytes(n, accf);
+    const size_t bytes = head + (waves ? gbt_render_state_bytes(paths, 0) : 0);
+    if (cudaMalloc(&g->state, bytes) != cudaSuccess) return fail(gbt_fail(ctx, GBT_ENOMEM, "batch graph: state"));
+    FrameBufs fb;
+    bind_head(g->state, n, &fb);
+    if (waves) gbt_render_state_bind(static_cast<unsigned char *>(g->state) + head, paths, 0, &fb.rs);
+    place(hi, fb.acc);
+    if (cudaMallocHost(&g->pinned_items, hi.size() * sizeof(ItemDev)) != cudaSuccess)
+        return fail(gbt_fail(ctx, GBT_ENOMEM, "batch graph: pinned descriptors"));
     std::memcpy(g->pinned_items, hi.data(), hi.size() * sizeof(ItemDev));
-    // grow every scratch buffer the captured work uses before capturing
+    // grow the scratch the captured rebuilds use before capturing; it may not move while the graph lives
     for (uint32_t i = 0; rebuild_lbvh && i < n; i++) {
         void *scr;
         rc = gbt_scratch(ctx, gbt_lbvh_scratch_bytes(items[i].bvh->n_prim), &scr);
-        if (rc) { delete g; return rc; }
+        if (rc) return fail(rc);
     }
     cudaStream_t st = ctx->stream;
-    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-        delete g;
-        return gbt_fail(ctx, GBT_ECUDA, "batch graph: begin capture");
-    }
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(gbt_fail(ctx, GBT_ECUDA, "batch graph: begin capture"));
     for (uint32_t i = 0; rebuild_lbvh && i < n && !rc; i++) rc = gbt_lbvh_enqueue(ctx, items[i].bvh);
-    if (!rc)
-        rc = enqueue_frame(ctx, static_cast<const ItemDev *>(g->pinned_items), hi.size(), paths, accf,
-                           cfg ? *cfg : default_config(ctx), width);
+    if (!rc) rc = enqueue_frame(ctx, fb, static_cast<const ItemDev *>(g->pinned_items), hi.size(), paths, accf, c, width);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &graph);
-    if (rc || e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        cudaFreeHost(g->pinned_items);
-        delete g;
-        cudaGetLastError();
-        return rc ? rc : gbt_fail(ctx, GBT_ECUDA, std::string("batch graph: capture: ") + cudaGetErrorString(e));
-    }
     g->graph = graph;
-    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        cudaFreeHost(g->pinned_items);
-        delete g;
-        cudaGetLastError();
-        return gbt_fail(ctx, GBT_ECUDA, "batch graph: instantiate");
+    if (rc || e != cudaSuccess)
+        return fail(rc ? rc : gbt_fail(ctx, GBT_ECUDA, std::string("batch graph: capture: ") + cudaGetErrorString(e)));
+    if (cudaGraphInstantiate(&g->exec, graph, 0) != cudaSuccess)
+        return fail(gbt_fail(ctx, GBT_ECUDA, "batch graph: instantiate"));
+    if (rebuild_lbvh) {
+        g->pins_scratch = 1;
+        ctx->scratch_pins++;
     }
     ctx->last_stats.paths = 0;
     *out = g;
@@ -520,10 +693,14 @@ extern "C" int gbt_graph_launch(gbt_ctx *ctx, gbt_graph *g) {
 
 extern "C" int gbt_graph_destroy(gbt_graph *g) {
     if (!g) return GBT_EINVAL;
-    if (g->ctx) cudaStreamSynchronize(g->ctx->stream);
+    if (g->ctx) {
+        cudaStreamSynchronize(g->ctx->stream);
+        if (g->pins_scratch) g->ctx->scratch_pins--;
+    }
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
     if (g->pinned_items) cudaFreeHost(g->pinned_items);
+    if (g->state) cudaFree(g->state);
     delete g;
     return GBT_OK;
 }

@@ -29,6 +29,7 @@ struct gbt_ctx {
     // grow-only scratch, reused by every build on this context
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    int scratch_pins = 0;  // live graphs whose captured work uses the scratch: it may not move
     // render state (grow-only)
     void *rstate = nullptr;
     size_t rstate_bytes = 0;
@@ -150,10 +151,33 @@ int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, u
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
                          const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s,
                          unsigned long long *d_counters = nullptr, bool any = false);
+// One tree of a batched frame as the multi-tree traversal reads it: a ray's
+// tree is the index in .w of its second path record (aux[2 i + 1].w).
+struct TreeRef {
+    const BvhHeader *hdr;
+    const float4 *nodes;
+    const float4 *recs;
+    int32_t any_level;  // the level whose rays take an any-hit query (-1: none)
+    int32_t pad;
+};
+// trees: entry k at byte offset k * stride
+void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays, const float4 *aux,
+                               float4 *hits, uint32_t n, const uint32_t *d_count, int level, cudaStream_t s);
 // 32-ray packets per warp (coherent camera rays) over a 4-wide tree; false when the tree has no 4-wide nodes
 bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,
                                  unsigned int *d_error, cudaStream_t s, unsigned long long *d_counters);
-// render.cu
+// render.cu: wavefront path state (ping-pong rays and path records, hits, per-level counts, accumulator)
+struct RenderState {
+    size_t cap;  // paths per wave
+    float4 *rays[2], *aux[2];
+    float4 *hits;
+    uint32_t *counts;  // per level
+    float *acc;
+};
+// bytes of the state for waves over `total` paths and npix pixels, and its layout at base
+size_t gbt_render_state_bytes(size_t total, size_t npix);
+void gbt_render_state_bind(void *base, size_t total, size_t npix, RenderState *rs);
+int gbt_render_buffers(gbt_ctx *ctx, size_t total, size_t npix, RenderState *rs);
 int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
                        float *d_rgb);
 // phr.cu

@@ -147,14 +147,6 @@ ShadeParams gbt_make_shade_params(const gbt_render_params *p, uint32_t n_tri) {
     return sp;
 }
 
-// Per-context render state: ping-pong path buffers, hits, counters, accumulator.
-struct RenderState {
-    size_t cap;  // paths per wave
-    float4 *rays[2], *aux[2];
-    float4 *hits;
-    uint32_t *counts;  // per level
-    float *acc;
-};
 
 static size_t render_layout(size_t cap, size_t npix, size_t *off) {
     size_t o = 0;
@@ -166,6 +158,55 @@ static size_t render_layout(size_t cap, size_t npix, size_t *off) {
     off[5] = o; o = gbt_align(o + 64 * sizeof(uint32_t));
     off[6] = o; o = gbt_align(o + npix * 3 * sizeof(float));
     return o;
+}
+
+#define GBT_TRY_R(x)         \
+    do {                     \
+        int rc_ = (x);       \
+        if (rc_) return rc_; \
+    } while (0)
+
+static size_t wave_cap(size_t total) { return total < (size_t)(1u << 23) ? total : (size_t)(1u << 23); }
+
+size_t gbt_render_state_bytes(size_t total, size_t npix) {
+    size_t off[7];
+    return render_layout(wave_cap(total), npix, off);
+}
+
+void gbt_render_state_bind(void *base, size_t total, size_t npix, RenderState *rs) {
+    size_t off[7];
+    const size_t cap = wave_cap(total);
+    render_layout(cap, npix, off);
+    unsigned char *b = static_cast<unsigned char *>(base);
+    rs->cap = cap;
+    rs->rays[0] = reinterpret_cast<float4 *>(b + off[0]);
+    rs->rays[1] = reinterpret_cast<float4 *>(b + off[1]);
+    rs->aux[0] = reinterpret_cast<float4 *>(b + off[2]);
+    rs->aux[1] = reinterpret_cast<float4 *>(b + off[3]);
+    rs->hits = reinterpret_cast<float4 *>(b + off[4]);
+    rs->counts = reinterpret_cast<uint32_t *>(b + off[5]);
+    rs->acc = reinterpret_cast<float *>(b + off[6]);
+}
+
+// The context's path buffers for waves of up to 2^23 of `total` paths and an
+// accumulator of npix pixels (grow-only; a growth synchronises the stream).
+int gbt_render_buffers(gbt_ctx *ctx, size_t total, size_t npix, RenderState *rs) {
+    const size_t need = gbt_render_state_bytes(total, npix);
+    if (ctx->rstate_bytes < need) {
+        if (ctx->rstate) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->rstate);
+        }
+        ctx->rstate = nullptr;
+        ctx->rstate_bytes = 0;
+        if (cudaMalloc(&ctx->rstate, need) != cudaSuccess) {
+            cudaGetLastError();
+            return gbt_fail(ctx, GBT_ENOMEM, "render: state allocation");
+        }
+        ctx->rstate_bytes = need;
+    }
+    gbt_render_state_bind(ctx->rstate, total, npix, rs);
+    return GBT_OK;
 }
 
 int gbt_render_check(gbt_ctx *ctx, const gbt_render_params *p) {
@@ -181,32 +222,9 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
     if (rc) return rc;
     const size_t npix = (size_t)p->width * p->height;
     const size_t total = npix * (size_t)p->spp;
-    size_t cap = total < (size_t)(1u << 23) ? total : (size_t)(1u << 23);
-    size_t off[7];
-    size_t need = render_layout(cap, npix, off);
-    if (ctx->rstate_bytes < need) {
-        if (ctx->rstate) {
-            cudaStreamSynchronize(ctx->stream);
-            cudaFree(ctx->rstate);
-        }
-        ctx->rstate = nullptr;
-        ctx->rstate_bytes = 0;
-        if (cudaMalloc(&ctx->rstate, need) != cudaSuccess) {
-            cudaGetLastError();
-            return gbt_fail(ctx, GBT_ENOMEM, "render: state allocation");
-        }
-        ctx->rstate_bytes = need;
-    }
-    unsigned char *b = static_cast<unsigned char *>(ctx->rstate);
     RenderState rs;
-    rs.cap = cap;
-    rs.rays[0] = reinterpret_cast<float4 *>(b + off[0]);
-    rs.rays[1] = reinterpret_cast<float4 *>(b + off[1]);
-    rs.aux[0] = reinterpret_cast<float4 *>(b + off[2]);
-    rs.aux[1] = reinterpret_cast<float4 *>(b + off[3]);
-    rs.hits = reinterpret_cast<float4 *>(b + off[4]);
-    rs.counts = reinterpret_cast<uint32_t *>(b + off[5]);
-    rs.acc = reinterpret_cast<float *>(b + off[6]);
+    GBT_TRY_R(gbt_render_buffers(ctx, total, npix, &rs));
+    const size_t cap = rs.cap;
 
     cudaStream_t st = ctx->stream;
     gbt_scene *sc = bvh->scene;

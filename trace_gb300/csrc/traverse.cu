@@ -304,6 +304,110 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
     flush_work<COUNT>(w, counters);
 }
 
+// The persistent traversal over the rays of many trees (a batched frame):
+// each lane takes its tree, and whether its ray is an any-hit query, from the
+// tree table when it fetches a ray.  Hits are written as (t, u, v, record).
+template <int W, int DYN>
+__global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_multi(const TreeRef *__restrict__ trees, uint32_t stride,
+                                                                  const float4 *__restrict__ rays,
+                                                                  const float4 *__restrict__ aux,
+                                                                  float4 *__restrict__ hits, uint32_t n,
+                                                                  const uint32_t *__restrict__ d_count, int level,
+                                                                  unsigned int *err, uint32_t *fetch) {
+    constexpr int STACK = W == 2 ? 64 : 96;
+    constexpr int SH = GBT_PT_SH;
+    const uint32_t total = d_count ? *d_count : n;
+    const uint32_t lane = threadIdx.x & 31;
+    __shared__ int2 s_se[SH * 128];
+    __shared__ float s_st[SH * 128];
+    gbt_dev::SharedTopStack<STACK, SH> st;
+    st.se = s_se + threadIdx.x;
+    st.st = s_st + threadIdx.x;
+    st.stride = 128;
+    int sp = 0;
+    int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
+    gbt_dev::Ray r;
+    gbt_dev::Hit h;
+    h.t = 0.f;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    const float4 *nodes = nullptr, *recs = nullptr;
+    bool any = false;
+    uint32_t rid = 0xffffffffu;
+    bool pool_empty = false;  // warp-uniform
+    for (;;) {
+        if (node.y < 0 && leaf.y <= 0 && rid != 0xffffffffu) {
+            gbt_dev::store_hit(hits, rid, h, recs, 1);
+            rid = 0xffffffffu;
+        }
+        const bool want = rid == 0xffffffffu && !pool_empty;
+        const uint32_t need = __ballot_sync(0xffffffffu, want);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == (uint32_t)leader) base = atomicAdd(fetch, (uint32_t)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            bool empty_here = false;
+            if (want) {
+                const uint32_t id = base + __popc(need & lane_lt());
+                if (id < total) {
+                    rid = id;
+                    r = gbt_dev::load_ray(rays, id);
+                    const TreeRef tr = *reinterpret_cast<const TreeRef *>(
+                        reinterpret_cast<const unsigned char *>(trees) +
+                        (size_t)__float_as_int(__ldg(&aux[2 * (size_t)id + 1].w)) * stride);
+                    nodes = tr.nodes;
+                    recs = tr.recs;
+                    any = tr.any_level == level;
+                    h.t = r.tmax;
+                    h.u = h.v = 0.f;
+                    h.rec = -1;
+                    sp = 0;
+                    leaf = make_int2(0, 0);
+                    float te;
+                    const float *lo = tr.hdr->root_lo, *hi = tr.hdr->root_hi;
+                    node = gbt_dev::slab(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], r, h.t, te)
+                               ? make_int2(tr.hdr->root_ref, tr.hdr->root_cnt)
+                               : make_int2(0, -1);
+                    if (node.y > 0) {
+                        leaf = node;
+                        node = make_int2(0, -1);
+                    }
+                } else {
+                    empty_here = true;
+                }
+            }
+            pool_empty = __any_sync(0xffffffffu, empty_here) || pool_empty;
+        }
+        if (__all_sync(0xffffffffu, rid == 0xffffffffu)) break;
+        while (node.y >= 0 || leaf.y > 0) {
+            while (node.y == 0) {
+                node = W == 2 ? gbt_dev::step2(nodes, node, st, sp, r, h.t, err)
+                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err);
+                if (node.y > 0 && leaf.y <= 0) {
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                }
+                if (!__any_sync(__activemask(), leaf.y <= 0)) break;
+            }
+            while (leaf.y > 0) {
+                gbt_dev::leaf(recs, leaf.x, leaf.y, r, h);
+                if (any && h.rec >= 0) {  // any hit ends the query
+                    node = make_int2(0, -1);
+                    leaf = make_int2(0, 0);
+                    sp = 0;
+                } else if (node.y > 0) {
+                    leaf = node;
+                    node = st.pop(sp, h.t);
+                } else {
+                    leaf = make_int2(0, 0);
+                }
+            }
+            if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
+        }
+    }
+}
+
 template <int W, bool COUNT, int DYN, bool ANY>
 void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
@@ -373,6 +477,27 @@ void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, u
         else
             k_trace2<false><<<blocks, 128, 0, s>>>(bvh->d_hdr, bvh->d_nodes, bvh->d_prims, rays, hits, n, d_count, out_mode, d_error, nullptr);
     }
+}
+
+void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays, const float4 *aux,
+                               float4 *hits, uint32_t n, const uint32_t *d_count, int level, cudaStream_t s) {
+    if (n == 0) return;
+    static int per_sm[2] = {0, 0};
+    const int w = width == 4 ? 1 : 0;
+    if (per_sm[w] == 0) {
+        if (w) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[w], k_trace_multi<4, GBT_PT_DYN>, 128, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[w], k_trace_multi<2, GBT_PT_DYN>, 128, 0);
+        if (per_sm[w] <= 0) per_sm[w] = 1;
+    }
+    uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
+    cudaMemsetAsync(fetch, 0, sizeof(uint32_t), s);
+    uint32_t grid = (uint32_t)(ctx->num_sms * per_sm[w]);
+    const uint32_t need = (n + 127) / 128;
+    if (need < grid) grid = need;
+    if (w) k_trace_multi<4, GBT_PT_DYN><<<grid, 128, 0, s>>>(trees, (uint32_t)stride, rays, aux, hits, n, d_count, level,
+                                                                   ctx->d_error, fetch);
+    else k_trace_multi<2, GBT_PT_DYN><<<grid, 128, 0, s>>>(trees, (uint32_t)stride, rays, aux, hits, n, d_count, level,
+                                                                   ctx->d_error, fetch);
 }
 
 bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,
