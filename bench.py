@@ -263,8 +263,9 @@ def run_batch_workload(args):
     ms_plain, rays_plain = timed("plain", steps)
     plain = [b.read(i) for i in range(b.n)]
     forms = {}
-    for name, mode in (("wavefront", _lib.BATCH_WAVEFRONT), ("megakernel", _lib.BATCH_MEGAKERNEL)):
-        ms_f, rays_f = timed("batched", steps, _lib.BatchConfig(128, 16, 0, mode))
+    for name, mode, packets in (("wavefront_packets", _lib.BATCH_WAVEFRONT, 1), ("wavefront", _lib.BATCH_WAVEFRONT, 0),
+                                ("megakernel", _lib.BATCH_MEGAKERNEL, 0)):
+        ms_f, rays_f = timed("batched", steps, _lib.BatchConfig(128, 16, 0, mode, packets))
         forms[name] = {"value": rays_f / ms_f / 1e3, "ms_per_frame": ms_f}
     cfg, tune_ms = b.autotune()
     ms_batch, rays_batch = timed("batched", steps, cfg)
@@ -278,7 +279,7 @@ def run_batch_workload(args):
             "plain": {"value": rays_plain / ms_plain / 1e3, "ms_per_frame": ms_plain, "rays": rays_plain},
             "batched": {"value": rays_batch / ms_batch / 1e3, "ms_per_frame": ms_batch, "rays": rays_batch,
                         "config": {"mode": ["megakernel", "wavefront"][cfg.mode], "block": cfg.block,
-                                   "fetch_min": cfg.fetch_min, "stack": cfg.stack},
+                                   "fetch_min": cfg.fetch_min, "stack": cfg.stack, "packets": cfg.packets},
                         "autotune_best_ms": tune_ms},
             "forms": forms,
             "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},

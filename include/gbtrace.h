@@ -172,6 +172,12 @@ int gbt_bvh_destroy(gbt_bvh *bvh);
  * traverses the binary nodes.  Results are identical; only speed differs.
  * gbt_lbvh_rebuild_async drops the 4-wide view.  No counterpart in the reference. */
 int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width);
+/* Camera rays of a 4-wide tree: 0 measures on the next render whether 32-ray
+ * packets or one ray per lane is faster (also what a rebuild or a layout change
+ * resets to), 1 packets, 2 one ray per lane.  Under GBT_OPT_PRIMARY_PACKETS 2
+ * (the default) renders and batched frames follow this choice; hits are the
+ * same either way.  No counterpart in the reference. */
+int gbt_bvh_set_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t choice);
 
 int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost); /* bvh.go:46-48 BVH.Cost */
 int gbt_bvh_size(gbt_ctx *ctx, gbt_bvh *bvh, int64_t *size); /* bvh.go:50-52 BVH.Size */
@@ -248,13 +254,16 @@ typedef struct {
     int32_t fetch_min; /* megakernel: 0, a warp refills only when all its lanes are idle; 16, when fewer than 16 are busy */
     int32_t stack;     /* megakernel: 0, traversal stack in local memory; 1, its first 12 entries in shared memory */
     int32_t mode;      /* GBT_BATCH_MEGAKERNEL or GBT_BATCH_WAVEFRONT (which ignores the three fields above) */
+    int32_t packets;   /* wavefront over 4-wide trees: 1 traces the camera rays of every item whose tree is
+                          faster so (measured once per tree, as gbt_render_async does) as 32-ray packets */
 } gbt_batch_config;
 
 /* All items as one frame: either one persistent launch pulling (scene, path)
  * work from a device queue, each path running to completion in one lane, or
  * the wavefront over all items (two launches per bounce level).  Images equal
  * those of gbt_render_async per item up to float summation order.  cfg NULL:
- * the autotuned choice of this context, else the wavefront form.  All BVHs
+ * the autotuned choice of this context, else the wavefront form with camera
+ * ray packets as GBT_OPT_PRIMARY_PACKETS allows.  All BVHs
  * must share a traversal layout (gbt_bvh_set_layout).  Enqueue only; the
  * first call may grow the context's batch state and path buffers. */
 int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, const gbt_batch_config *cfg);

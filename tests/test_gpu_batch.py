@@ -25,12 +25,13 @@ def make_batch(ctx, count=6, lo=1_000, hi=60_000, w=96, h=64, spp=4, depth=3):
     return ss, pt.Batch(ctx, bvhs, cams, params)
 
 
-MEGA = _lib.BatchConfig(128, 16, 0, _lib.BATCH_MEGAKERNEL)
-WAVE = _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT)
+MEGA = _lib.BatchConfig(128, 16, 0, _lib.BATCH_MEGAKERNEL, 0)
+WAVE = _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT, 0)
+WAVE_PACKETS = _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT, 1)
 
 
-@pytest.mark.parametrize("cfg", [None, MEGA, WAVE, _lib.BatchConfig(256, 0, 1, _lib.BATCH_MEGAKERNEL)],
-                         ids=["default", "megakernel", "wavefront", "megakernel_b256_shared"])
+@pytest.mark.parametrize("cfg", [None, MEGA, WAVE, WAVE_PACKETS, _lib.BatchConfig(256, 0, 1, _lib.BATCH_MEGAKERNEL, 0)],
+                         ids=["default", "megakernel", "wavefront", "wavefront_packets", "megakernel_b256_shared"])
 def test_batched_equals_plain(ctx, cfg):
     ss, b = make_batch(ctx)
     try:
@@ -79,7 +80,7 @@ def test_mixed_depths_and_sizes(ctx):
     try:
         b.render("plain")
         plain = [b.read(i) for i in range(b.n)]
-        for cfg in (WAVE, MEGA):
+        for cfg in (WAVE, WAVE_PACKETS, MEGA):
             b.render("batched", cfg)
             for i, p in enumerate(plain):
                 np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
@@ -93,12 +94,14 @@ def test_bad_config_is_rejected(ctx):
         with pytest.raises(pt.GbtError):
             b.render("batched", _lib.BatchConfig(96, 16, 0, _lib.BATCH_MEGAKERNEL))
         with pytest.raises(pt.GbtError):
-            b.render("batched", _lib.BatchConfig(128, 16, 0, 7))
+            b.render("batched", _lib.BatchConfig(128, 16, 0, 7, 0))
+        with pytest.raises(pt.GbtError):
+            b.render("batched", _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT, 2))
     finally:
         b.close()
 
 
-@pytest.mark.parametrize("cfg", [WAVE, MEGA], ids=["wavefront", "megakernel"])
+@pytest.mark.parametrize("cfg", [WAVE, WAVE_PACKETS, MEGA], ids=["wavefront", "wavefront_packets", "megakernel"])
 def test_batch_graph_with_rebuild(ctx, cfg):
     ss, b = make_batch(ctx, count=4)
     try:
@@ -121,7 +124,7 @@ def test_graph_owns_its_buffers(ctx):
     the graph's replays must not be affected."""
     ss, b = make_batch(ctx, count=2)
     try:
-        b.make_graph(rebuild=False, cfg=WAVE)
+        b.make_graph(rebuild=False, cfg=WAVE_PACKETS)
         b.render("graph")
         g1 = [b.read(i) for i in range(b.n)]
         s = scenes.batch(count=1, lo=2_000, hi=2_001, seed=9, width=256, height=256, spp=8, max_depth=2)[0]
@@ -132,4 +135,50 @@ def test_graph_owns_its_buffers(ctx):
         for x, y in zip(g1, g2):
             np.testing.assert_allclose(x, y, rtol=1e-4, atol=1e-5)
     finally:
+        b.close()
+
+
+def test_packet_and_single_ray_items_in_one_wave(ctx):
+    """Items whose trees take camera rays as packets lead the queue; a wave splits into a
+    packet range and a one-ray-per-lane range (here inside the first of two waves)."""
+    ss = scenes.batch(count=3, lo=2_000, hi=8_000, seed=6, width=1024, height=1024, spp=3, max_depth=2)
+    bvhs, cams, params = [], [], []
+    for k, s in enumerate(ss):
+        g = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s))
+        g.set_packets([2, 1, 1][k])  # the single-ray item first in the caller's order
+        bvhs.append(g)
+        cams.append(s["camera"])
+        p = dict(s["render"])
+        p["seed"] = 40 + k
+        params.append(p)
+    b = pt.Batch(ctx, bvhs, cams, params)
+    try:
+        assert b.paths > (1 << 23)  # two waves
+        b.render("plain")
+        plain = [b.read(i) for i in range(b.n)]
+        b.render("batched", WAVE_PACKETS)
+        for i, p in enumerate(plain):
+            np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
+        b.make_graph(cfg=WAVE_PACKETS)
+        b.render("graph")
+        for i, p in enumerate(plain):
+            np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
+    finally:
+        b.close()
+
+
+def test_forced_packets_option(ctx):
+    """GBT_OPT_PRIMARY_PACKETS 1 takes every item's camera rays as packets, 0 none; the
+    images are the same."""
+    ss, b = make_batch(ctx, count=3)
+    try:
+        b.render("plain")
+        plain = [b.read(i) for i in range(b.n)]
+        for opt in (1, 0):
+            ctx.set_option("primary_packets", opt)
+            b.render("batched", WAVE_PACKETS)
+            for i, p in enumerate(plain):
+                np.testing.assert_allclose(b.read(i), p, rtol=1e-4, atol=1e-5)
+    finally:
+        ctx.set_option("primary_packets", 2)
         b.close()

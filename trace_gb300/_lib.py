@@ -24,7 +24,7 @@ EXPORTS = [
     "gbt_bvh_cost", "gbt_bvh_size", "gbt_bvh_counts", "gbt_bvh_export", "gbt_lbvh_sorted",
     "gbt_trace", "gbt_trace_async", "gbt_render", "gbt_render_async", "gbt_render_last_stats",
     "gbt_device_alloc", "gbt_device_free", "gbt_copy_h2d_async", "gbt_copy_d2h_async",
-    "gbt_sort_morton_pairs_noalloc", "gbt_bvh_set_layout",
+    "gbt_sort_morton_pairs_noalloc", "gbt_bvh_set_layout", "gbt_bvh_set_packets",
     "gbt_render_batch_async", "gbt_render_batch_plain_async", "gbt_batch_autotune", "gbt_batch_graph_create",
     "gbt_graph_launch", "gbt_graph_destroy",
     "gbt_adjoint_forward_async", "gbt_adjoint_backward_async", "gbt_l2_loss_async",
@@ -57,7 +57,8 @@ BATCH_MEGAKERNEL, BATCH_WAVEFRONT = 0, 1
 
 
 class BatchConfig(C.Structure):
-    _fields_ = [("block", C.c_int32), ("fetch_min", C.c_int32), ("stack", C.c_int32), ("mode", C.c_int32)]
+    _fields_ = [("block", C.c_int32), ("fetch_min", C.c_int32), ("stack", C.c_int32), ("mode", C.c_int32),
+                ("packets", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -119,6 +120,7 @@ def load():
         "gbt_copy_d2h_async": ([P, P, P, C.c_size_t], C.c_int),
         "gbt_sort_morton_pairs_noalloc": ([P, P, P, P, u32], C.c_int),
         "gbt_bvh_set_layout": ([P, P, i32], C.c_int),
+        "gbt_bvh_set_packets": ([P, P, i32], C.c_int),
         "gbt_render_batch_async": ([P, P, u32, P], C.c_int),
         "gbt_render_batch_plain_async": ([P, P, u32], C.c_int),
         "gbt_batch_autotune": ([P, P, u32, P, C.POINTER(d)], C.c_int),

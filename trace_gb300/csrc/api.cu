@@ -354,6 +354,12 @@ extern "C" int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width) {
     return gbt_check_device_error(ctx, "bvh_set_layout");
 }
 
+extern "C" int gbt_bvh_set_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t choice) {
+    if (!ctx || !bvh || choice < 0 || choice > 2) return GBT_EINVAL;
+    bvh->packet_choice = choice;
+    return GBT_OK;
+}
+
 static int phr_build(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int32_t branching, bool view,
                      gbt_bvh **out) {
     if (!ctx || !aux || !out) return GBT_EINVAL;

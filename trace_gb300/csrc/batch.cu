@@ -375,26 +375,41 @@ int check_items(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, int *widt
 }
 
 int check_config(gbt_ctx *ctx, const gbt_batch_config &c, int width) {
-    if (c.mode == GBT_BATCH_WAVEFRONT) return GBT_OK;
+    if (c.mode == GBT_BATCH_WAVEFRONT && (c.packets == 0 || c.packets == 1)) return GBT_OK;
     if (c.mode != GBT_BATCH_MEGAKERNEL || !(width == 4 ? pick<4>(c) : pick<2>(c)))
         return gbt_fail(ctx, GBT_EINVAL, "batch: unsupported configuration");
     return GBT_OK;
 }
 
-// Item descriptors of one frame; acc pointers are set by place().
+// camera rays of this tree go as packets (when the frame's form allows them): the context forces
+// them, or the tree's measured or set choice says so
+bool packet_tree(const gbt_ctx *ctx, const gbt_bvh *b) {
+    return ctx->primary_packets == 1 || (ctx->primary_packets == 2 && b->packet_choice == 1);
+}
+
+// Item descriptors of one frame; acc pointers are set by place().  Items whose
+// tree traces camera rays faster as packets come first (in their given order),
+// so that their paths form one leading range of the queue; the accumulators
+// follow the same order.  The order changes nothing but float summation order.
 int describe(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, std::vector<ItemDev> &hi, uint64_t *total_paths,
              size_t *acc_floats) {
     hi.resize(n);
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    for (int pass = 0; pass < 2; pass++)
+        for (uint32_t i = 0; i < n; i++)
+            if (packet_tree(ctx, items[i].bvh) == (pass == 0)) order.push_back(i);
     uint64_t paths = 0, pix = 0;
-    for (uint32_t i = 0; i < n; i++) {
+    for (uint32_t k = 0; k < n; k++) {
+        const uint32_t i = order[k];
         const gbt_batch_item &it = items[i];
         const gbt_bvh *b = it.bvh;
-        ItemDev &d = hi[i];
+        ItemDev &d = hi[k];
         d.tree.hdr = b->has_nodes4 ? b->d_hdr4 : b->d_hdr;
         d.tree.nodes = b->has_nodes4 ? b->d_nodes4 : b->d_nodes;
         d.tree.recs = b->d_prims;
         d.tree.any_level = ctx->anyhit_last ? it.params.max_depth + 1 : -1;
-        d.tree.pad = 0;
+        d.tree.packets = packet_tree(ctx, b) ? 1 : 0;
         d.prim_mat = b->scene->d_prim_mat;
         d.mats = b->scene->d_mats;
         d.normals = b->scene->d_normals;
@@ -476,8 +491,14 @@ int enqueue_frame(gbt_ctx *ctx, const FrameBufs &fb, const ItemDev *h_items, siz
     } else {
         const RenderState &rs = fb.rs;
         if (rs.cap == 0) return gbt_fail(ctx, GBT_EINVAL, "batch: wavefront form without path buffers");
-        int levels = 0;  // surfaces at depth 0..MaxDepth+1 of the deepest item
-        for (size_t i = 0; i < n_items; i++) levels = std::max(levels, h_items[i].sp.max_depth + 2);
+        int levels = 0;           // surfaces at depth 0..MaxDepth+1 of the deepest item
+        uint64_t packet_paths = 0;  // the leading range of paths whose camera rays go as packets
+        for (size_t i = 0; i < n_items; i++) {
+            levels = std::max(levels, h_items[i].sp.max_depth + 2);
+            if (h_items[i].tree.packets)
+                packet_paths = (uint64_t)h_items[i].path_base + (uint64_t)h_items[i].sp.npix * h_items[i].sp.spp;
+        }
+        if (!cfg.packets || width != 4) packet_paths = 0;
         for (uint64_t g0 = 0; g0 < paths; g0 += rs.cap) {
             const uint32_t count = (uint32_t)std::min<uint64_t>(paths - g0, rs.cap);
             const uint32_t blocks = (count + 255) / 256;
@@ -487,8 +508,20 @@ int enqueue_frame(gbt_ctx *ctx, const FrameBufs &fb, const ItemDev *h_items, siz
             launches++;
             for (int lv = 0; lv < levels; lv++) {
                 const int a = lv & 1;
-                gbt_launch_traverse_multi(ctx, &fb.items->tree, sizeof(ItemDev), width, rs.rays[a], rs.aux[a], rs.hits,
-                                          count, rs.counts + lv, lv, st);
+                // level 0 (every path has its camera ray, in queue order): the wave's leading rays of packet
+                // trees as packets, the rest one per lane
+                const uint32_t np = lv == 0 && packet_paths > g0 ? (uint32_t)std::min<uint64_t>(packet_paths - g0, count) : 0;
+                if (np > 0) {
+                    gbt_launch_traverse_packets_multi(&fb.items->tree, sizeof(ItemDev), rs.rays[0], rs.aux[0], rs.hits,
+                                                      np, ctx->d_error, st);
+                    launches++;
+                }
+                if (np == 0)
+                    gbt_launch_traverse_multi(ctx, &fb.items->tree, sizeof(ItemDev), width, rs.rays[a], rs.aux[a],
+                                              rs.hits, count, rs.counts + lv, lv, st);
+                else if (np < count)
+                    gbt_launch_traverse_multi(ctx, &fb.items->tree, sizeof(ItemDev), width, rs.rays[0] + 2 * (size_t)np,
+                                              rs.aux[0] + 2 * (size_t)np, rs.hits + np, count - np, nullptr, 0, st);
                 k_shade_batch<<<blocks, 256, 0, st>>>(fb.items, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv,
                                                       rs.rays[a ^ 1], rs.aux[a ^ 1], rs.counts + lv + 1,
                                                       (uint32_t)rs.cap);
@@ -515,7 +548,17 @@ gbt_batch_config default_config(const gbt_ctx *ctx) {
     c.fetch_min = 16;
     c.stack = 0;
     c.mode = GBT_BATCH_WAVEFRONT;
+    c.packets = ctx->primary_packets && ctx->primary_tiles ? 1 : 0;
     return c;
+}
+
+// the measured camera-ray packet choice of every item's tree (once per tree)
+int measure_items(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n) {
+    for (uint32_t i = 0; i < n; i++) {
+        int rc = gbt_measure_packets(ctx, items[i].bvh, &items[i].camera, &items[i].params);
+        if (rc) return rc;
+    }
+    return GBT_OK;
 }
 
 // descriptors and the context's buffers for one frame in form cfg
@@ -540,6 +583,10 @@ extern "C" int gbt_render_batch_async(gbt_ctx *ctx, const gbt_batch_item *items,
     const gbt_batch_config c = cfg ? *cfg : default_config(ctx);
     rc = check_config(ctx, c, width);
     if (rc) return rc;
+    if (c.mode == GBT_BATCH_WAVEFRONT && c.packets && width == 4 && ctx->primary_packets == 2) {
+        rc = measure_items(ctx, items, n);
+        if (rc) return rc;
+    }
     std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;
@@ -568,6 +615,10 @@ extern "C" int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uin
     int width;
     int rc = check_items(ctx, items, n, &width);
     if (rc) return rc;
+    if (width == 4 && ctx->primary_packets == 2) {
+        rc = measure_items(ctx, items, n);
+        if (rc) return rc;
+    }
     std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;
@@ -575,10 +626,11 @@ extern "C" int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uin
     rc = setup(ctx, items, n, true, hi, &paths, &accf, &fb);
     if (rc) return rc;
     std::vector<gbt_batch_config> cands;
-    cands.push_back(gbt_batch_config{128, 16, 0, GBT_BATCH_WAVEFRONT});
+    cands.push_back(gbt_batch_config{128, 16, 0, GBT_BATCH_WAVEFRONT, 0});
+    if (width == 4 && ctx->primary_packets) cands.push_back(gbt_batch_config{128, 16, 0, GBT_BATCH_WAVEFRONT, 1});
     for (int b : {64, 128, 256})
         for (int f : {0, 16})
-            for (int s : {0, 1}) cands.push_back(gbt_batch_config{b, f, s, GBT_BATCH_MEGAKERNEL});
+            for (int s : {0, 1}) cands.push_back(gbt_batch_config{b, f, s, GBT_BATCH_MEGAKERNEL, 0});
     double bms = 1e30;
     gbt_batch_config bc = cands[0];
     for (const gbt_batch_config &c : cands) {
@@ -629,6 +681,10 @@ extern "C" int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items,
     rc = check_config(ctx, c, width);
     if (rc) return rc;
     const bool waves = c.mode == GBT_BATCH_WAVEFRONT;
+    if (waves && c.packets && width == 4 && ctx->primary_packets == 2) {
+        rc = measure_items(ctx, items, n);
+        if (rc) return rc;
+    }
     std::vector<ItemDev> hi;
     uint64_t paths;
     size_t accf;

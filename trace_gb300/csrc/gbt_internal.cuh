@@ -158,11 +158,15 @@ struct TreeRef {
     const float4 *nodes;
     const float4 *recs;
     int32_t any_level;  // the level whose rays take an any-hit query (-1: none)
-    int32_t pad;
+    int32_t packets;    // 1: this tree's camera rays trace faster as packets (its measured choice)
 };
 // trees: entry k at byte offset k * stride
-void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays, const float4 *aux,
-                               float4 *hits, uint32_t n, const uint32_t *d_count, int level, cudaStream_t s);
+void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays,
+                               const float4 *aux, float4 *hits, uint32_t n, const uint32_t *d_count, int level,
+                               cudaStream_t s);
+// packets over the camera rays of many 4-wide trees (tree index in aux[2 i + 1].w)
+void gbt_launch_traverse_packets_multi(const TreeRef *trees, size_t stride, const float4 *rays, const float4 *aux,
+                                      float4 *hits, uint32_t n, unsigned int *d_error, cudaStream_t s);
 // 32-ray packets per warp (coherent camera rays) over a 4-wide tree; false when the tree has no 4-wide nodes
 bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,
                                  unsigned int *d_error, cudaStream_t s, unsigned long long *d_counters);
@@ -178,6 +182,9 @@ struct RenderState {
 size_t gbt_render_state_bytes(size_t total, size_t npix);
 void gbt_render_state_bind(void *base, size_t total, size_t npix, RenderState *rs);
 int gbt_render_buffers(gbt_ctx *ctx, size_t total, size_t npix, RenderState *rs);
+// Measures, once per tree, whether camera rays of this view trace faster as packets (bvh->packet_choice
+// 1) or one ray per lane (2); leaves it unmeasured (0) below 65536 camera rays or while profiling.
+int gbt_measure_packets(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p);
 int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p,
                        float *d_rgb);
 // phr.cu

@@ -209,6 +209,46 @@ int gbt_render_buffers(gbt_ctx *ctx, size_t total, size_t npix, RenderState *rs)
     return GBT_OK;
 }
 
+int gbt_render_check(gbt_ctx *ctx, const gbt_render_params *p);
+
+// Times the packet and the one-ray-per-lane kernels on the same camera rays (both leave the same
+// hits) and keeps the faster for this tree.  Synchronises the stream.
+static void measure_packets(gbt_ctx *ctx, gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t count,
+                            const uint32_t *d_count) {
+    cudaStream_t st = ctx->stream;
+    cudaEventRecord(ctx->tune_ev[0], st);
+    gbt_launch_traverse_packets(bvh, rays, hits, count, 1, ctx->d_error, st, nullptr);
+    cudaEventRecord(ctx->tune_ev[1], st);
+    gbt_launch_traverse(bvh, rays, hits, count, d_count, 1, ctx->d_error, st, nullptr);
+    cudaEventRecord(ctx->tune_ev[2], st);
+    float tp = 0.f, ts = 0.f;
+    if (cudaEventSynchronize(ctx->tune_ev[2]) == cudaSuccess &&
+        cudaEventElapsedTime(&tp, ctx->tune_ev[0], ctx->tune_ev[1]) == cudaSuccess &&
+        cudaEventElapsedTime(&ts, ctx->tune_ev[1], ctx->tune_ev[2]) == cudaSuccess)
+        bvh->packet_choice = tp < ts ? 1 : 2;
+    else
+        bvh->packet_choice = 2;
+}
+
+int gbt_measure_packets(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *p) {
+    if (bvh->packet_choice != 0 || ctx->profiling != 0 || !(bvh->has_nodes4 || bvh->arity == 4)) return GBT_OK;
+    int rc = gbt_render_check(ctx, p);
+    if (rc) return rc;
+    const size_t total = (size_t)p->width * p->height * (size_t)p->spp;
+    RenderState rs;
+    GBT_TRY_R(gbt_render_buffers(ctx, total, 0, &rs));
+    const uint32_t count = (uint32_t)rs.cap;  // the first wave, as the renderer's own first frame
+    if (count < (1u << 16)) return GBT_OK;
+    ShadeParams sp = gbt_make_shade_params(p, bvh->scene->n_tri);
+    sp.tiles = ctx->primary_tiles ? 1u : 0u;
+    GBT_CUDA(ctx, cudaMemsetAsync(rs.counts, 0, 64 * sizeof(uint32_t), ctx->stream));
+    k_raygen<<<(count + 255) / 256, 256, 0, ctx->stream>>>(gbt_make_cam(cam), sp, 0, count, rs.rays[0], rs.aux[0],
+                                                             rs.counts);
+    GBT_CUDA(ctx, cudaGetLastError());
+    measure_packets(ctx, bvh, rs.rays[0], rs.hits, count, rs.counts);
+    return gbt_check_device_error(ctx, "measure_packets");
+}
+
 int gbt_render_check(gbt_ctx *ctx, const gbt_render_params *p) {
     if (p->width < 2 || p->height < 2 || p->spp < 1 || p->max_depth < 0 || p->max_depth > 60)
         return gbt_fail(ctx, GBT_EINVAL, "render: width/height >= 2, spp >= 1, 0 <= max_depth <= 60");
@@ -254,18 +294,7 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
             if (lv == 0 && ctx->primary_tiles && four && ctx->primary_packets) {
                 if (ctx->primary_packets == 2 && bvh->packet_choice == 0 && ctx->profiling == 0 && count >= (1u << 16)) {
                     // first render on this tree: time both kernels on this wave's camera rays
-                    cudaEventRecord(ctx->tune_ev[0], st);
-                    gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, nullptr);
-                    cudaEventRecord(ctx->tune_ev[1], st);
-                    gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, nullptr);
-                    cudaEventRecord(ctx->tune_ev[2], st);
-                    float tp = 0.f, ts = 0.f;
-                    if (cudaEventSynchronize(ctx->tune_ev[2]) == cudaSuccess &&
-                        cudaEventElapsedTime(&tp, ctx->tune_ev[0], ctx->tune_ev[1]) == cudaSuccess &&
-                        cudaEventElapsedTime(&ts, ctx->tune_ev[1], ctx->tune_ev[2]) == cudaSuccess)
-                        bvh->packet_choice = tp < ts ? 1 : 2;
-                    else
-                        bvh->packet_choice = 2;
+                    measure_packets(ctx, bvh, rs.rays[a], rs.hits, count, rs.counts + lv);
                     done = true;
                     launches += 1;
                 }

@@ -184,6 +184,134 @@ __global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restri
     flush_work<COUNT>(w, counters);
 }
 
+// One packet walk over a 4-wide tree by a warp of a 128-thread block: every
+// lane takes part (a lane without a ray carries one that misses everything).
+// The warp's stack lives in shared memory.  The walk is k_trace_packet4's
+// (above); that kernel keeps its own inline copy, which ptxas allocates
+// without spills (as a call of this function it spills 20 bytes).
+template <bool COUNT>
+__device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+                                             const float4 *__restrict__ recs, const gbt_dev::Ray &r, gbt_dev::Hit &h,
+                                             unsigned int *err, gbt_dev::Work &w) {
+    constexpr int PSTACK = 96;
+    constexpr uint32_t FULL = 0xffffffffu;
+    __shared__ int2 s_e[4][PSTACK];
+    __shared__ float s_t[4][PSTACK];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float MISS = __int_as_float(0x7f800000);
+    float te;
+    const bool root_hit = gbt_dev::slab(hdr->root_lo[0], hdr->root_lo[1], hdr->root_lo[2], hdr->root_hi[0],
+                                        hdr->root_hi[1], hdr->root_hi[2], r, h.t, te);
+    int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
+    int sp = 0;
+    auto pop = [&]() -> int2 {
+        while (sp > 0) {
+            --sp;
+            const float t = s_t[wp][sp];
+            const int2 e = s_e[wp][sp];
+            if (__any_sync(FULL, t <= h.t * 1.0000005f)) return e;
+        }
+        return make_int2(0, -1);
+    };
+    for (;;) {
+        if (node.y == 0) {
+            if (COUNT && lane == 0) w.nodes++;
+            const float4 *nd = nodes + 8 * (size_t)node.x;
+            float4 lx, hx, ly, hy, lz, hz, rff, cnf;
+            gbt_dev::ldg256(nd, lx, hx);
+            gbt_dev::ldg256(nd + 2, ly, hy);
+            gbt_dev::ldg256(nd + 4, lz, hz);
+            gbt_dev::ldg256(nd + 6, rff, cnf);
+            float t;
+            // per lane entry distance (+0 for -0, so that unsigned min orders them), MISS if missed
+            const float t0 = (__float_as_int(cnf.x) >= 0 && gbt_dev::slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) ? t + 0.f : MISS;
+            const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
+            const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
+            const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
+            gbt_dev::Cand c0, c1, c2, c3;
+            c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
+            c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
+            c2.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t2)));
+            c3.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t3)));
+            c0.e = make_int2(__float_as_int(rff.x), __float_as_int(cnf.x));
+            c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
+            c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
+            c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
+            gbt_dev::cx(c0, c1);
+            gbt_dev::cx(c2, c3);
+            gbt_dev::cx(c0, c2);
+            gbt_dev::cx(c1, c3);
+            gbt_dev::cx(c1, c2);
+            if (c0.t == MISS) {
+                node = pop();
+                continue;
+            }
+            const int np = (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
+            if (sp + np > PSTACK) {
+                if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
+            } else {
+                if (lane == 0) {
+                    int q = sp;
+                    if (c3.t != MISS) { s_e[wp][q] = c3.e; s_t[wp][q] = c3.t; ++q; }
+                    if (c2.t != MISS) { s_e[wp][q] = c2.e; s_t[wp][q] = c2.t; ++q; }
+                    if (c1.t != MISS) { s_e[wp][q] = c1.e; s_t[wp][q] = c1.t; ++q; }
+                }
+                sp += np;
+                __syncwarp();
+            }
+            node = c0.e;
+        } else if (node.y > 0) {
+            if (COUNT && lane == 0) w.prims += (uint32_t)node.y;
+            gbt_dev::leaf(recs, node.x, node.y, r, h);
+            node = pop();
+        } else {
+            break;
+        }
+    }
+    __syncwarp();  // the stack is free for the warp's next walk
+}
+
+__device__ __forceinline__ gbt_dev::Ray missing_ray() {  // a ray that hits nothing keeps a lane in step
+    gbt_dev::Ray r;
+    r.o = make_float3(0.f, 0.f, 0.f);
+    r.d = make_float3(1.f, 1.f, 1.f);
+    r.tmin = 1.f;
+    r.tmax = 0.f;
+    gbt_dev::finish_ray(r);
+    return r;
+}
+
+// The packet traversal over camera rays of many trees (a batched frame, the
+// tree index in aux[2 i + 1].w): a warp walks once per distinct tree among its
+// 32 rays, with the other lanes carrying missing rays.  Hits are (t, u, v, record).
+__global__ void __launch_bounds__(128) k_trace_packet4_multi(const TreeRef *__restrict__ trees, uint32_t stride,
+                                                             const float4 *__restrict__ rays,
+                                                             const float4 *__restrict__ aux, float4 *__restrict__ hits,
+                                                             uint32_t n, unsigned int *err) {
+    const uint32_t id = blockIdx.x * 128 + threadIdx.x;
+    const bool live = id < n;
+    gbt_dev::Work w;
+    const int item = live ? __float_as_int(__ldg(&aux[2 * (size_t)id + 1].w)) : -1;
+    const gbt_dev::Ray mine = live ? gbt_dev::load_ray(rays, id) : missing_ray();
+    gbt_dev::Hit out;
+    uint32_t todo = __ballot_sync(0xffffffffu, live);
+    while (todo) {
+        const int it = __shfl_sync(0xffffffffu, item, __ffs(todo) - 1);
+        const bool in = live && item == it;
+        todo &= ~__ballot_sync(0xffffffffu, in);
+        const TreeRef tr = *reinterpret_cast<const TreeRef *>(reinterpret_cast<const unsigned char *>(trees) +
+                                                              (size_t)it * stride);
+        const gbt_dev::Ray r = in ? mine : missing_ray();
+        gbt_dev::Hit h;
+        h.t = r.tmax;
+        h.u = h.v = 0.f;
+        h.rec = -1;
+        packet_walk4<false>(tr.hdr, tr.nodes, tr.recs, r, h, err, w);
+        if (in) out = h;
+    }
+    if (live) gbt_dev::store_hit(hits, id, out, nullptr, 1);
+}
+
 __device__ __forceinline__ uint32_t lane_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -351,11 +479,11 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_multi(const TreeRef 
             if (want) {
                 const uint32_t id = base + __popc(need & lane_lt());
                 if (id < total) {
-                    rid = id;
-                    r = gbt_dev::load_ray(rays, id);
                     const TreeRef tr = *reinterpret_cast<const TreeRef *>(
                         reinterpret_cast<const unsigned char *>(trees) +
                         (size_t)__float_as_int(__ldg(&aux[2 * (size_t)id + 1].w)) * stride);
+                    rid = id;
+                    r = gbt_dev::load_ray(rays, id);
                     nodes = tr.nodes;
                     recs = tr.recs;
                     any = tr.any_level == level;
@@ -479,8 +607,9 @@ void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, u
     }
 }
 
-void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays, const float4 *aux,
-                               float4 *hits, uint32_t n, const uint32_t *d_count, int level, cudaStream_t s) {
+void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride, int width, const float4 *rays,
+                               const float4 *aux, float4 *hits, uint32_t n, const uint32_t *d_count, int level,
+                               cudaStream_t s) {
     if (n == 0) return;
     static int per_sm[2] = {0, 0};
     const int w = width == 4 ? 1 : 0;
@@ -498,6 +627,12 @@ void gbt_launch_traverse_multi(gbt_ctx *ctx, const TreeRef *trees, size_t stride
                                                                    ctx->d_error, fetch);
     else k_trace_multi<2, GBT_PT_DYN><<<grid, 128, 0, s>>>(trees, (uint32_t)stride, rays, aux, hits, n, d_count, level,
                                                                    ctx->d_error, fetch);
+}
+
+void gbt_launch_traverse_packets_multi(const TreeRef *trees, size_t stride, const float4 *rays, const float4 *aux,
+                                      float4 *hits, uint32_t n, unsigned int *d_error, cudaStream_t s) {
+    if (n == 0) return;
+    k_trace_packet4_multi<<<(n + 127) / 128, 128, 0, s>>>(trees, (uint32_t)stride, rays, aux, hits, n, d_error);
 }
 
 bool gbt_launch_traverse_packets(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, int out_mode,

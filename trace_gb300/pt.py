@@ -195,6 +195,14 @@ class BVH:
         self.ctx.check(self.ctx.L.gbt_bvh_size(self.ctx.h, self.h, C.byref(c)), "bvh_size")
         return c.value
 
+    def set_layout(self, width):
+        """Traversal layout: 4 (a 4-wide view collapsed from the binary tree) or 2 (the binary nodes)."""
+        self.ctx.check(self.ctx.L.gbt_bvh_set_layout(self.ctx.h, self.h, int(width)), "bvh_set_layout")
+
+    def set_packets(self, choice):
+        """Camera rays of a 4-wide tree: 0 measure on the next render, 1 packets, 2 one ray per lane."""
+        self.ctx.check(self.ctx.L.gbt_bvh_set_packets(self.ctx.h, self.h, int(choice)), "bvh_set_packets")
+
     def counts(self):
         out = np.zeros(4, np.int64)
         self.ctx.check(self.ctx.L.gbt_bvh_counts(self.ctx.h, self.h, _p(out)), "bvh_counts")
