@@ -220,8 +220,11 @@ def run_reference(args, ws, rank):
 def run_batch_workload(args):
     """64 scenes of log-uniform size in [1k, 2M] triangles (seed 3), each a soup or
     an fBm terrain patch, 512x512, 16 spp, depth 4: the per-scene wavefront loop
-    (gbt_render_async per scene) against one persistent launch over all scenes,
-    and that launch replayed from a CUDA graph.  Mrays/s counts every traced ray."""
+    (gbt_render_async per scene) against the batched frame over all scenes (the
+    autotuned form, and each form), that frame replayed from a CUDA graph, and the
+    frame with every LBVH rebuilt first: per scene (rebuild, collapse into the
+    4-wide view, render) against one graph holding the rebuilds, the collapses and
+    the batched frame.  Mrays/s counts every traced ray."""
     import torch
 
     from trace_gb300 import _lib, pt, scenes
@@ -245,14 +248,17 @@ def run_batch_workload(args):
     st = _lib.RenderStats()
 
     def timed(mode, steps, cfg=None):
+        return timed_with(b, mode, steps, cfg)
+
+    def timed_with(obj, mode, steps, cfg=None):
         for _ in range(args.warmup):
-            b.render(mode, cfg)
+            obj.render(mode, cfg)
         ctx.sync()
         ctx.check(ctx.L.gbt_render_last_stats(ctx.h, C.byref(st)))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            b.render(mode, cfg)
+            obj.render(mode, cfg)
         e1.record(stream)
         ctx.sync()
         ctx.check(ctx.L.gbt_render_last_stats(ctx.h, C.byref(st)))
@@ -272,6 +278,25 @@ def run_batch_workload(args):
     batched = [b.read(i) for i in range(b.n)]
     b.make_graph(rebuild=False, cfg=cfg)
     ms_graph, rays_graph = timed("graph", steps)
+    b.close_graph()
+    # frames that rebuild every LBVH first
+    choices = [g.packets() for g in bvhs]
+
+    class PlainRebuild:
+        def render(self, mode=None, cfg=None):
+            for g in bvhs:
+                ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, g.h), "rebuild")
+            for g, c in zip(bvhs, choices):
+                g.set_layout(4)
+                g.set_packets(c)  # the measured choice stays: rebuilds over unchanged vertices
+            b.render("plain")
+
+    pr = PlainRebuild()
+    ms_plain_rb, _ = timed_with(pr, "plain", steps)
+    b.make_graph(rebuild=True, cfg=cfg)
+    ms_graph_rb, _ = timed("graph", steps)
+    rebuilt = [b.read(i) for i in range(b.n)]
+    diff_rb = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, rebuilt))
     diff = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, batched))
     rmse = float(np.sqrt(np.mean([np.mean((x - y) ** 2) for x, y in zip(plain, batched)])))
     line = {"metric": "Mrays/s (64-scene batch)", "unit": "Mrays/s", "workload": "batch%d_512x512_spp16_depth4" % count,
@@ -283,6 +308,11 @@ def run_batch_workload(args):
                         "autotune_best_ms": tune_ms},
             "forms": forms,
             "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},
+            "with_lbvh_rebuilds": {
+                "plain_ms_per_frame": ms_plain_rb, "graph_ms_per_frame": ms_graph_rb,
+                "plain_value": rays_plain / ms_plain_rb / 1e3, "graph_value": rays_plain / ms_graph_rb / 1e3,
+                "speedup_graph_vs_plain": ms_plain_rb / ms_graph_rb,
+                "max_abs_diff_graph_vs_plain": diff_rb},
             "speedup_batched_vs_plain": (rays_batch / ms_batch) / (rays_plain / ms_plain),
             "images": {"max_abs_diff_batched_vs_plain": diff, "rmse_batched_vs_plain": rmse},
             "scene_generation_s": gen_s}

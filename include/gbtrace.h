@@ -178,6 +178,7 @@ int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width);
  * (the default) renders and batched frames follow this choice; hits are the
  * same either way.  No counterpart in the reference. */
 int gbt_bvh_set_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t choice);
+int gbt_bvh_get_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t *choice);
 
 int gbt_bvh_cost(gbt_ctx *ctx, gbt_bvh *bvh, double *cost); /* bvh.go:46-48 BVH.Cost */
 int gbt_bvh_size(gbt_ctx *ctx, gbt_bvh *bvh, int64_t *size); /* bvh.go:50-52 BVH.Size */
@@ -275,7 +276,8 @@ int gbt_render_batch_plain_async(gbt_ctx *ctx, const gbt_batch_item *items, uint
 int gbt_batch_autotune(gbt_ctx *ctx, const gbt_batch_item *items, uint32_t n, gbt_batch_config *best,
                        double *best_ms);
 /* A CUDA graph of one batched frame: optionally the in-place LBVH rebuild of
- * every item (which switches their traversal to the binary nodes), then the
+ * every item (for items in the 4-wide layout followed by the collapse into
+ * their 4-wide view, a conditional WHILE node over its levels), then the
  * accumulator clear, the frame in form cfg and the resolve.  The graph owns
  * its descriptors, accumulators and path buffers; with rebuilds it also holds
  * the context's scratch, which cannot grow (larger builds fail with

@@ -182,3 +182,54 @@ def test_forced_packets_option(ctx):
     finally:
         ctx.set_option("primary_packets", 2)
         b.close()
+
+
+@pytest.mark.parametrize("layout", [4, 2])
+def test_graph_rebuild_follows_moved_vertices(ctx, layout):
+    """A graph with rebuilds renders the scenes as they are at replay: after the vertices move
+    (gbt_scene_update_async), one replay gives the images of freshly built trees.  In the
+    4-wide layout the replay also collapses each rebuilt tree (a conditional graph node)."""
+    ss = scenes.batch(count=3, lo=3_000, hi=30_000, seed=8, width=96, height=64, spp=4, max_depth=3)
+    dss, bvhs, cams, params = [], [], [], []
+    for k, s in enumerate(ss):
+        ds = pt.DeviceScene.from_dict(ctx, s)
+        g = pt.DefaultLBVH(ds)
+        g.set_layout(layout)
+        dss.append(ds)
+        bvhs.append(g)
+        cams.append(s["camera"])
+        p = dict(s["render"])
+        p["seed"] = 60 + k
+        params.append(p)
+    b = pt.Batch(ctx, bvhs, cams, params)
+    bufs = []
+    try:
+        b.make_graph(rebuild=True, cfg=WAVE)
+        b.render("graph")
+        before = [b.read(i) for i in range(b.n)]
+        rng = np.random.default_rng(1)
+        moved = []
+        for ds, s in zip(dss, ss):
+            v = (s["verts"] + rng.normal(0, 0.01, s["verts"].shape)).astype(np.float32)
+            d = ctx.alloc(v.nbytes)
+            ctx.h2d(d, v)
+            bufs.append(d)
+            ctx.check(ctx.L.gbt_scene_update_async(ctx.h, ds.h, d), "scene_update")
+            moved.append(v)
+        b.render("graph")
+        after = [b.read(i) for i in range(b.n)]
+        assert any(np.max(np.abs(x - y)) > 1e-3 for x, y in zip(before, after))
+        # fresh trees over the moved vertices, rendered one by one
+        for i, (s, v) in enumerate(zip(ss, moved)):
+            s2 = dict(s)
+            s2["verts"] = v
+            g = pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s2))
+            g.set_layout(layout)
+            p = params[i]
+            img, _ = g.render(s["camera"], p["width"], p["height"], p["spp"], p["max_depth"], p["miss_mode"],
+                              p.get("miss_color", (0, 0, 0)), p["seed"])
+            np.testing.assert_allclose(after[i], img, rtol=1e-4, atol=1e-5)
+    finally:
+        b.close()
+        for d in bufs:
+            ctx.free(d)

@@ -25,6 +25,7 @@ EXPORTS = [
     "gbt_trace", "gbt_trace_async", "gbt_render", "gbt_render_async", "gbt_render_last_stats",
     "gbt_device_alloc", "gbt_device_free", "gbt_copy_h2d_async", "gbt_copy_d2h_async",
     "gbt_sort_morton_pairs_noalloc", "gbt_bvh_set_layout", "gbt_bvh_set_packets",
+    "gbt_bvh_get_packets",
     "gbt_render_batch_async", "gbt_render_batch_plain_async", "gbt_batch_autotune", "gbt_batch_graph_create",
     "gbt_graph_launch", "gbt_graph_destroy",
     "gbt_adjoint_forward_async", "gbt_adjoint_backward_async", "gbt_l2_loss_async",
@@ -121,6 +122,7 @@ def load():
         "gbt_sort_morton_pairs_noalloc": ([P, P, P, P, u32], C.c_int),
         "gbt_bvh_set_layout": ([P, P, i32], C.c_int),
         "gbt_bvh_set_packets": ([P, P, i32], C.c_int),
+        "gbt_bvh_get_packets": ([P, P, P], C.c_int),
         "gbt_render_batch_async": ([P, P, u32, P], C.c_int),
         "gbt_render_batch_plain_async": ([P, P, u32], C.c_int),
         "gbt_batch_autotune": ([P, P, u32, P, C.POINTER(d)], C.c_int),

@@ -131,6 +131,7 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     for (auto &e : ctx->tune_ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     delete ctx;
     return GBT_OK;
 }
@@ -357,6 +358,12 @@ extern "C" int gbt_bvh_set_layout(gbt_ctx *ctx, gbt_bvh *bvh, int32_t width) {
 extern "C" int gbt_bvh_set_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t choice) {
     if (!ctx || !bvh || choice < 0 || choice > 2) return GBT_EINVAL;
     bvh->packet_choice = choice;
+    return GBT_OK;
+}
+
+extern "C" int gbt_bvh_get_packets(gbt_ctx *ctx, gbt_bvh *bvh, int32_t *choice) {
+    if (!ctx || !bvh || !choice) return GBT_EINVAL;
+    *choice = bvh->packet_choice;
     return GBT_OK;
 }
 

@@ -669,14 +669,10 @@ extern "C" int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items,
     int width;
     int rc = check_items(ctx, items, n, &width);
     if (rc) return rc;
-    if (rebuild_lbvh) {
+    if (rebuild_lbvh)
         for (uint32_t i = 0; i < n; i++)
             if (items[i].bvh->kind != GBT_BVH_LBVH)
                 return gbt_fail(ctx, GBT_EINVAL, "batch graph: rebuilding needs LBVH items");
-        // rebuilds replace the binary nodes, so the frame traverses those
-        for (uint32_t i = 0; i < n; i++) items[i].bvh->has_nodes4 = 0;
-        width = 2;
-    }
     const gbt_batch_config c = cfg ? *cfg : default_config(ctx);
     rc = check_config(ctx, c, width);
     if (rc) return rc;
@@ -713,16 +709,25 @@ extern "C" int gbt_batch_graph_create(gbt_ctx *ctx, const gbt_batch_item *items,
     if (cudaMallocHost(&g->pinned_items, hi.size() * sizeof(ItemDev)) != cudaSuccess)
         return fail(gbt_fail(ctx, GBT_ENOMEM, "batch graph: pinned descriptors"));
     std::memcpy(g->pinned_items, hi.data(), hi.size() * sizeof(ItemDev));
-    // grow the scratch the captured rebuilds use before capturing; it may not move while the graph lives
+    // grow the scratch the captured rebuilds (and collapses into the 4-wide views) use before
+    // capturing; it may not move while the graph lives
     for (uint32_t i = 0; rebuild_lbvh && i < n; i++) {
+        size_t need = gbt_lbvh_scratch_bytes(items[i].bvh->n_prim), need4 = 0;
+        if (width == 4) {
+            rc = gbt_collapse4_reserve(ctx, items[i].bvh, &need4);
+            if (rc) return fail(rc);
+        }
         void *scr;
-        rc = gbt_scratch(ctx, gbt_lbvh_scratch_bytes(items[i].bvh->n_prim), &scr);
+        rc = gbt_scratch(ctx, std::max(need, need4), &scr);
         if (rc) return fail(rc);
     }
     cudaStream_t st = ctx->stream;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return fail(gbt_fail(ctx, GBT_ECUDA, "batch graph: begin capture"));
-    for (uint32_t i = 0; rebuild_lbvh && i < n && !rc; i++) rc = gbt_lbvh_enqueue(ctx, items[i].bvh);
+    for (uint32_t i = 0; rebuild_lbvh && i < n && !rc; i++) {
+        rc = gbt_lbvh_enqueue(ctx, items[i].bvh);
+        if (!rc && width == 4) rc = gbt_collapse4_enqueue(ctx, items[i].bvh);
+    }
     if (!rc) rc = enqueue_frame(ctx, fb, static_cast<const ItemDev *>(g->pinned_items), hi.size(), paths, accf, c, width);
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &graph);

@@ -32,13 +32,11 @@ __device__ __forceinline__ float area(const Child &c) {
     return w * h + w * d + h * d;
 }
 
-// One level: every queued binary node becomes the 4-wide node already assigned to it.
-__global__ void k_collapse_level(const float4 *__restrict__ bin, const int2 *__restrict__ q_in,
-                                 const uint32_t *__restrict__ n_in, int2 *__restrict__ q_out, uint32_t *n_out,
-                                 uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_in) return;
-    const int2 e = q_in[i];  // (binary node, 4-wide node)
+// A queued binary node becomes the 4-wide node already assigned to it; its
+// inner children are queued for the next level.
+__device__ void collapse_one(const float4 *__restrict__ bin, int2 e, int2 *__restrict__ q_out, uint32_t *n_out,
+                             uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
+    // e = (binary node, 4-wide node)
     Child c[4];
     load_slots(bin, e.x, c[0], c[1]);
     int nc = 0;
@@ -99,8 +97,42 @@ __global__ void k_collapse_level(const float4 *__restrict__ bin, const int2 *__r
     reinterpret_cast<int4 *>(nd)[7] = make_int4(cnt[0], cnt[1], cnt[2], cnt[3]);
 }
 
-__global__ void k_collapse_root(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q, uint32_t *n_q,
-                                uint32_t *n_nodes4) {
+// One level, one thread per queued node.
+__global__ void k_collapse_level(const float4 *__restrict__ bin, const int2 *__restrict__ q_in,
+                                 const uint32_t *__restrict__ n_in, int2 *__restrict__ q_out, uint32_t *n_out,
+                                 uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *n_in) collapse_one(bin, q_in[i], q_out, n_out, n_nodes4, out, cap, err);
+}
+
+// Counters of the graph form: [0], [1] the two queues' sizes, [2] 4-wide nodes, [3] the input
+// queue of the current level, [4] levels done.
+constexpr uint32_t MAX_LEVELS = 4096;  // a tree deeper than this is reported, not walked
+
+// One level of the graph form over a fixed grid: the input queue is ctr[3]'s.
+__global__ void k_collapse_level_gs(const float4 *__restrict__ bin, int2 *q0, int2 *q1, uint32_t *ctr,
+                                    float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
+    const uint32_t par = ctr[3];
+    const uint32_t n = ctr[par];
+    const int2 *q_in = par ? q1 : q0;
+    int2 *q_out = par ? q0 : q1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        collapse_one(bin, q_in[i], q_out, ctr + (par ^ 1), ctr + 2, out, cap, err);
+}
+
+// After a level: the output queue becomes the input, and the loop goes on while it is non-empty.
+__global__ void k_collapse_advance(uint32_t *ctr, cudaGraphConditionalHandle loop, unsigned int *err) {
+    const uint32_t par = ctr[3], next = par ^ 1;
+    ctr[par] = 0;
+    ctr[3] = next;
+    const uint32_t levels = ++ctr[4];
+    const bool more = ctr[next] > 0;
+    if (more && levels >= MAX_LEVELS) atomicOr(err, GBT_DEVERR_CAPACITY);
+    cudaGraphSetConditional(loop, more && levels < MAX_LEVELS ? 1u : 0u);
+}
+
+__device__ void k_collapse_root_body(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q, uint32_t *n_q,
+                                     uint32_t *n_nodes4) {
     *hdr4 = *hdr;
     if (hdr->root_cnt == 0) {  // an inner root becomes 4-wide node 0
         q[0] = make_int2(hdr->root_ref, 0);
@@ -113,15 +145,23 @@ __global__ void k_collapse_root(const BvhHeader *__restrict__ hdr, BvhHeader *hd
     }
 }
 
+__global__ void k_collapse_root(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q, uint32_t *n_q,
+                                uint32_t *n_nodes4) {
+    k_collapse_root_body(hdr, hdr4, q, n_q, n_nodes4);
+}
+
+__global__ void k_collapse_root_graph(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q0, uint32_t *ctr,
+                                      cudaGraphConditionalHandle loop) {
+    k_collapse_root_body(hdr, hdr4, q0, ctr + 0, ctr + 2);
+    ctr[1] = 0;
+    ctr[3] = 0;
+    ctr[4] = 0;
+    cudaGraphSetConditional(loop, ctr[0] > 0 ? 1u : 0u);
+}
+
 }  // namespace
 
-int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
-    if (bvh->arity != 2) return GBT_OK;
-    cudaStream_t st = ctx->stream;
-    BvhHeader h;
-    GBT_CUDA(ctx, cudaMemcpyAsync(&h, bvh->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
-    GBT_CUDA(ctx, cudaStreamSynchronize(st));
-    const uint32_t cap = h.n_nodes + 1;  // a 4-wide tree never has more nodes than the binary one
+static int reserve4(gbt_ctx *ctx, gbt_bvh *bvh, uint32_t cap) {
     if (bvh->nodes4_cap < cap) {
         cudaFree(bvh->d_nodes4);
         bvh->d_nodes4 = nullptr;
@@ -136,8 +176,22 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
         cudaGetLastError();
         return gbt_fail(ctx, GBT_ENOMEM, "collapse: header allocation");
     }
+    return GBT_OK;
+}
+
+static size_t queue_bytes(uint32_t cap) { return gbt_align((size_t)cap * sizeof(int2)); }
+
+int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
+    if (bvh->arity != 2) return GBT_OK;
+    cudaStream_t st = ctx->stream;
+    BvhHeader h;
+    GBT_CUDA(ctx, cudaMemcpyAsync(&h, bvh->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    const uint32_t cap = h.n_nodes + 1;  // a 4-wide tree never has more nodes than the binary one
+    int rc0 = reserve4(ctx, bvh, cap);
+    if (rc0) return rc0;
     // queues (two halves), counters
-    size_t qbytes = gbt_align((size_t)cap * sizeof(int2));
+    size_t qbytes = queue_bytes(cap);
     void *scr = nullptr;
     int rc = gbt_scratch(ctx, 2 * qbytes + 256, &scr);
     if (rc) return rc;
@@ -157,5 +211,65 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
         par ^= 1;
     }
     bvh->has_nodes4 = 1;
+    return GBT_OK;
+}
+
+int gbt_collapse4_reserve(gbt_ctx *ctx, gbt_bvh *bvh, size_t *scratch_bytes) {
+    *scratch_bytes = 0;
+    if (bvh->arity != 2) return GBT_OK;
+    BvhHeader h;
+    GBT_CUDA(ctx, cudaMemcpyAsync(&h, bvh->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const uint32_t cap = h.n_nodes + 1;  // rebuilds over the same scene keep the node count
+    int rc = reserve4(ctx, bvh, cap);
+    if (rc) return rc;
+    *scratch_bytes = 2 * queue_bytes(cap) + 256;
+    return GBT_OK;
+}
+
+int gbt_collapse4_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
+    if (bvh->arity != 2) return GBT_OK;
+    cudaStream_t st = ctx->stream;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    GBT_CUDA(ctx, cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+    if (cs != cudaStreamCaptureStatusActive) return gbt_fail(ctx, GBT_EINVAL, "collapse: enqueue outside a capture");
+    const uint32_t cap = bvh->nodes4_cap;
+    if (cap == 0 || !bvh->d_hdr4) return gbt_fail(ctx, GBT_EINVAL, "collapse: view not reserved");
+    const size_t qbytes = queue_bytes(cap);
+    void *scr = nullptr;
+    int rc = gbt_scratch(ctx, 2 * qbytes + 256, &scr);
+    if (rc) return rc;
+    unsigned char *sb = static_cast<unsigned char *>(scr);
+    int2 *q0 = reinterpret_cast<int2 *>(sb), *q1 = reinterpret_cast<int2 *>(sb + qbytes);
+    uint32_t *ctr = reinterpret_cast<uint32_t *>(sb + 2 * qbytes);
+    cudaGraphConditionalHandle loop;
+    GBT_CUDA(ctx, cudaGraphConditionalHandleCreate(&loop, g, 0, cudaGraphCondAssignDefault));
+    k_collapse_root_graph<<<1, 1, 0, st>>>(bvh->d_hdr, bvh->d_hdr4, q0, ctr, loop);
+    GBT_CUDA(ctx, cudaGetLastError());
+    // the WHILE node after the root, its body captured on the side stream
+    GBT_CUDA(ctx, cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    GBT_CUDA(ctx, cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    GBT_CUDA(ctx, cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    if (!ctx->side) GBT_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+    GBT_CUDA(ctx, cudaStreamBeginCaptureToGraph(ctx->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    k_collapse_level_gs<<<(unsigned)ctx->num_sms * 4, 128, 0, ctx->side>>>(bvh->d_nodes, q0, q1, ctr, bvh->d_nodes4, cap,
+                                                                          ctx->d_error);
+    k_collapse_advance<<<1, 1, 0, ctx->side>>>(ctr, loop, ctx->d_error);
+    const cudaError_t le = cudaGetLastError();
+    cudaGraph_t captured = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(ctx->side, &captured);
+    if (le != cudaSuccess || ee != cudaSuccess)
+        return gbt_fail(ctx, GBT_ECUDA, std::string("collapse: body capture: ") +
+                                            cudaGetErrorString(le != cudaSuccess ? le : ee));
     return GBT_OK;
 }

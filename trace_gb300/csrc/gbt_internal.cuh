@@ -45,7 +45,8 @@ struct gbt_ctx {
     // batched rendering (batch.cu): item descriptors + accumulators, autotuned launch config
     void *bstate = nullptr;
     size_t bstate_bytes = 0;
-    gbt_batch_config batch_cfg{128, 16, 0};
+    gbt_batch_config batch_cfg{128, 16, 0, GBT_BATCH_WAVEFRONT, 0};
+    cudaStream_t side = nullptr;  // captures the bodies of conditional graph nodes (created on first use)
     int batch_tuned = 0;
     // traversal kernel: 0 persistent with dynamic ray fetch (default), 1 one thread per ray,
     // 2 persistent without mid-ray refills (GBT_TRAVERSAL=simple|ww at context creation)
@@ -121,6 +122,11 @@ struct gbt_bvh {
 
 // collapse.cu
 int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh);
+// For graph capture: gbt_collapse4_reserve allocates the 4-wide view of a tree of this size and
+// returns the scratch bytes gbt_collapse4_enqueue needs; gbt_collapse4_enqueue (only while the
+// context's stream is capturing) records the collapse as a conditional WHILE node over its levels.
+int gbt_collapse4_reserve(gbt_ctx *ctx, gbt_bvh *bvh, size_t *scratch_bytes);
+int gbt_collapse4_enqueue(gbt_ctx *ctx, gbt_bvh *bvh);
 // cost.cu: BVH.Cost of the tree as built
 int gbt_cost_device(gbt_ctx *ctx, gbt_bvh *bvh, double *out);
 

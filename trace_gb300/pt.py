@@ -203,6 +203,11 @@ class BVH:
         """Camera rays of a 4-wide tree: 0 measure on the next render, 1 packets, 2 one ray per lane."""
         self.ctx.check(self.ctx.L.gbt_bvh_set_packets(self.ctx.h, self.h, int(choice)), "bvh_set_packets")
 
+    def packets(self):
+        c = C.c_int32()
+        self.ctx.check(self.ctx.L.gbt_bvh_get_packets(self.ctx.h, self.h, C.byref(c)), "bvh_get_packets")
+        return c.value
+
     def counts(self):
         out = np.zeros(4, np.int64)
         self.ctx.check(self.ctx.L.gbt_bvh_counts(self.ctx.h, self.h, _p(out)), "bvh_counts")
@@ -285,10 +290,16 @@ class Batch:
         return best, ms.value
 
     def make_graph(self, rebuild=False, cfg=None):
+        self.close_graph()
         g = C.c_void_p()
         self.ctx.check(self.ctx.L.gbt_batch_graph_create(self.ctx.h, self.items, self.n, C.byref(cfg) if cfg else None,
                                                          1 if rebuild else 0, C.byref(g)), "graph create")
         self.graph = g
+
+    def close_graph(self):
+        if self.graph:
+            self.ctx.L.gbt_graph_destroy(self.graph)
+            self.graph = None
 
     def read(self, i):
         d, h, w = self.images[i]
