@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "gbt_internal.cuh"
+#include "phr_exact.cuh"
 
 namespace {
 
@@ -56,7 +57,7 @@ struct PNode {
 struct PhrGlobals {
     uint32_t pnode_ctr, rec_ctr;
     int32_t root;
-    uint32_t pad;
+    uint32_t screen_bad;  // 1: some box coordinate is outside the float32 screening range
     uint32_t job_ctr[2], pool_ctr[2], max_n[2];
     unsigned long long build_cost;  // sizes of the cuts handed to Split (phr.go:214)
 };
@@ -75,14 +76,7 @@ __device__ __forceinline__ double surface(const float *lo, const float *hi) {
     return __dadd_rn(__dadd_rn(a, b), c);
 }
 
-__device__ __forceinline__ double bary(const AuxNode &a, int axis) {
-    return __dmul_rn(__dadd_rn((double)a.lo[axis], (double)a.hi[axis]), 0.5);
-}
 
-__device__ __forceinline__ unsigned long long dbl_key(double d) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
-}
 
 struct BoxAgg {
     float lo[3], hi[3];
@@ -218,6 +212,17 @@ __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__r
     me.count = run[lr.y + 1] - run[lr.x];
 }
 
+// Whether every box coordinate lies in the float32 screening range (phr_exact.cuh);
+// the boxes of every cut and of every union of cut nodes are made of these.
+__global__ void k_phr_screen(const AuxNode *__restrict__ aux, uint32_t n_aux, PhrGlobals *g) {
+    bool ok = true;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_aux; i += gridDim.x * blockDim.x) {
+        const AuxNode &a = aux[i];
+        for (int k = 0; k < 3; k++) ok = ok && gbt_phr::phr_screen_ok(a.lo[k]) && gbt_phr::phr_screen_ok(a.hi[k]);
+    }
+    if (__any_sync(0xffffffffu, !ok) && (threadIdx.x & 31) == 0) atomicOr(&g->screen_bad, 1u);
+}
+
 // ---------------------------------------------------------------------------
 // initial cut: FIFO breadth-first expansion with the MAX_CUT_SIZE cap
 // ---------------------------------------------------------------------------
@@ -338,7 +343,9 @@ __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t
     uint32_t P = pow2_at_least(n);
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
         if (i < n) {
-            s.skey[i] = dbl_key(bary(aux[in[i]], axis));
+            // the float64 barycenter (lo + hi) * 0.5, computed exactly from the float32 bounds
+            const AuxNode &x = aux[in[i]];
+            s.skey[i] = gbt_phr::key_of_bits(gbt_phr::bary_bits(x.lo[axis], x.hi[axis]));
         } else {
             s.skey[i] = ~0ULL;
         }
@@ -369,6 +376,93 @@ __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t
     __syncthreads();
 }
 
+// The same sort for one-warp blocks and n <= 256: a bitonic network over
+// 32 * E (key, position) pairs held in registers, E consecutive ones per lane;
+// partners within a lane (stride J < E) swap in registers, partners in other
+// lanes are read through shuffles.
+template <int E, int J>
+__device__ __forceinline__ void bitonic_in_lane(unsigned long long (&key)[E], uint32_t (&val)[E], uint32_t lane,
+                                                uint32_t k) {
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const int p = e ^ J;
+        if (p > e) {
+            const bool asc = ((lane * E + e) & k) == 0;
+            const bool gt = key[e] > key[p] || (key[e] == key[p] && val[e] > val[p]);
+            if (gt == asc) {
+                const unsigned long long tk = key[e];
+                key[e] = key[p];
+                key[p] = tk;
+                const uint32_t tv = val[e];
+                val[e] = val[p];
+                val[p] = tv;
+            }
+        }
+    }
+}
+
+template <int E>
+__device__ void warp_sort_axis_e(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
+                                 uint32_t *out) {
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long key[E];
+    uint32_t val[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const uint32_t i = lane * E + e;
+        if (i < n) {
+            const AuxNode &x = aux[in[i]];
+            key[e] = gbt_phr::key_of_bits(gbt_phr::bary_bits(x.lo[axis], x.hi[axis]));
+        } else {
+            key[e] = ~0ULL;  // padding sorts last
+        }
+        val[e] = i;
+    }
+    for (uint32_t k = 2; k <= 32u * E; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            if (j >= (uint32_t)E) {
+                const int lj = (int)(j / E);
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const unsigned long long pk = __shfl_xor_sync(0xffffffffu, key[e], lj);
+                    const uint32_t pv = __shfl_xor_sync(0xffffffffu, val[e], lj);
+                    const uint32_t i = lane * E + e;
+                    const bool asc = (i & k) == 0, lower = (i & j) == 0;
+                    const bool gt = key[e] > pk || (key[e] == pk && val[e] > pv);
+                    // the lower position keeps the smaller pair when ascending, the larger otherwise
+                    if (lower ? (gt == asc) : (gt != asc)) {
+                        key[e] = pk;
+                        val[e] = pv;
+                    }
+                }
+            } else if (j == 4) {
+                bitonic_in_lane<E, (E > 4 ? 4 : 0)>(key, val, lane, k);
+            } else if (j == 2) {
+                bitonic_in_lane<E, (E > 2 ? 2 : 0)>(key, val, lane, k);
+            } else {
+                bitonic_in_lane<E, (E > 1 ? 1 : 0)>(key, val, lane, k);
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        const uint32_t i = lane * E + e;
+        if (i < n) out[i] = in[val[e]];
+    }
+    __syncwarp();
+}
+
+// stable_sort_axis for a one-warp block: registers up to 256 nodes, else the
+// shared-scratch network.
+__device__ void warp_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
+                               uint32_t *out, const Scratch &s) {
+    if (n <= 32) warp_sort_axis_e<1>(aux, in, n, axis, out);
+    else if (n <= 64) warp_sort_axis_e<2>(aux, in, n, axis, out);
+    else if (n <= 128) warp_sort_axis_e<4>(aux, in, n, axis, out);
+    else if (n <= 256) warp_sort_axis_e<8>(aux, in, n, axis, out);
+    else stable_sort_axis(aux, in, n, axis, out, s);
+}
+
 struct SahResult {
     double cost;
     uint32_t split;  // 0: not splitting is cheapest
@@ -376,9 +470,13 @@ struct SahResult {
 };
 
 // minCost (phr.go:414-459) over the order `ord`.
+// With `screen`, every split position's cost is first taken in float32 and
+// only positions within the screening slack of the least float32 cost are
+// evaluated in float64 (phr_exact.cuh): the float64 minimum is among them, so
+// the result is the same.
 __device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n, const float *clo,
                               const float *chi, const Scratch &s, BoxAgg *s_tmp, BoxAgg *s_rank, double *s_cost,
-                              uint32_t *s_idx) {
+                              uint32_t *s_idx, bool screen, double *s_nosplit) {
     const int t = threadIdx.x;
     const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
     const uint32_t a = min(n, t * chunk), b = min(n, a + chunk);
@@ -414,9 +512,28 @@ __device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *o
     }
     __syncthreads();
     // costs for every split position, first minimum wins
+    auto cost32 = [&](uint32_t i) {
+        const float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
+        const float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
+        return __fadd_rn(__fmul_rn(gbt_phr::surface32(rl, rh), gbt_phr::count_f32(s.rc[i])),
+                         __fmul_rn(gbt_phr::surface32(ll, lh), gbt_phr::count_f32(s.lc[i])));
+    };
+    float limit = INFINITY;  // positions with a float32 cost above this cannot be the minimum
+    if (screen) {
+        float m = INFINITY;
+        for (uint32_t i = 1 + t; i < n; i += blockDim.x) m = fminf(m, cost32(i));
+        for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        float *s_m = reinterpret_cast<float *>(s_cost);
+        if ((t & 31) == 0) s_m[t >> 5] = m;
+        __syncthreads();
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fminf(m, s_m[w]);
+        __syncthreads();
+        limit = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
+    }
     double best = INFINITY;
     uint32_t bi = 0xffffffffu;
     for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
+        if (screen && !(cost32(i) <= limit)) continue;
         float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
         float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
         double rcost = __dmul_rn(surface(rl, rh), (double)s.rc[i]);
@@ -426,6 +543,8 @@ __device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *o
             bi = i;
         }
     }
+    // the cost of not splitting, the same for every axis: taken once per cut (NaN until then)
+    if (t == 0 && !(*s_nosplit >= 0.0)) *s_nosplit = __dmul_rn(surface(clo, chi), (double)s.rc[0]);
     s_cost[t] = best;
     s_idx[t] = bi;
     __syncthreads();
@@ -441,8 +560,7 @@ __device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *o
         __syncthreads();
     }
     SahResult r;
-    uint32_t total = s.rc[0];
-    double nosplit = __dmul_rn(surface(clo, chi), (double)total);
+    const double nosplit = *s_nosplit;
     double bc = s_cost[0];
     uint32_t bidx = s_idx[0];
     __syncthreads();
@@ -493,6 +611,7 @@ struct LevelArgs {
     float4 *recs;
     PNode *pn;
     const double *thr;
+    const float *thr_lo, *thr_hi;  // thr * (1 -+ 2^-19) in float32: the screening band
     const PJob *jobs_in;
     PJob *jobs_out;
     const uint32_t *pool_in;
@@ -526,10 +645,11 @@ __device__ void attach(const LevelArgs &A, int32_t parent, int32_t slot, int32_t
 // run with one-warp blocks (BS = 32), so a job costs warp barriers only and 32
 // jobs are resident per SM.
 template <int BS>
-__global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
+__global__ void __launch_bounds__(BS, BS == 32 ? 32 : 1) k_phr_level(LevelArgs A) {
     __shared__ BoxAgg s_tmp[BS / 32];
     __shared__ BoxAgg s_rank[BS];
     __shared__ double s_cost[BS];
+    __shared__ double s_nosplit;
     __shared__ uint32_t s_idx[BS];
     __shared__ uint32_t s_u[32];
     __shared__ Cut s_cuts[4];
@@ -538,6 +658,9 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
     const int in = A.parity, out = A.parity ^ 1;
     const uint32_t n_jobs = A.g->job_ctr[in];
     Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
+    const bool screen = A.g->screen_bad == 0;
+    unsigned long long blk_build_cost = 0;  // thread 0's sums over this block's jobs
+    uint32_t blk_max_n = 0;
     for (uint32_t j = blockIdx.x; j < n_jobs; j += gridDim.x) {
         const PJob job = A.jobs_in[j];
         if (job.n > A.nmax) {
@@ -597,7 +720,7 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
             for (int i = 0; i < nc; i++)
                 if (s_cuts[i].n > mx) { mx = s_cuts[i].n; mi = i; }
             if (mx <= 1) break;
-            if (threadIdx.x == 0) atomicAdd(&A.g->build_cost, (unsigned long long)mx);
+            if (threadIdx.x == 0) blk_build_cost += mx;
             const Cut cut = s_cuts[mi];
             const uint32_t n = cut.n;
             // a refined cut of this job can be larger than the job's own cut (bf > 2)
@@ -606,22 +729,27 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
                 break;
             }
             for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
+            if (threadIdx.x == 0) s_nosplit = __longlong_as_double(0x7ff8000000000000ll);  // NaN: not yet taken
             __syncthreads();
             // SweepSAH: x from the cut order, y from the x order
-            stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
-            stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
-            SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
-            SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+            if (BS == 32) warp_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
+            else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
+            if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+            else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+            SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+            SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
             SahResult win;
             int warr;
             if (xs.cost < ys.cost) {  // z from the y order
-                stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
-                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+                if (BS == 32) warp_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
+                else stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
+                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
                 if (xs.cost < zs.cost) { win = xs; warr = 0; }
                 else { win = zs; warr = 2; }
             } else {  // z from the x order
-                stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
-                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx);
+                if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
+                else stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
+                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
                 if (ys.cost < zs.cost) { win = ys; warr = 1; }
                 else { win = zs; warr = 2; }
             }
@@ -666,6 +794,8 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
             const uint32_t ns[2] = {win.split, n - win.split};
             const uint32_t *srcs[2] = {ord, ord + win.split};
             const double thr = A.thr[min(cut.depth, DEPTH_TABLE - 1)];
+            const float thr_lo = A.thr_lo[min(cut.depth, DEPTH_TABLE - 1)];
+            const float thr_hi = A.thr_hi[min(cut.depth, DEPTH_TABLE - 1)];
             if (cut.depth >= DEPTH_TABLE - 1 && threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
             for (int side = 0; side < 2; side++) {
                 const uint32_t m = ns[side];
@@ -675,7 +805,14 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
                 uint32_t loc = 0;
                 for (uint32_t i = a; i < b; i++) {
                     const AuxNode &x = A.aux[sr[i]];
-                    bool keep = x.c0 < 0 || surface(x.lo, x.hi) < thr;
+                    // surface(x) < thr, decided in float32 outside a narrow band around thr
+                    bool keep = x.c0 < 0;
+                    if (!keep) {
+                        const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
+                        if (screen && s32 < thr_lo) keep = true;
+                        else if (screen && s32 > thr_hi) keep = false;
+                        else keep = surface(x.lo, x.hi) < thr;
+                    }
                     S.flag[i] = keep ? 1u : 2u;
                     loc += S.flag[i];
                 }
@@ -768,11 +905,16 @@ __global__ void __launch_bounds__(BS) k_phr_level(LevelArgs A) {
                     nj.slot = i;
                     nj.pad = 0;
                     A.jobs_out[q] = nj;
-                    atomicMax(&A.g->max_n[out], c.n);
+                    blk_max_n = max(blk_max_n, c.n);
                 }
             }
         }
         __syncthreads();
+    }
+    // the block's totals, one atomic each (per-split atomics on these counters contend)
+    if (threadIdx.x == 0) {
+        if (blk_build_cost) atomicAdd(&A.g->build_cost, blk_build_cost);
+        if (blk_max_n) atomicMax(&A.g->max_n[out], blk_max_n);
     }
 }
 
@@ -903,7 +1045,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_front[i], 2 * (size_t)n_aux + 2, tmp);
     for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_pool[i], pool_cap, tmp);
     for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_jobs[i], job_cap, tmp);
-    if (!rc) rc = palloc(ctx, &d_thr, DEPTH_TABLE, tmp);
+    if (!rc) rc = palloc(ctx, &d_thr, 2 * DEPTH_TABLE, tmp);  // the table, then its float32 band edges
     if (rc) { cleanup(); return rc; }
     // DefaultThreshold table (phr.go:356-358), host float64
     double S;
@@ -912,16 +1054,23 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         double w = (double)hi[0] - (double)lo[0], hh = (double)hi[1] - (double)lo[1], d = (double)hi[2] - (double)lo[2];
         S = 2 * w * hh + 2 * w * d + 2 * hh * d;
     }
-    std::vector<double> thr(DEPTH_TABLE);
-    for (int d = 0; d < DEPTH_TABLE; d++) thr[d] = S / std::pow(2.0, alpha * (double)d + delta);
-    GBT_CUDA(ctx, cudaMemcpyAsync(d_thr, thr.data(), DEPTH_TABLE * sizeof(double), cudaMemcpyHostToDevice, st));
+    std::vector<double> thr(2 * DEPTH_TABLE);
+    float *band = reinterpret_cast<float *>(thr.data() + DEPTH_TABLE);
+    for (int d = 0; d < DEPTH_TABLE; d++) {
+        thr[d] = S / std::pow(2.0, alpha * (double)d + delta);
+        band[d] = (float)(thr[d] * gbt_phr::THR_LO);
+        band[DEPTH_TABLE + d] = (float)(thr[d] * gbt_phr::THR_HI);
+    }
+    GBT_CUDA(ctx, cudaMemcpyAsync(d_thr, thr.data(), 2 * DEPTH_TABLE * sizeof(double), cudaMemcpyHostToDevice, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));  // the table is a pageable host vector
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, sizeof(PhrGlobals), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0xff, offsetof(PhrGlobals, pad), st));  // counters 0, root -1 below
+    GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0xff, offsetof(PhrGlobals, screen_bad), st));  // counters 0, root -1 below
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, offsetof(PhrGlobals, root), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_pn, 0, (size_t)pnode_cap * sizeof(PNode), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_aux, 0, (size_t)n_aux * sizeof(AuxNode), st));
     k_aux_build<<<(U + 255) / 256 + 1, 256, 0, st>>>(aux->d_hdr, aux->d_nodes, aux->d_size, aux->d_range, aux->d_run,
                                                      d_aux, U, N);
+    k_phr_screen<<<ctx->num_sms * 4, 256, 0, st>>>(d_aux, n_aux, d_g);
     const int32_t root = h.root_cnt > 0 ? 0 : h.root_ref;
     k_initial_cut<<<1, 1024, 0, st>>>(d_aux, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
     GBT_CUDA(ctx, cudaGetLastError());
@@ -934,7 +1083,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     size_t scratch_bytes = 0;
     int parity = 0;
     const int max_grid = ctx->num_sms * 4;         // 256-thread blocks
-    const int max_grid_small = ctx->num_sms * 16;  // one-warp blocks (about 18 resident per SM)
+    const int max_grid_small = ctx->num_sms * 32;  // one-warp blocks (32 resident per SM at 64 registers)
     int levels = 0;
     while (n_jobs > 0) {
         const bool small = nmax <= PHR_SMALL_CUT;
@@ -971,6 +1120,8 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         A.recs = out->d_prims;
         A.pn = d_pn;
         A.thr = d_thr;
+        A.thr_lo = reinterpret_cast<const float *>(d_thr + DEPTH_TABLE);
+        A.thr_hi = A.thr_lo + DEPTH_TABLE;
         A.jobs_in = d_jobs[parity];
         A.jobs_out = d_jobs[o];
         A.pool_in = d_pool[parity];
