@@ -33,6 +33,10 @@ constexpr int PT = 256;                  // threads per job block
 #define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
 #endif
 constexpr int DEPTH_TABLE = 4096;
+// Cuts of at most this many nodes are swept by a single lane (bf = 2): most
+// cuts are that small (on a 1M-triangle soup 93% of the splits sort 2-16
+// nodes), and a warp then works on 32 of them at once.
+constexpr uint32_t LANE_CUT = 16;
 
 struct AuxNode {
     float lo[3], hi[3];
@@ -60,6 +64,10 @@ struct PhrGlobals {
     uint32_t screen_bad;  // 1: some box coordinate is outside the float32 screening range
     uint32_t job_ctr[2], pool_ctr[2], max_n[2];
     unsigned long long build_cost;  // sizes of the cuts handed to Split (phr.go:214)
+    // Jobs of a level are kept in two lists in one array: cuts a single lane
+    // sweeps (2..LANE_CUT nodes, bf = 2) from the front (job_ctr), the others
+    // from the back (job_big_ctr).
+    uint32_t job_big_ctr[2];
 };
 
 // ---------------------------------------------------------------------------
@@ -641,280 +649,762 @@ __device__ void attach(const LevelArgs &A, int32_t parent, int32_t slot, int32_t
     else A.pn[parent].child[slot] = child;
 }
 
-// One block per job; BS threads per block.  Levels whose largest cut is small
-// run with one-warp blocks (BS = 32), so a job costs warp barriers only and 32
-// jobs are resident per SM.
+// Shared state of a block working on one job at a time.
 template <int BS>
-__global__ void __launch_bounds__(BS, BS == 32 ? 32 : 1) k_phr_level(LevelArgs A) {
-    __shared__ BoxAgg s_tmp[BS / 32];
-    __shared__ BoxAgg s_rank[BS];
-    __shared__ double s_cost[BS];
-    __shared__ double s_nosplit;
-    __shared__ uint32_t s_idx[BS];
-    __shared__ uint32_t s_u[32];
-    __shared__ Cut s_cuts[4];
-    __shared__ int32_t s_branch, s_ncuts;
-    __shared__ uint32_t s_off;
-    const int in = A.parity, out = A.parity ^ 1;
-    const uint32_t n_jobs = A.g->job_ctr[in];
-    Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
-    const bool screen = A.g->screen_bad == 0;
-    unsigned long long blk_build_cost = 0;  // thread 0's sums over this block's jobs
-    uint32_t blk_max_n = 0;
-    for (uint32_t j = blockIdx.x; j < n_jobs; j += gridDim.x) {
-        const PJob job = A.jobs_in[j];
-        if (job.n > A.nmax) {
-            if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
-            continue;
-        }
-        if (job.n <= 1) {  // only the root job when the auxiliary root is a leaf
-            if (threadIdx.x == 0) {
-                uint32_t id = A.pool_in[job.off];
-                const AuxNode &a = A.aux[id];
-                int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
-                if (p >= 0) {
-                    uint32_t ro = atomicAdd(&A.g->rec_ctr, a.count);
-                    PNode &q = A.pn[p];
-                    for (int k = 0; k < 3; k++) { q.lo[k] = a.lo[k]; q.hi[k] = a.hi[k]; }
-                    q.leaf = 1;
-                    q.nchild = 0;
-                    q.rec_off = ro;
-                    q.rec_cnt = a.count;
-                    attach(A, job.parent, job.slot, p);
-                    s_off = ro;
-                    s_u[0] = a.first;
-                    s_u[1] = a.count;
-                }
-            }
-            __syncthreads();
-            copy_records(A.aux_recs, A.recs, s_u[0], s_u[1], s_off, A.n_prim, A.err);
-            __syncthreads();
-            continue;
-        }
+struct BlockShared {
+    BoxAgg tmp[BS / 32];
+    BoxAgg rank[BS];
+    double cost[BS];
+    double nosplit;
+    uint32_t idx[BS];
+    uint32_t u[32];
+    Cut cuts[4];
+    int32_t branch, ncuts;
+    uint32_t off;
+};
+
+// Whether a job goes to the lane list: bf = 2 and a cut of 2..LANE_CUT nodes.
+__device__ __forceinline__ bool lane_cut_job(const LevelArgs &A, uint32_t n) {
+    return A.bf == 2 && n >= 2 && n <= LANE_CUT;
+}
+
+// Index in jobs_out for one new job of the given list (0xffffffff: no room).
+__device__ __forceinline__ uint32_t push_job_slot(const LevelArgs &A, bool lane_list) {
+    const int out = A.parity ^ 1;
+    const uint32_t q = atomicAdd(lane_list ? &A.g->job_ctr[out] : &A.g->job_big_ctr[out], 1u);
+    if (q >= A.job_cap) {
+        atomicOr(A.err, GBT_DEVERR_CAPACITY);
+        return 0xffffffffu;
+    }
+    return lane_list ? q : A.job_cap - 1 - q;
+}
+
+__device__ __forceinline__ void store_job(const LevelArgs &A, const PJob &nj, uint32_t slot) {
+    if (slot != 0xffffffffu) A.jobs_out[slot] = nj;
+}
+
+// buildSubTree (phr.go:92-152) for one job by the whole block: split the
+// largest cut until BranchingFactor cuts, then the branch and its children.
+// Thread 0 accumulates the build cost and the largest new cut.
+template <int BS>
+__device__ __noinline__ void job_block(const LevelArgs &A, const PJob &job, BlockShared<BS> &sh, const Scratch &S, bool screen,
+                          unsigned long long &blk_build_cost, uint32_t &blk_max_n) {
+    BoxAgg *s_tmp = sh.tmp;
+    BoxAgg *s_rank = sh.rank;
+    double *s_cost = sh.cost;
+    double &s_nosplit = sh.nosplit;
+    uint32_t *s_idx = sh.idx;
+    uint32_t *s_u = sh.u;
+    Cut *s_cuts = sh.cuts;
+    int32_t &s_branch = sh.branch, &s_ncuts = sh.ncuts;
+    uint32_t &s_off = sh.off;
+    const int out = A.parity ^ 1;
+    if (job.n > A.nmax) {
+        if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+        return;
+    }
+    if (job.n <= 1) {  // only the root job when the auxiliary root is a leaf
         if (threadIdx.x == 0) {
-            int32_t b = new_pnode(A.g, A.pnode_cap, A.err);
-            s_branch = b;
-            if (b >= 0) {
-                PNode &q = A.pn[b];
-                for (int k = 0; k < 3; k++) { q.lo[k] = job.lo[k]; q.hi[k] = job.hi[k]; }
-                q.leaf = 0;
+            uint32_t id = A.pool_in[job.off];
+            const AuxNode &a = A.aux[id];
+            int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
+            if (p >= 0) {
+                uint32_t ro = atomicAdd(&A.g->rec_ctr, a.count);
+                PNode &q = A.pn[p];
+                for (int k = 0; k < 3; k++) { q.lo[k] = a.lo[k]; q.hi[k] = a.hi[k]; }
+                q.leaf = 1;
                 q.nchild = 0;
-                attach(A, job.parent, job.slot, b);
+                q.rec_off = ro;
+                q.rec_cnt = a.count;
+                attach(A, job.parent, job.slot, p);
+                s_off = ro;
+                s_u[0] = a.first;
+                s_u[1] = a.count;
             }
-            Cut c0;
-            c0.off = job.off;
-            c0.n = job.n;
-            c0.src = A.pool_in + job.off;
-            for (int k = 0; k < 3; k++) { c0.lo[k] = job.lo[k]; c0.hi[k] = job.hi[k]; }
-            c0.depth = job.depth;
-            c0.leaf = -1;
-            s_cuts[0] = c0;
-            s_ncuts = 1;
         }
         __syncthreads();
-        if (s_branch < 0) continue;
-        // buildSubTree's loop: split the largest cut until BranchingFactor cuts
-        while (s_ncuts < A.bf) {
-            int nc = s_ncuts, mi = 0;
-            uint32_t mx = 0;
-            for (int i = 0; i < nc; i++)
-                if (s_cuts[i].n > mx) { mx = s_cuts[i].n; mi = i; }
-            if (mx <= 1) break;
-            if (threadIdx.x == 0) blk_build_cost += mx;
-            const Cut cut = s_cuts[mi];
-            const uint32_t n = cut.n;
-            // a refined cut of this job can be larger than the job's own cut (bf > 2)
-            if (n > A.cap) {
-                if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
-                break;
+        copy_records(A.aux_recs, A.recs, s_u[0], s_u[1], s_off, A.n_prim, A.err);
+        __syncthreads();
+        return;
+    }
+    if (threadIdx.x == 0) {
+        int32_t b = new_pnode(A.g, A.pnode_cap, A.err);
+        s_branch = b;
+        if (b >= 0) {
+            PNode &q = A.pn[b];
+            for (int k = 0; k < 3; k++) { q.lo[k] = job.lo[k]; q.hi[k] = job.hi[k]; }
+            q.leaf = 0;
+            q.nchild = 0;
+            attach(A, job.parent, job.slot, b);
+        }
+        Cut c0;
+        c0.off = job.off;
+        c0.n = job.n;
+        c0.src = A.pool_in + job.off;
+        for (int k = 0; k < 3; k++) { c0.lo[k] = job.lo[k]; c0.hi[k] = job.hi[k]; }
+        c0.depth = job.depth;
+        c0.leaf = -1;
+        s_cuts[0] = c0;
+        s_ncuts = 1;
+    }
+    __syncthreads();
+    if (s_branch < 0) return;
+    // buildSubTree's loop: split the largest cut until BranchingFactor cuts
+    while (s_ncuts < A.bf) {
+        int nc = s_ncuts, mi = 0;
+        uint32_t mx = 0;
+        for (int i = 0; i < nc; i++)
+            if (s_cuts[i].n > mx) { mx = s_cuts[i].n; mi = i; }
+        if (mx <= 1) break;
+        if (threadIdx.x == 0) blk_build_cost += mx;
+        const Cut cut = s_cuts[mi];
+        const uint32_t n = cut.n;
+        // a refined cut of this job can be larger than the job's own cut (bf > 2)
+        if (n > A.cap) {
+            if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            break;
+        }
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
+        if (threadIdx.x == 0) s_nosplit = __longlong_as_double(0x7ff8000000000000ll);  // NaN: not yet taken
+        __syncthreads();
+        // SweepSAH: x from the cut order, y from the x order
+        if (BS == 32) warp_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
+        else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
+        if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+        else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+        SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+        SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+        SahResult win;
+        int warr;
+        if (xs.cost < ys.cost) {  // z from the y order
+            if (BS == 32) warp_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
+            else stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
+            SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+            if (xs.cost < zs.cost) { win = xs; warr = 0; }
+            else { win = zs; warr = 2; }
+        } else {  // z from the x order
+            if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
+            else stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
+            SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+            if (ys.cost < zs.cost) { win = ys; warr = 1; }
+            else { win = zs; warr = 2; }
+        }
+        const uint32_t *ord = S.ord[warr];
+        if (win.split == 0) {
+            // makeLeaf(left.bounding, left.nodes...) over the winning order
+            uint32_t loc = 0;
+            const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
+            const uint32_t a = min(n, threadIdx.x * chunk), b = min(n, a + chunk);
+            for (uint32_t i = a; i < b; i++) loc += A.aux[ord[i]].count;
+            uint32_t tot;
+            uint32_t ex = block_scan_u32(loc, s_u, &tot);
+            for (uint32_t i = a; i < b; i++) {
+                S.flag[i] = ex;
+                ex += A.aux[ord[i]].count;
             }
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
-            if (threadIdx.x == 0) s_nosplit = __longlong_as_double(0x7ff8000000000000ll);  // NaN: not yet taken
-            __syncthreads();
-            // SweepSAH: x from the cut order, y from the x order
-            if (BS == 32) warp_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
-            else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
-            if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
-            else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
-            SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-            SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-            SahResult win;
-            int warr;
-            if (xs.cost < ys.cost) {  // z from the y order
-                if (BS == 32) warp_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
-                else stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
-                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-                if (xs.cost < zs.cost) { win = xs; warr = 0; }
-                else { win = zs; warr = 2; }
-            } else {  // z from the x order
-                if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
-                else stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
-                SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-                if (ys.cost < zs.cost) { win = ys; warr = 1; }
-                else { win = zs; warr = 2; }
-            }
-            const uint32_t *ord = S.ord[warr];
-            if (win.split == 0) {
-                // makeLeaf(left.bounding, left.nodes...) over the winning order
-                uint32_t loc = 0;
-                const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
-                const uint32_t a = min(n, threadIdx.x * chunk), b = min(n, a + chunk);
-                for (uint32_t i = a; i < b; i++) loc += A.aux[ord[i]].count;
-                uint32_t tot;
-                uint32_t ex = block_scan_u32(loc, s_u, &tot);
-                for (uint32_t i = a; i < b; i++) {
-                    S.flag[i] = ex;
-                    ex += A.aux[ord[i]].count;
+            if (threadIdx.x == 0) {
+                int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
+                s_off = atomicAdd(&A.g->rec_ctr, tot);
+                if (p >= 0) {
+                    PNode &q = A.pn[p];
+                    for (int k = 0; k < 3; k++) { q.lo[k] = win.llo[k]; q.hi[k] = win.lhi[k]; }
+                    q.leaf = 1;
+                    q.nchild = 0;
+                    q.rec_off = s_off;
+                    q.rec_cnt = tot;
                 }
+                Cut c;
+                c.n = 1;
+                c.leaf = p;
+                s_cuts[mi] = c;
+            }
+            __syncthreads();
+            for (uint32_t i = 0; i < n; i++) {
+                const AuxNode &x = A.aux[ord[i]];
+                copy_records(A.aux_recs, A.recs, x.first, x.count, s_off + S.flag[i], A.n_prim, A.err);
+            }
+            __syncthreads();
+            continue;
+        }
+        // refined(left), refined(right)
+        const uint32_t ns[2] = {win.split, n - win.split};
+        const uint32_t *srcs[2] = {ord, ord + win.split};
+        const double thr = A.thr[min(cut.depth, DEPTH_TABLE - 1)];
+        const float thr_lo = A.thr_lo[min(cut.depth, DEPTH_TABLE - 1)];
+        const float thr_hi = A.thr_hi[min(cut.depth, DEPTH_TABLE - 1)];
+        if (cut.depth >= DEPTH_TABLE - 1 && threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+        for (int side = 0; side < 2; side++) {
+            const uint32_t m = ns[side];
+            const uint32_t *sr = srcs[side];
+            const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
+            const uint32_t a = min(m, threadIdx.x * chunk), b = min(m, a + chunk);
+            uint32_t loc = 0;
+            for (uint32_t i = a; i < b; i++) {
+                const AuxNode &x = A.aux[sr[i]];
+                // surface(x) < thr, decided in float32 outside a narrow band around thr
+                bool keep = x.c0 < 0;
+                if (!keep) {
+                    const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
+                    if (screen && s32 < thr_lo) keep = true;
+                    else if (screen && s32 > thr_hi) keep = false;
+                    else keep = surface(x.lo, x.hi) < thr;
+                }
+                S.flag[i] = keep ? 1u : 2u;
+                loc += S.flag[i];
+            }
+            uint32_t tot;
+            uint32_t ex = block_scan_u32(loc, s_u, &tot);
+            const float *blo = side ? win.rlo : win.llo, *bhi = side ? win.rhi : win.lhi;
+            if (tot == 1) {  // a one-node cut becomes a leaf of everything below it
                 if (threadIdx.x == 0) {
+                    const AuxNode &x = A.aux[sr[0]];
                     int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
-                    s_off = atomicAdd(&A.g->rec_ctr, tot);
+                    s_off = atomicAdd(&A.g->rec_ctr, x.count);
+                    s_u[8] = x.first;
+                    s_u[9] = x.count;
                     if (p >= 0) {
                         PNode &q = A.pn[p];
-                        for (int k = 0; k < 3; k++) { q.lo[k] = win.llo[k]; q.hi[k] = win.lhi[k]; }
+                        for (int k = 0; k < 3; k++) { q.lo[k] = blo[k]; q.hi[k] = bhi[k]; }
                         q.leaf = 1;
                         q.nchild = 0;
                         q.rec_off = s_off;
-                        q.rec_cnt = tot;
+                        q.rec_cnt = x.count;
                     }
                     Cut c;
                     c.n = 1;
                     c.leaf = p;
-                    s_cuts[mi] = c;
+                    s_cuts[side == 0 ? mi : s_ncuts] = c;
                 }
                 __syncthreads();
-                for (uint32_t i = 0; i < n; i++) {
-                    const AuxNode &x = A.aux[ord[i]];
-                    copy_records(A.aux_recs, A.recs, x.first, x.count, s_off + S.flag[i], A.n_prim, A.err);
+                copy_records(A.aux_recs, A.recs, s_u[8], s_u[9], s_off, A.n_prim, A.err);
+            } else {
+                if (threadIdx.x == 0) {
+                    uint32_t o = atomicAdd(&A.g->pool_ctr[out], tot);
+                    if (o + tot > A.pool_cap) {
+                        atomicOr(A.err, GBT_DEVERR_CAPACITY);
+                        o = 0xffffffffu;
+                    }
+                    s_off = o;
                 }
                 __syncthreads();
-                continue;
+                const uint32_t o = s_off;
+                if (o != 0xffffffffu) {
+                    for (uint32_t i = a; i < b; i++) {
+                        const AuxNode &x = A.aux[sr[i]];
+                        if (S.flag[i] == 1u) {
+                            A.pool_out[o + ex] = sr[i];
+                            ex += 1;
+                        } else {
+                            A.pool_out[o + ex] = (uint32_t)x.c0;
+                            A.pool_out[o + ex + 1] = (uint32_t)x.c1;
+                            ex += 2;
+                        }
+                    }
+                }
+                if (threadIdx.x == 0) {
+                    Cut c;
+                    c.off = o == 0xffffffffu ? 0 : o;
+                    c.n = o == 0xffffffffu ? 1 : tot;
+                    c.src = A.pool_out + c.off;
+                    for (int k = 0; k < 3; k++) { c.lo[k] = blo[k]; c.hi[k] = bhi[k]; }
+                    c.depth = cut.depth + 1;
+                    c.leaf = o == 0xffffffffu ? -2 : -1;
+                    s_cuts[side == 0 ? mi : s_ncuts] = c;
+                }
             }
-            // refined(left), refined(right)
-            const uint32_t ns[2] = {win.split, n - win.split};
-            const uint32_t *srcs[2] = {ord, ord + win.split};
-            const double thr = A.thr[min(cut.depth, DEPTH_TABLE - 1)];
-            const float thr_lo = A.thr_lo[min(cut.depth, DEPTH_TABLE - 1)];
-            const float thr_hi = A.thr_hi[min(cut.depth, DEPTH_TABLE - 1)];
-            if (cut.depth >= DEPTH_TABLE - 1 && threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
-            for (int side = 0; side < 2; side++) {
-                const uint32_t m = ns[side];
-                const uint32_t *sr = srcs[side];
-                const uint32_t chunk = (m + blockDim.x - 1) / blockDim.x;
-                const uint32_t a = min(m, threadIdx.x * chunk), b = min(m, a + chunk);
-                uint32_t loc = 0;
-                for (uint32_t i = a; i < b; i++) {
-                    const AuxNode &x = A.aux[sr[i]];
-                    // surface(x) < thr, decided in float32 outside a narrow band around thr
-                    bool keep = x.c0 < 0;
-                    if (!keep) {
-                        const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
-                        if (screen && s32 < thr_lo) keep = true;
-                        else if (screen && s32 > thr_hi) keep = false;
-                        else keep = surface(x.lo, x.hi) < thr;
-                    }
-                    S.flag[i] = keep ? 1u : 2u;
-                    loc += S.flag[i];
-                }
-                uint32_t tot;
-                uint32_t ex = block_scan_u32(loc, s_u, &tot);
-                const float *blo = side ? win.rlo : win.llo, *bhi = side ? win.rhi : win.lhi;
-                if (tot == 1) {  // a one-node cut becomes a leaf of everything below it
-                    if (threadIdx.x == 0) {
-                        const AuxNode &x = A.aux[sr[0]];
-                        int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
-                        s_off = atomicAdd(&A.g->rec_ctr, x.count);
-                        s_u[8] = x.first;
-                        s_u[9] = x.count;
-                        if (p >= 0) {
-                            PNode &q = A.pn[p];
-                            for (int k = 0; k < 3; k++) { q.lo[k] = blo[k]; q.hi[k] = bhi[k]; }
-                            q.leaf = 1;
-                            q.nchild = 0;
-                            q.rec_off = s_off;
-                            q.rec_cnt = x.count;
-                        }
-                        Cut c;
-                        c.n = 1;
-                        c.leaf = p;
-                        s_cuts[side == 0 ? mi : s_ncuts] = c;
-                    }
-                    __syncthreads();
-                    copy_records(A.aux_recs, A.recs, s_u[8], s_u[9], s_off, A.n_prim, A.err);
-                } else {
-                    if (threadIdx.x == 0) {
-                        uint32_t o = atomicAdd(&A.g->pool_ctr[out], tot);
-                        if (o + tot > A.pool_cap) {
-                            atomicOr(A.err, GBT_DEVERR_CAPACITY);
-                            o = 0xffffffffu;
-                        }
-                        s_off = o;
-                    }
-                    __syncthreads();
-                    const uint32_t o = s_off;
-                    if (o != 0xffffffffu) {
-                        for (uint32_t i = a; i < b; i++) {
-                            const AuxNode &x = A.aux[sr[i]];
-                            if (S.flag[i] == 1u) {
-                                A.pool_out[o + ex] = sr[i];
-                                ex += 1;
-                            } else {
-                                A.pool_out[o + ex] = (uint32_t)x.c0;
-                                A.pool_out[o + ex + 1] = (uint32_t)x.c1;
-                                ex += 2;
-                            }
-                        }
-                    }
-                    if (threadIdx.x == 0) {
-                        Cut c;
-                        c.off = o == 0xffffffffu ? 0 : o;
-                        c.n = o == 0xffffffffu ? 1 : tot;
-                        c.src = A.pool_out + c.off;
-                        for (int k = 0; k < 3; k++) { c.lo[k] = blo[k]; c.hi[k] = bhi[k]; }
-                        c.depth = cut.depth + 1;
-                        c.leaf = o == 0xffffffffu ? -2 : -1;
-                        s_cuts[side == 0 ? mi : s_ncuts] = c;
-                    }
-                }
-                __syncthreads();
-            }
-            if (threadIdx.x == 0) s_ncuts = s_ncuts + 1;
             __syncthreads();
         }
-        // the branch and its children
-        if (threadIdx.x == 0) {
-            const int32_t b = s_branch;
-            const int nc = s_ncuts;
-            A.pn[b].nchild = nc;
-            for (int i = 0; i < nc; i++) {
-                const Cut &c = s_cuts[i];
-                if (c.leaf >= 0) {
-                    A.pn[b].child[i] = c.leaf;
-                } else if (c.leaf == -1) {
-                    uint32_t q = atomicAdd(&A.g->job_ctr[out], 1u);
-                    if (q >= A.job_cap) {
-                        atomicOr(A.err, GBT_DEVERR_CAPACITY);
-                        continue;
+        if (threadIdx.x == 0) s_ncuts = s_ncuts + 1;
+        __syncthreads();
+    }
+    // the branch and its children
+    if (threadIdx.x == 0) {
+        const int32_t b = s_branch;
+        const int nc = s_ncuts;
+        A.pn[b].nchild = nc;
+        for (int i = 0; i < nc; i++) {
+            const Cut &c = s_cuts[i];
+            if (c.leaf >= 0) {
+                A.pn[b].child[i] = c.leaf;
+            } else if (c.leaf == -1) {
+                PJob nj;
+                nj.off = c.off;
+                nj.n = c.n;
+                for (int k = 0; k < 3; k++) { nj.lo[k] = c.lo[k]; nj.hi[k] = c.hi[k]; }
+                nj.depth = c.depth;
+                nj.parent = b;
+                nj.slot = i;
+                nj.pad = 0;
+                store_job(A, nj, push_job_slot(A, lane_cut_job(A, nj.n)));
+                blk_max_n = max(blk_max_n, c.n);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// lane path: one lane sweeps one cut of at most LANE_CUT nodes (bf = 2)
+// ---------------------------------------------------------------------------
+// The same SweepSAH, minCost, refined and makeLeaf as job_block, for one cut
+// per lane.  Costs are taken in float32 and decided exactly: a comparison
+// whose float32 values are further apart than the screening slack is decided
+// by them (phr_exact.cuh), any other one by the float64 values, recomputed for
+// just those candidates; without screening every cost is float64.
+
+// Per-lane scratch, index-major so that the lanes of a warp use different banks.
+struct LaneScratch {
+    union {
+        unsigned long long key[LANE_CUT][32];  // sort keys
+        float c32[LANE_CUT][32];               // float32 split costs of a sweep
+    };
+    uint32_t id[LANE_CUT][32];       // the cut's node ids, in cut order
+    uint8_t ord[3][LANE_CUT][32];    // x, y, z orders: positions into id
+};
+
+struct LaneBox {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ void lbox_empty(LaneBox &b) {
+    b.lo[0] = b.lo[1] = b.lo[2] = INFINITY;
+    b.hi[0] = b.hi[1] = b.hi[2] = -INFINITY;
+}
+
+__device__ __forceinline__ void lbox_add(LaneBox &b, const AuxNode &x) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = fminf(b.lo[k], x.lo[k]);
+        b.hi[k] = fmaxf(b.hi[k], x.hi[k]);
+    }
+}
+
+struct LaneCut {
+    uint32_t n, total;   // nodes, sum of their subtree sizes
+    float lo[3], hi[3];  // the cut's box
+    float ns32;          // float32 cost of not splitting
+    double ns64;         // its float64 value, once taken
+    bool ns_has;
+};
+
+// A minCost result: split position (0: not splitting is cheapest) of order k.
+struct LanePick {
+    float c32;
+    double c64;
+    uint32_t split;
+    int k;
+    bool has64;
+};
+
+__device__ __forceinline__ const AuxNode &lane_node(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+                                                    uint32_t i, int ln) {
+    return aux[L.id[L.ord[k][i][ln]][ln]];
+}
+
+// sort.SliceStable by barycenter component `axis`: insertion sort of the
+// order `src` (-1: the cut order) into `dst`; equal keys keep their order.
+__device__ void lane_sort(const AuxNode *__restrict__ aux, LaneScratch &L, int src, int dst, int axis, uint32_t n,
+                          int ln) {
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t p = src < 0 ? i : L.ord[src][i][ln];
+        const AuxNode &x = aux[L.id[p][ln]];
+        const unsigned long long key = gbt_phr::key_of_bits(gbt_phr::bary_bits(x.lo[axis], x.hi[axis]));
+        uint32_t j = i;
+        while (j > 0 && L.key[j - 1][ln] > key) {
+            L.key[j][ln] = L.key[j - 1][ln];
+            L.ord[dst][j][ln] = L.ord[dst][j - 1][ln];
+            j--;
+        }
+        L.key[j][ln] = key;
+        L.ord[dst][j][ln] = (uint8_t)p;
+    }
+}
+
+// minCost's float64 cost of splitting order k before position i (phr.go:423-445).
+__device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k, uint32_t n,
+                                    uint32_t i, int ln) {
+    LaneBox l, r;
+    lbox_empty(l);
+    lbox_empty(r);
+    uint32_t lc = 0, rc = 0;
+    for (uint32_t t = 0; t < n; t++) {
+        const AuxNode &x = lane_node(aux, L, k, t, ln);
+        if (t < i) {
+            lbox_add(l, x);
+            lc += x.size;
+        } else {
+            lbox_add(r, x);
+            rc += x.size;
+        }
+    }
+    const double rcost = __dmul_rn(surface(r.lo, r.hi), (double)rc);
+    return __dadd_rn(rcost, __dmul_rn(surface(l.lo, l.hi), (double)lc));
+}
+
+__device__ __forceinline__ void lane_make64(LanePick &p, const AuxNode *__restrict__ aux, const LaneScratch &L, LaneCut &c, int ln) {
+    if (p.has64) return;
+    if (p.split) {
+        p.c64 = lane_split_cost64(aux, L, p.k, c.n, p.split, ln);
+    } else {
+        if (!c.ns_has) {
+            c.ns64 = __dmul_rn(surface(c.lo, c.hi), (double)c.total);
+            c.ns_has = true;
+        }
+        p.c64 = c.ns64;
+    }
+    p.has64 = true;
+}
+
+// a.cost < b.cost in float64
+__device__ bool lane_less(LanePick &a, LanePick &b, const AuxNode *__restrict__ aux, const LaneScratch &L,
+                          LaneCut &c, int ln) {
+    if (!(a.has64 && b.has64)) {
+        if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
+        if (__fmul_rn(b.c32, gbt_phr::SCREEN_SLACK) < a.c32) return false;
+        lane_make64(a, aux, L, c, ln);
+        lane_make64(b, aux, L, c, ln);
+    }
+    return a.c64 < b.c64;
+}
+
+// minCost (phr.go:414-459) over order k: the first cheapest split position,
+// or not splitting when that is not cheaper.
+__device__ LanePick lane_min_cost(const AuxNode *__restrict__ aux, LaneScratch &L, int k, LaneCut &c, bool screen,
+                                  int ln) {
+    const uint32_t n = c.n;
+    LanePick best;
+    best.k = k;
+    best.has64 = false;
+    best.c64 = 0.0;
+    if (screen) {
+        LaneBox r;
+        lbox_empty(r);
+        uint32_t rc = 0;
+        for (uint32_t i = n - 1; i >= 1; i--) {
+            const AuxNode &x = lane_node(aux, L, k, i, ln);
+            lbox_add(r, x);
+            rc += x.size;
+            L.c32[i][ln] = __fmul_rn(gbt_phr::surface32(r.lo, r.hi), gbt_phr::count_f32(rc));
+        }
+        LaneBox l;
+        lbox_empty(l);
+        uint32_t lc = 0, mi = 1;
+        float m = INFINITY;
+        for (uint32_t i = 1; i < n; i++) {
+            const AuxNode &x = lane_node(aux, L, k, i - 1, ln);
+            lbox_add(l, x);
+            lc += x.size;
+            const float cc = __fadd_rn(L.c32[i][ln], __fmul_rn(gbt_phr::surface32(l.lo, l.hi), gbt_phr::count_f32(lc)));
+            L.c32[i][ln] = cc;
+            if (cc < m) {
+                m = cc;
+                mi = i;
+            }
+        }
+        // positions whose float32 cost is within the slack of the least one
+        const float lim = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
+        uint32_t cand = 0;
+        for (uint32_t i = 1; i < n; i++) cand += L.c32[i][ln] <= lim ? 1u : 0u;
+        best.c32 = m;
+        best.split = mi;
+        if (cand > 1) {  // decided in float64 among the candidates, first minimum wins
+            double bc = INFINITY;
+            uint32_t bi = mi;
+            for (uint32_t i = 1; i < n; i++) {
+                if (!(L.c32[i][ln] <= lim)) continue;
+                const double d = lane_split_cost64(aux, L, k, n, i, ln);
+                if (d < bc) {
+                    bc = d;
+                    bi = i;
+                }
+            }
+            best.split = bi;
+            best.c32 = L.c32[bi][ln];
+            best.c64 = bc;
+            best.has64 = true;
+        }
+    } else {
+        double bc = INFINITY;
+        uint32_t bi = 1;
+        for (uint32_t i = 1; i < n; i++) {
+            const double d = lane_split_cost64(aux, L, k, n, i, ln);
+            if (d < bc) {
+                bc = d;
+                bi = i;
+            }
+        }
+        best.split = bi;
+        best.c32 = 0.f;
+        best.c64 = bc;
+        best.has64 = true;
+    }
+    LanePick ns;
+    ns.k = k;
+    ns.split = 0;
+    ns.c32 = c.ns32;
+    ns.has64 = false;
+    ns.c64 = 0.0;
+    if (!screen) lane_make64(ns, aux, L, c, ln);
+    if (lane_less(best, ns, aux, L, c, ln)) return best;
+    return ns;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_sum(uint32_t v, int ln) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (ln >= o) v += y;
+    }
+    return v;
+}
+
+// Allocates `v` entries of a counter for every lane with one atomic per warp;
+// returns this lane's first index (the warp's base + the lanes before it).
+__device__ __forceinline__ uint32_t warp_alloc(uint32_t *ctr, uint32_t v, int ln) {
+    const uint32_t incl = warp_incl_sum(v, ln);
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (ln == 0 && total) base = atomicAdd(ctr, total);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + incl - v;
+}
+
+// Record copy by one lane (copy_records for a single thread).
+__device__ void lane_copy_records(const float4 *__restrict__ src, float4 *__restrict__ dst, uint32_t from,
+                                  uint32_t count, uint32_t to, uint32_t n, unsigned int *err) {
+    if ((uint64_t)from + count > n || (uint64_t)to + count > n) {
+        atomicOr(err, GBT_DEVERR_BOUNDS);
+        return;
+    }
+    for (uint32_t i = 0; i < 3 * count; i++) dst[3 * (size_t)to + i] = src[3 * (size_t)from + i];
+}
+
+// One job per lane for the lanes with `mine`; every lane of the warp calls
+// this (the allocations are warp-wide).  Each lane accumulates its build cost
+// and largest new cut.
+__device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch &L, bool screen,
+                          unsigned long long &my_build_cost, uint32_t &my_max_n) {
+    const int ln = threadIdx.x & 31;
+    const AuxNode *__restrict__ aux = A.aux;
+    uint32_t n_pn = 0, n_rec = 0, n_pool = 0, n_lane_jobs = 0, n_big_jobs = 0;
+    uint32_t n = 0, split = 0, tot[2] = {0, 0}, keep[2] = {0, 0};
+    int k = 0;
+    if (mine) {
+        // SweepSAH (phr.go:368-405)
+        const PJob &job = A.jobs_in[j];
+        LaneCut c;
+        c.n = n = job.n;
+        c.total = 0;
+        const uint32_t off = job.off;
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t id = A.pool_in[off + i];
+            L.id[i][ln] = id;
+            c.total += aux[id].size;
+        }
+        for (int a = 0; a < 3; a++) {
+            c.lo[a] = job.lo[a];
+            c.hi[a] = job.hi[a];
+        }
+        c.ns32 = __fmul_rn(gbt_phr::surface32(c.lo, c.hi), gbt_phr::count_f32(c.total));
+        c.ns_has = false;
+        c.ns64 = 0.0;
+        lane_sort(aux, L, -1, 0, 0, n, ln);
+        LanePick xs = lane_min_cost(aux, L, 0, c, screen, ln);
+        lane_sort(aux, L, 0, 1, 1, n, ln);
+        LanePick ys = lane_min_cost(aux, L, 1, c, screen, ln);
+        // z from the y order when x is cheaper than y, else from the x order
+        const bool x_first = lane_less(xs, ys, aux, L, c, ln);
+        lane_sort(aux, L, x_first ? 1 : 0, 2, 2, n, ln);
+        LanePick zs = lane_min_cost(aux, L, 2, c, screen, ln);
+        LanePick &other = x_first ? xs : ys;
+        const LanePick win = lane_less(other, zs, aux, L, c, ln) ? other : zs;
+        my_build_cost += n;
+        k = win.k;
+        split = win.split;
+        if (split == 0) {  // makeLeaf over the winning order
+            n_pn = 2;
+            for (uint32_t i = 0; i < n; i++) n_rec += lane_node(aux, L, k, i, ln).count;
+        } else {  // refined(left), refined(right)
+            const int32_t depth = job.depth;
+            const int di = min(depth, DEPTH_TABLE - 1);
+            if (depth >= DEPTH_TABLE - 1) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            const double thr = A.thr[di];
+            const float thr_lo = A.thr_lo[di], thr_hi = A.thr_hi[di];
+            n_pn = 1;
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const uint32_t a = s ? split : 0, e = s ? n : split;
+                for (uint32_t i = a; i < e; i++) {
+                    const AuxNode &x = lane_node(aux, L, k, i, ln);
+                    bool kept = x.c0 < 0;
+                    if (!kept) {
+                        const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
+                        if (screen && s32 < thr_lo) kept = true;
+                        else if (screen && s32 > thr_hi) kept = false;
+                        else kept = surface(x.lo, x.hi) < thr;
                     }
-                    PJob nj;
-                    nj.off = c.off;
-                    nj.n = c.n;
-                    for (int k = 0; k < 3; k++) { nj.lo[k] = c.lo[k]; nj.hi[k] = c.hi[k]; }
-                    nj.depth = c.depth;
-                    nj.parent = b;
-                    nj.slot = i;
-                    nj.pad = 0;
-                    A.jobs_out[q] = nj;
-                    blk_max_n = max(blk_max_n, c.n);
+                    if (kept) keep[s] |= 1u << (i - a);
+                    tot[s] += kept ? 1u : 2u;
+                }
+                if (tot[s] == 1) {  // a one-node cut becomes a leaf of everything below it
+                    n_pn++;
+                    n_rec += lane_node(aux, L, k, a, ln).count;
+                } else {
+                    n_pool += tot[s];
+                    if (lane_cut_job(A, tot[s])) n_lane_jobs++;
+                    else n_big_jobs++;
                 }
             }
         }
-        __syncthreads();
+    }
+    // one atomic per counter and warp
+    const int out = A.parity ^ 1;
+    uint32_t pn = warp_alloc(&A.g->pnode_ctr, n_pn, ln);
+    uint32_t rec = warp_alloc(&A.g->rec_ctr, n_rec, ln);
+    uint32_t pool = warp_alloc(&A.g->pool_ctr[out], n_pool, ln);
+    uint32_t qs = warp_alloc(&A.g->job_ctr[out], n_lane_jobs, ln);
+    uint32_t qb = warp_alloc(&A.g->job_big_ctr[out], n_big_jobs, ln);
+    if (!mine) return;
+    if ((uint64_t)pn + n_pn > A.pnode_cap || (uint64_t)pool + n_pool > A.pool_cap ||
+        (uint64_t)qs + n_lane_jobs > A.job_cap || (uint64_t)qb + n_big_jobs > A.job_cap) {
+        atomicOr(A.err, GBT_DEVERR_CAPACITY);
+        return;
+    }
+    const PJob &job = A.jobs_in[j];
+    const int32_t b = (int32_t)pn++;
+    {
+        PNode &q = A.pn[b];
+        for (int a = 0; a < 3; a++) {
+            q.lo[a] = job.lo[a];
+            q.hi[a] = job.hi[a];
+        }
+        q.leaf = 0;
+        q.nchild = split ? 2 : 1;
+        attach(A, job.parent, job.slot, b);
+    }
+    if (split == 0) {
+        const int32_t p = (int32_t)pn;
+        PNode &q = A.pn[p];
+        for (int a = 0; a < 3; a++) {
+            q.lo[a] = job.lo[a];
+            q.hi[a] = job.hi[a];
+        }
+        q.leaf = 1;
+        q.nchild = 0;
+        q.rec_off = rec;
+        q.rec_cnt = n_rec;
+        A.pn[b].child[0] = p;
+        for (uint32_t i = 0; i < n; i++) {
+            const AuxNode &x = lane_node(aux, L, k, i, ln);
+            lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+            rec += x.count;
+        }
+        return;
+    }
+    const int32_t depth = job.depth;
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const uint32_t a = s ? split : 0, e = s ? n : split;
+        LaneBox box;  // the side's box: union of its nodes before refinement
+        lbox_empty(box);
+        for (uint32_t i = a; i < e; i++) lbox_add(box, lane_node(aux, L, k, i, ln));
+        if (tot[s] == 1) {
+            const AuxNode &x = lane_node(aux, L, k, a, ln);
+            const int32_t p = (int32_t)pn++;
+            PNode &q = A.pn[p];
+            for (int d = 0; d < 3; d++) {
+                q.lo[d] = box.lo[d];
+                q.hi[d] = box.hi[d];
+            }
+            q.leaf = 1;
+            q.nchild = 0;
+            q.rec_off = rec;
+            q.rec_cnt = x.count;
+            A.pn[b].child[s] = p;
+            lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+            rec += x.count;
+        } else {
+            PJob nj;
+            nj.off = pool;
+            nj.n = tot[s];
+            for (int d = 0; d < 3; d++) {
+                nj.lo[d] = box.lo[d];
+                nj.hi[d] = box.hi[d];
+            }
+            nj.depth = depth + 1;
+            nj.parent = b;
+            nj.slot = s;
+            nj.pad = 0;
+            for (uint32_t i = a; i < e; i++) {
+                const uint32_t id = L.id[L.ord[k][i][ln]][ln];
+                if (keep[s] >> (i - a) & 1u) {
+                    A.pool_out[pool++] = id;
+                } else {
+                    const AuxNode &x = aux[id];
+                    A.pool_out[pool++] = (uint32_t)x.c0;
+                    A.pool_out[pool++] = (uint32_t)x.c1;
+                }
+            }
+            if (lane_cut_job(A, tot[s])) A.jobs_out[qs++] = nj;
+            else A.jobs_out[A.job_cap - 1 - qb++] = nj;
+            my_max_n = max(my_max_n, tot[s]);
+        }
+    }
+}
+
+// One tree level.  256-thread blocks take one job at a time (levels with a
+// cut of more than PHR_SMALL_CUT nodes).  One-warp blocks take either one job
+// of the second list, swept by the whole warp, or 32 jobs of the lane list,
+// one per lane; a job of the lane list whose cut does not qualify (the root
+// job) is swept by the whole warp after them.
+template <int BS>
+__global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A) {
+    __shared__ BlockShared<BS> sh;
+    __shared__ LaneScratch s_lane[1];  // lane path (one-warp blocks only)
+    const int in = A.parity, out = A.parity ^ 1;
+    const uint32_t n_lane = A.g->job_ctr[in], n_big = A.g->job_big_ctr[in];
+    Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
+    const bool screen = A.g->screen_bad == 0;
+    unsigned long long my_build_cost = 0;  // this thread's sums (thread 0 for whole-block jobs)
+    uint32_t my_max_n = 0;
+    if (BS == 32) {
+        const uint32_t items = n_big + (n_lane + 31) / 32;
+        for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
+            if (it < n_big) {
+                job_block<BS>(A, A.jobs_in[A.job_cap - 1 - it], sh, S, screen, my_build_cost, my_max_n);
+                continue;
+            }
+            const uint32_t base = (it - n_big) * 32, j = base + threadIdx.x;
+            const bool valid = j < n_lane;
+            bool mine = false;
+            if (valid) {
+                const uint32_t n = A.jobs_in[j].n;
+                mine = lane_cut_job(A, n) && n <= A.nmax;
+            }
+            lane_jobs(A, j, mine, s_lane[0], screen, my_build_cost, my_max_n);
+            unsigned rest = __ballot_sync(0xffffffffu, valid && !mine);
+            while (rest) {
+                const int l = __ffs(rest) - 1;
+                rest &= rest - 1;
+                job_block<BS>(A, A.jobs_in[base + l], sh, S, screen, my_build_cost, my_max_n);
+            }
+        }
+    } else {
+        const uint32_t items = n_lane + n_big;
+        for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
+            const uint32_t j = it < n_lane ? it : A.job_cap - 1 - (it - n_lane);
+            job_block<BS>(A, A.jobs_in[j], sh, S, screen, my_build_cost, my_max_n);
+        }
     }
     // the block's totals, one atomic each (per-split atomics on these counters contend)
-    if (threadIdx.x == 0) {
-        if (blk_build_cost) atomicAdd(&A.g->build_cost, blk_build_cost);
-        if (blk_max_n) atomicMax(&A.g->max_n[out], blk_max_n);
+    if (threadIdx.x < 32) {
+        for (int o = 16; o > 0; o >>= 1) {
+            my_build_cost += __shfl_xor_sync(0xffffffffu, my_build_cost, o);
+            my_max_n = max(my_max_n, __shfl_xor_sync(0xffffffffu, my_max_n, o));
+        }
+        if (threadIdx.x == 0) {
+            if (my_build_cost) atomicAdd(&A.g->build_cost, my_build_cost);
+            if (my_max_n) atomicMax(&A.g->max_n[out], my_max_n);
+        }
     }
 }
 
@@ -1077,17 +1567,23 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     PhrGlobals g;
     GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
-    uint32_t n_jobs = g.job_ctr[0], nmax = g.max_n[0];
+    uint32_t n_lane = g.job_ctr[0], n_big = g.job_big_ctr[0], nmax = g.max_n[0];
+    uint32_t n_jobs = n_lane + n_big;
     const uint64_t initial_cut = g.pool_ctr[0];
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int parity = 0;
-    const int max_grid = ctx->num_sms * 4;         // 256-thread blocks
-    const int max_grid_small = ctx->num_sms * 32;  // one-warp blocks (32 resident per SM at 64 registers)
+    const int max_grid = ctx->num_sms * 4;  // 256-thread blocks
+    int warp_blocks_per_sm = 0;            // one-warp blocks resident per SM
+    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&warp_blocks_per_sm, k_phr_level<32>, 32, 0));
+    warp_blocks_per_sm = std::max(1, warp_blocks_per_sm);
+    const int max_grid_small = ctx->num_sms * warp_blocks_per_sm;
     int levels = 0;
     while (n_jobs > 0) {
         const bool small = nmax <= PHR_SMALL_CUT;
-        uint32_t grid = std::min<uint32_t>(n_jobs, (uint32_t)(small ? max_grid_small : max_grid));
+        // work items: one-warp blocks take a second-list job or 32 lane-list jobs
+        const uint32_t items = small ? n_big + (n_lane + 31) / 32 : n_jobs;
+        uint32_t grid = std::min<uint32_t>(items, (uint32_t)(small ? max_grid_small : max_grid));
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
         if (nmax > (1u << 28)) {
@@ -1114,6 +1610,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, job_ctr) + o * 4, 0, 4, st));
         GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, pool_ctr) + o * 4, 0, 4, st));
         GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, max_n) + o * 4, 0, 4, st));
+        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, job_big_ctr) + o * 4, 0, 4, st));
         LevelArgs A;
         A.aux = d_aux;
         A.aux_recs = aux->d_prims;
@@ -1146,7 +1643,14 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         unsigned int flags = 0;
         GBT_CUDA(ctx, cudaMemcpy(&flags, ctx->d_error, sizeof(flags), cudaMemcpyDeviceToHost));
         if (flags) break;  // reported by the caller's device-error check
-        n_jobs = g.job_ctr[o];
+        n_lane = g.job_ctr[o];
+        n_big = g.job_big_ctr[o];
+        if ((uint64_t)n_lane + n_big > job_cap) {  // the two lists met
+            flags = GBT_DEVERR_CAPACITY;
+            GBT_CUDA(ctx, cudaMemcpy(ctx->d_error, &flags, sizeof(flags), cudaMemcpyHostToDevice));
+            break;
+        }
+        n_jobs = n_lane + n_big;
         nmax = g.max_n[o];
         parity = o;
         levels++;
