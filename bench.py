@@ -486,7 +486,8 @@ def run_lbvh_workload(args):
 def run_profile_case(args):
     """The benchmark's scene, without timing: a case small enough for an ncu capture
     (about 0.3 GB on the device for the soup, 3 GB for the terrain).  `render`: 3
-    frames on the chosen tree; `lbvh`: 3 LBVH builds (the first one allocates)."""
+    frames on the chosen tree; `lbvh`: 3 LBVH builds (the first one allocates);
+    `phr`: 3 PHR refinements of the scene's LBVH."""
     from trace_gb300 import _lib, pt, scenes
 
     ctx = pt.Context(0)
@@ -501,6 +502,12 @@ def run_profile_case(args):
             ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
         ctx.sync()
         print("profile case lbvh: 3 builds of %d triangles" % s["verts"].shape[0])
+        return 0
+    if args.profile == "phr":
+        for _ in range(3):
+            pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux).close()
+        ctx.sync()
+        print("profile case phr: 3 PHR%s builds of %d triangles" % (str(PHR), s["verts"].shape[0]))
         return 0
     bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux) if args.bvh == "phr" else aux
     ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, bvh.h, args.layout), "layout")
@@ -526,8 +533,9 @@ def main():
                     help="traversal layout: the 4-wide view collapsed from the binary tree, or the binary nodes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
-    ap.add_argument("--profile", choices=["render", "lbvh"], default=None,
-                    help="run a small fixed case for an ncu capture and exit: 3 frames (render) or 3 LBVH builds")
+    ap.add_argument("--profile", choices=["render", "lbvh", "phr"], default=None,
+                    help="run a small fixed case for an ncu capture and exit: 3 frames (render), 3 LBVH builds "
+                         "or 3 PHR refinements of the LBVH")
     ap.add_argument("--profile-scene", choices=["soup", "terrain"], default="soup",
                     help="scene of --profile lbvh: the 1M soup or the 8.4M-triangle terrain")
     ap.add_argument("--workload", choices=["soup", "batch", "adjoint", "terrain", "lbvh"], default="soup",

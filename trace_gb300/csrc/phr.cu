@@ -29,6 +29,7 @@ namespace {
 
 constexpr uint32_t MAX_CUT_SIZE = 2500;  // phr.go:11
 constexpr int PT = 256;                  // threads per job block
+constexpr int WIDE = 512;                // threads per job block on levels of a few large cuts
 #ifndef PHR_SMALL_CUT
 #define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
 #endif
@@ -1358,8 +1359,12 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
 // job) is swept by the whole warp after them.
 template <int BS>
 __global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A) {
-    __shared__ BlockShared<BS> sh;
-    __shared__ LaneScratch s_lane[1];  // lane path (one-warp blocks only)
+    // the lane path (one-warp blocks) and whole-block jobs take turns, so they share the space
+    __shared__ union Shared {
+        BlockShared<BS> block;
+        LaneScratch lane;
+    } smem;
+    BlockShared<BS> &sh = smem.block;
     const int in = A.parity, out = A.parity ^ 1;
     const uint32_t n_lane = A.g->job_ctr[in], n_big = A.g->job_big_ctr[in];
     Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
@@ -1380,7 +1385,7 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A
                 const uint32_t n = A.jobs_in[j].n;
                 mine = lane_cut_job(A, n) && n <= A.nmax;
             }
-            lane_jobs(A, j, mine, s_lane[0], screen, my_build_cost, my_max_n);
+            lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
             unsigned rest = __ballot_sync(0xffffffffu, valid && !mine);
             while (rest) {
                 const int l = __ffs(rest) - 1;
@@ -1486,29 +1491,41 @@ __global__ void k_phr_finalize(const PNode *__restrict__ pn, const PhrGlobals *_
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
-template <class T>
-static int palloc(gbt_ctx *ctx, T **p, size_t count, std::vector<void *> &owned) {
-    *p = nullptr;
-    if (cudaMalloc(reinterpret_cast<void **>(p), (count ? count : 1) * sizeof(T)) != cudaSuccess) {
-        cudaGetLastError();
-        return gbt_fail(ctx, GBT_ENOMEM, "phr: device allocation of " + std::to_string(count * sizeof(T)) + " bytes");
+// One device allocation for the temporaries of a build, carved in 256-byte
+// aligned pieces.
+struct Arena {
+    size_t used = 0;
+    char *base = nullptr;
+    template <class T>
+    void take(T **p, size_t count) {
+        *p = reinterpret_cast<T *>(base + used);
+        used += gbt_align((count ? count : 1) * sizeof(T));
     }
-    owned.push_back(*p);
-    return GBT_OK;
-}
+};
 
 int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, gbt_bvh *out) {
     cudaStream_t st = ctx->stream;
+    // the level loop reads the counters and the error word back through pinned memory
+    struct Readback {
+        PhrGlobals g;
+        unsigned int flags;
+    };
+    Readback *hb = nullptr;
+    if (cudaMallocHost(&hb, sizeof(Readback)) != cudaSuccess) {
+        cudaGetLastError();
+        return gbt_fail(ctx, GBT_ENOMEM, "phr: pinned host allocation");
+    }
     BvhHeader h;
     GBT_CUDA(ctx, cudaMemcpyAsync(&h, aux->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
     const uint32_t U = h.n_unique, N = aux->n_prim;
     const uint32_t n_aux = U > 0 ? 2 * U - 1 : 1;
-    std::vector<void *> tmp;  // freed at the end
-    int rc = GBT_OK;
+    void *arena_mem = nullptr, *scratch = nullptr;
     auto cleanup = [&]() {
         cudaStreamSynchronize(st);
-        for (void *p : tmp) cudaFree(p);
+        if (scratch) cudaFree(scratch);
+        if (arena_mem) cudaFree(arena_mem);
+        cudaFreeHost(hb);
     };
     // outputs
     out->n_prim = N;
@@ -1519,6 +1536,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         cudaMalloc(&out->d_parent, (size_t)pnode_cap * sizeof(int32_t)) != cudaSuccess ||
         cudaMalloc(&out->d_hdr, sizeof(BvhHeader)) != cudaSuccess) {
         cudaGetLastError();
+        cudaFreeHost(hb);
         return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
     }
     out->node_cap = pnode_cap;
@@ -1529,14 +1547,26 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     PJob *d_jobs[2];
     double *d_thr;
     const uint32_t pool_cap = 3 * n_aux + 4096, job_cap = n_aux + 16;
-    if (!rc) rc = palloc(ctx, &d_aux, n_aux, tmp);
-    if (!rc) rc = palloc(ctx, &d_pn, pnode_cap, tmp);
-    if (!rc) rc = palloc(ctx, &d_g, 1, tmp);
-    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_front[i], 2 * (size_t)n_aux + 2, tmp);
-    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_pool[i], pool_cap, tmp);
-    for (int i = 0; i < 2 && !rc; i++) rc = palloc(ctx, &d_jobs[i], job_cap, tmp);
-    if (!rc) rc = palloc(ctx, &d_thr, 2 * DEPTH_TABLE, tmp);  // the table, then its float32 band edges
-    if (rc) { cleanup(); return rc; }
+    Arena ar;
+    for (int pass = 0; pass < 2; pass++) {  // sizes, then pointers
+        ar.used = 0;
+        ar.take(&d_aux, n_aux);
+        ar.take(&d_pn, pnode_cap);
+        ar.take(&d_g, 1);
+        for (int i = 0; i < 2; i++) ar.take(&d_front[i], 2 * (size_t)n_aux + 2);
+        for (int i = 0; i < 2; i++) ar.take(&d_pool[i], pool_cap);
+        for (int i = 0; i < 2; i++) ar.take(&d_jobs[i], job_cap);
+        ar.take(&d_thr, 2 * DEPTH_TABLE);  // the table, then its float32 band edges
+        if (pass == 0) {
+            if (cudaMalloc(&arena_mem, ar.used) != cudaSuccess) {
+                cudaGetLastError();
+                arena_mem = nullptr;
+                cleanup();
+                return gbt_fail(ctx, GBT_ENOMEM, "phr: device allocation of " + std::to_string(ar.used) + " bytes");
+            }
+            ar.base = static_cast<char *>(arena_mem);
+        }
+    }
     // DefaultThreshold table (phr.go:356-358), host float64
     double S;
     {
@@ -1552,7 +1582,6 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         band[DEPTH_TABLE + d] = (float)(thr[d] * gbt_phr::THR_HI);
     }
     GBT_CUDA(ctx, cudaMemcpyAsync(d_thr, thr.data(), 2 * DEPTH_TABLE * sizeof(double), cudaMemcpyHostToDevice, st));
-    GBT_CUDA(ctx, cudaStreamSynchronize(st));  // the table is a pageable host vector
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, sizeof(PhrGlobals), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0xff, offsetof(PhrGlobals, screen_bad), st));  // counters 0, root -1 below
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, offsetof(PhrGlobals, root), st));
@@ -1564,43 +1593,50 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     const int32_t root = h.root_cnt > 0 ? 0 : h.root_ref;
     k_initial_cut<<<1, 1024, 0, st>>>(d_aux, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
     GBT_CUDA(ctx, cudaGetLastError());
-    PhrGlobals g;
-    GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
-    GBT_CUDA(ctx, cudaStreamSynchronize(st));
+    GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaStreamSynchronize(st));  // also: the threshold table's pageable source is consumed
+    const PhrGlobals &g = hb->g;
     uint32_t n_lane = g.job_ctr[0], n_big = g.job_big_ctr[0], nmax = g.max_n[0];
     uint32_t n_jobs = n_lane + n_big;
     const uint64_t initial_cut = g.pool_ctr[0];
-    void *scratch = nullptr;
     size_t scratch_bytes = 0;
     int parity = 0;
-    const int max_grid = ctx->num_sms * 4;  // 256-thread blocks
-    int warp_blocks_per_sm = 0;            // one-warp blocks resident per SM
-    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&warp_blocks_per_sm, k_phr_level<32>, 32, 0));
-    warp_blocks_per_sm = std::max(1, warp_blocks_per_sm);
-    const int max_grid_small = ctx->num_sms * warp_blocks_per_sm;
+    // grids: the most blocks that are resident at once
+    int per_sm[3] = {0, 0, 0};  // one-warp, PT-thread and WIDE-thread blocks
+    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_phr_level<32>, 32, 0));
+    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_phr_level<PT>, PT, 0));
+    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], k_phr_level<WIDE>, WIDE, 0));
+    const uint32_t max_grid[3] = {(uint32_t)(ctx->num_sms * std::max(1, per_sm[0])),
+                                  (uint32_t)(ctx->num_sms * std::max(1, per_sm[1])),
+                                  (uint32_t)(ctx->num_sms * std::max(1, per_sm[2]))};
     int levels = 0;
     while (n_jobs > 0) {
-        const bool small = nmax <= PHR_SMALL_CUT;
+        // one-warp blocks when every cut is small; WIDE-thread blocks for levels of a few
+        // large cuts (the first ones), PT-thread blocks otherwise
+        const int variant = nmax <= PHR_SMALL_CUT ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
         // work items: one-warp blocks take a second-list job or 32 lane-list jobs
-        const uint32_t items = small ? n_big + (n_lane + 31) / 32 : n_jobs;
-        uint32_t grid = std::min<uint32_t>(items, (uint32_t)(small ? max_grid_small : max_grid));
+        const uint32_t items = variant == 0 ? n_big + (n_lane + 31) / 32 : n_jobs;
+        const uint32_t grid = std::min<uint32_t>(items, max_grid[variant]);
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
         if (nmax > (1u << 28)) {
-            if (scratch) cudaFree(scratch);
             cleanup();
             return gbt_fail(ctx, GBT_ENOMEM, "phr: cut too large");
         }
         const uint32_t cap = nmax << (bf > 2 ? bf - 2 : 0);
-        size_t per_block = gbt_align(scratch_bytes_for(cap));
-        size_t need = per_block * grid;
-        if (need > scratch_bytes) {
+        const size_t per_block = gbt_align(scratch_bytes_for(cap));
+        if (per_block * grid > scratch_bytes) {
+            // sized for every block the variant can have resident, so that later
+            // levels seldom need to grow it
+            const size_t need = per_block * max_grid[variant];
             if (scratch) {
                 cudaStreamSynchronize(st);
                 cudaFree(scratch);
+                scratch = nullptr;
             }
             if (cudaMalloc(&scratch, need) != cudaSuccess) {
                 cudaGetLastError();
+                scratch = nullptr;
                 cleanup();
                 return gbt_fail(ctx, GBT_ENOMEM, "phr: scratch");
             }
@@ -1635,18 +1671,18 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         A.bf = bf;
         A.n_prim = N;
         A.err = ctx->d_error;
-        if (small) k_phr_level<32><<<grid, 32, 0, st>>>(A);
-        else k_phr_level<PT><<<grid, PT, 0, st>>>(A);
+        if (variant == 0) k_phr_level<32><<<grid, 32, 0, st>>>(A);
+        else if (variant == 1) k_phr_level<PT><<<grid, PT, 0, st>>>(A);
+        else k_phr_level<WIDE><<<grid, WIDE, 0, st>>>(A);
         GBT_CUDA(ctx, cudaGetLastError());
-        GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
+        GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
+        GBT_CUDA(ctx, cudaMemcpyAsync(&hb->flags, ctx->d_error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaStreamSynchronize(st));
-        unsigned int flags = 0;
-        GBT_CUDA(ctx, cudaMemcpy(&flags, ctx->d_error, sizeof(flags), cudaMemcpyDeviceToHost));
-        if (flags) break;  // reported by the caller's device-error check
+        if (hb->flags) break;  // reported by the caller's device-error check
         n_lane = g.job_ctr[o];
         n_big = g.job_big_ctr[o];
         if ((uint64_t)n_lane + n_big > job_cap) {  // the two lists met
-            flags = GBT_DEVERR_CAPACITY;
+            const unsigned int flags = GBT_DEVERR_CAPACITY;
             GBT_CUDA(ctx, cudaMemcpy(ctx->d_error, &flags, sizeof(flags), cudaMemcpyHostToDevice));
             break;
         }
@@ -1659,11 +1695,10 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
                                                             out->d_parent,
                                                             ctx->d_error);
     GBT_CUDA(ctx, cudaGetLastError());
-    GBT_CUDA(ctx, cudaMemcpyAsync(&g, d_g, sizeof(g), cudaMemcpyDeviceToHost, st));
+    GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
     out->n_nodes_host = g.pnode_ctr;
     out->build_cost = (int64_t)(initial_cut + g.build_cost);  // BuildWithCost (phr.go:154-192)
-    if (scratch) cudaFree(scratch);
     cleanup();
     return GBT_OK;
 }
