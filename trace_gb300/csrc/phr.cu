@@ -30,6 +30,7 @@ namespace {
 constexpr uint32_t MAX_CUT_SIZE = 2500;  // phr.go:11
 constexpr int PT = 256;                  // threads per job block
 constexpr int WIDE = 512;                // threads per job block on levels of a few large cuts
+constexpr uint32_t SORT_SMEM_MAX = 8192; // largest padded cut sorted in shared memory (96 KB)
 #ifndef PHR_SMALL_CUT
 #define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
 #endif
@@ -38,6 +39,8 @@ constexpr int DEPTH_TABLE = 4096;
 // cuts are that small (on a 1M-triangle soup 93% of the splits sort 2-16
 // nodes), and a warp then works on 32 of them at once.
 constexpr uint32_t LANE_CUT = 16;
+// Longer record ranges of the lane path's leaves are copied by the whole warp.
+constexpr uint32_t LANE_COPY = 8;
 
 struct AuxNode {
     float lo[3], hi[3];
@@ -631,6 +634,7 @@ struct LevelArgs {
     uint32_t cap;  // per-block scratch capacity in cut nodes: nmax * 2^(bf-2)
     unsigned char *scratch;
     size_t scratch_per_block;
+    uint32_t sort_smem;  // > 0: the block sort's keys and positions live in dynamic shared memory
     int bf;
     uint32_t n_prim;
     unsigned int *err;
@@ -688,7 +692,7 @@ __device__ __forceinline__ void store_job(const LevelArgs &A, const PJob &nj, ui
 // largest cut until BranchingFactor cuts, then the branch and its children.
 // Thread 0 accumulates the build cost and the largest new cut.
 template <int BS>
-__device__ __noinline__ void job_block(const LevelArgs &A, const PJob &job, BlockShared<BS> &sh, const Scratch &S, bool screen,
+__device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, BlockShared<BS> &sh, const Scratch &S, bool screen,
                           unsigned long long &blk_build_cost, uint32_t &blk_max_n) {
     BoxAgg *s_tmp = sh.tmp;
     BoxAgg *s_rank = sh.rank;
@@ -790,7 +794,7 @@ __device__ __noinline__ void job_block(const LevelArgs &A, const PJob &job, Bloc
             if (ys.cost < zs.cost) { win = ys; warr = 1; }
             else { win = zs; warr = 2; }
         }
-        const uint32_t *ord = S.ord[warr];
+        const uint32_t *ord = warr == 0 ? S.ord[0] : (warr == 1 ? S.ord[1] : S.ord[2]);
         if (win.split == 0) {
             // makeLeaf(left.bounding, left.nodes...) over the winning order
             uint32_t loc = 0;
@@ -834,6 +838,7 @@ __device__ __noinline__ void job_block(const LevelArgs &A, const PJob &job, Bloc
         const float thr_lo = A.thr_lo[min(cut.depth, DEPTH_TABLE - 1)];
         const float thr_hi = A.thr_hi[min(cut.depth, DEPTH_TABLE - 1)];
         if (cut.depth >= DEPTH_TABLE - 1 && threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+#pragma unroll
         for (int side = 0; side < 2; side++) {
             const uint32_t m = ns[side];
             const uint32_t *sr = srcs[side];
@@ -1056,7 +1061,7 @@ __device__ __forceinline__ void lane_make64(LanePick &p, const AuxNode *__restri
 }
 
 // a.cost < b.cost in float64
-__device__ bool lane_less(LanePick &a, LanePick &b, const AuxNode *__restrict__ aux, const LaneScratch &L,
+__device__ __forceinline__ bool lane_less(LanePick &a, LanePick &b, const AuxNode *__restrict__ aux, const LaneScratch &L,
                           LaneCut &c, int ln) {
     if (!(a.has64 && b.has64)) {
         if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
@@ -1216,7 +1221,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
         const bool x_first = lane_less(xs, ys, aux, L, c, ln);
         lane_sort(aux, L, x_first ? 1 : 0, 2, 2, n, ln);
         LanePick zs = lane_min_cost(aux, L, 2, c, screen, ln);
-        LanePick &other = x_first ? xs : ys;
+        LanePick other = x_first ? xs : ys;
         const LanePick win = lane_less(other, zs, aux, L, c, ln) ? other : zs;
         my_build_cost += n;
         k = win.k;
@@ -1264,90 +1269,117 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
     uint32_t pool = warp_alloc(&A.g->pool_ctr[out], n_pool, ln);
     uint32_t qs = warp_alloc(&A.g->job_ctr[out], n_lane_jobs, ln);
     uint32_t qb = warp_alloc(&A.g->job_big_ctr[out], n_big_jobs, ln);
-    if (!mine) return;
-    if ((uint64_t)pn + n_pn > A.pnode_cap || (uint64_t)pool + n_pool > A.pool_cap ||
-        (uint64_t)qs + n_lane_jobs > A.job_cap || (uint64_t)qb + n_big_jobs > A.job_cap) {
+    bool ok = mine;
+    if (ok && ((uint64_t)pn + n_pn > A.pnode_cap || (uint64_t)pool + n_pool > A.pool_cap ||
+               (uint64_t)qs + n_lane_jobs > A.job_cap || (uint64_t)qb + n_big_jobs > A.job_cap)) {
         atomicOr(A.err, GBT_DEVERR_CAPACITY);
-        return;
+        ok = false;
     }
-    const PJob &job = A.jobs_in[j];
-    const int32_t b = (int32_t)pn++;
-    {
-        PNode &q = A.pn[b];
-        for (int a = 0; a < 3; a++) {
-            q.lo[a] = job.lo[a];
-            q.hi[a] = job.hi[a];
+    // leaves' records: a lane copies ranges of up to LANE_COPY records itself and
+    // leaves longer ones to the whole warp below
+    const uint32_t rec_start = rec;
+    bool long_copy = false;
+    if (ok) {
+        const PJob &job = A.jobs_in[j];
+        const int32_t b = (int32_t)pn++;
+        {
+            PNode &q = A.pn[b];
+            for (int a = 0; a < 3; a++) {
+                q.lo[a] = job.lo[a];
+                q.hi[a] = job.hi[a];
+            }
+            q.leaf = 0;
+            q.nchild = split ? 2 : 1;
+            attach(A, job.parent, job.slot, b);
         }
-        q.leaf = 0;
-        q.nchild = split ? 2 : 1;
-        attach(A, job.parent, job.slot, b);
-    }
-    if (split == 0) {
-        const int32_t p = (int32_t)pn;
-        PNode &q = A.pn[p];
-        for (int a = 0; a < 3; a++) {
-            q.lo[a] = job.lo[a];
-            q.hi[a] = job.hi[a];
-        }
-        q.leaf = 1;
-        q.nchild = 0;
-        q.rec_off = rec;
-        q.rec_cnt = n_rec;
-        A.pn[b].child[0] = p;
-        for (uint32_t i = 0; i < n; i++) {
-            const AuxNode &x = lane_node(aux, L, k, i, ln);
-            lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
-            rec += x.count;
-        }
-        return;
-    }
-    const int32_t depth = job.depth;
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-        const uint32_t a = s ? split : 0, e = s ? n : split;
-        LaneBox box;  // the side's box: union of its nodes before refinement
-        lbox_empty(box);
-        for (uint32_t i = a; i < e; i++) lbox_add(box, lane_node(aux, L, k, i, ln));
-        if (tot[s] == 1) {
-            const AuxNode &x = lane_node(aux, L, k, a, ln);
-            const int32_t p = (int32_t)pn++;
+        if (split == 0) {
+            const int32_t p = (int32_t)pn;
             PNode &q = A.pn[p];
-            for (int d = 0; d < 3; d++) {
-                q.lo[d] = box.lo[d];
-                q.hi[d] = box.hi[d];
+            for (int a = 0; a < 3; a++) {
+                q.lo[a] = job.lo[a];
+                q.hi[a] = job.hi[a];
             }
             q.leaf = 1;
             q.nchild = 0;
             q.rec_off = rec;
-            q.rec_cnt = x.count;
-            A.pn[b].child[s] = p;
-            lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
-            rec += x.count;
-        } else {
-            PJob nj;
-            nj.off = pool;
-            nj.n = tot[s];
-            for (int d = 0; d < 3; d++) {
-                nj.lo[d] = box.lo[d];
-                nj.hi[d] = box.hi[d];
+            q.rec_cnt = n_rec;
+            A.pn[b].child[0] = p;
+            for (uint32_t i = 0; i < n; i++) {
+                const AuxNode &x = lane_node(aux, L, k, i, ln);
+                if (x.count <= LANE_COPY) lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+                else long_copy = true;
+                rec += x.count;
             }
-            nj.depth = depth + 1;
-            nj.parent = b;
-            nj.slot = s;
-            nj.pad = 0;
-            for (uint32_t i = a; i < e; i++) {
-                const uint32_t id = L.id[L.ord[k][i][ln]][ln];
-                if (keep[s] >> (i - a) & 1u) {
-                    A.pool_out[pool++] = id;
+        } else {
+            const int32_t depth = job.depth;
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const uint32_t a = s ? split : 0, e = s ? n : split;
+                LaneBox box;  // the side's box: union of its nodes before refinement
+                lbox_empty(box);
+                for (uint32_t i = a; i < e; i++) lbox_add(box, lane_node(aux, L, k, i, ln));
+                if (tot[s] == 1) {
+                    const AuxNode &x = lane_node(aux, L, k, a, ln);
+                    const int32_t p = (int32_t)pn++;
+                    PNode &q = A.pn[p];
+                    for (int d = 0; d < 3; d++) {
+                        q.lo[d] = box.lo[d];
+                        q.hi[d] = box.hi[d];
+                    }
+                    q.leaf = 1;
+                    q.nchild = 0;
+                    q.rec_off = rec;
+                    q.rec_cnt = x.count;
+                    A.pn[b].child[s] = p;
+                    if (x.count <= LANE_COPY) lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+                    else long_copy = true;
+                    rec += x.count;
                 } else {
-                    const AuxNode &x = aux[id];
-                    A.pool_out[pool++] = (uint32_t)x.c0;
-                    A.pool_out[pool++] = (uint32_t)x.c1;
+                    PJob nj;
+                    nj.off = pool;
+                    nj.n = tot[s];
+                    for (int d = 0; d < 3; d++) {
+                        nj.lo[d] = box.lo[d];
+                        nj.hi[d] = box.hi[d];
+                    }
+                    nj.depth = depth + 1;
+                    nj.parent = b;
+                    nj.slot = s;
+                    nj.pad = 0;
+                    for (uint32_t i = a; i < e; i++) {
+                        const uint32_t id = L.id[L.ord[k][i][ln]][ln];
+                        if (keep[s] >> (i - a) & 1u) {
+                            A.pool_out[pool++] = id;
+                        } else {
+                            const AuxNode &x = aux[id];
+                            A.pool_out[pool++] = (uint32_t)x.c0;
+                            A.pool_out[pool++] = (uint32_t)x.c1;
+                        }
+                    }
+                    if (lane_cut_job(A, tot[s])) A.jobs_out[qs++] = nj;
+                    else A.jobs_out[A.job_cap - 1 - qb++] = nj;
+                    my_max_n = max(my_max_n, tot[s]);
                 }
             }
-            if (lane_cut_job(A, tot[s])) A.jobs_out[qs++] = nj;
-            else A.jobs_out[A.job_cap - 1 - qb++] = nj;
-            my_max_n = max(my_max_n, tot[s]);
+        }
+    }
+    // the long record ranges, lane by lane, copied by the whole warp in the same walk order
+    unsigned pending = __ballot_sync(0xffffffffu, long_copy);
+    while (pending) {
+        const int l = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t r0 = __shfl_sync(0xffffffffu, rec_start, l), sp = __shfl_sync(0xffffffffu, split, l);
+        const uint32_t nl = __shfl_sync(0xffffffffu, n, l);
+        const int kl = __shfl_sync(0xffffffffu, k, l);
+        const uint32_t t0 = __shfl_sync(0xffffffffu, tot[0], l), t1 = __shfl_sync(0xffffffffu, tot[1], l);
+        uint32_t r = r0;
+        const uint32_t walk = sp == 0 ? nl : 2;
+        for (uint32_t q = 0; q < walk; q++) {
+            if (sp != 0 && (q ? t1 : t0) != 1) continue;  // that side is a cut, not a leaf
+            const uint32_t pos = sp == 0 ? q : (q ? sp : 0);
+            const AuxNode &x = aux[L.id[L.ord[kl][pos][l]][l]];
+            if (x.count > LANE_COPY) copy_records(A.aux_recs, A.recs, x.first, x.count, r, A.n_prim, A.err);
+            r += x.count;
         }
     }
 }
@@ -1358,7 +1390,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
 // one per lane; a job of the lane list whose cut does not qualify (the root
 // job) is swept by the whole warp after them.
 template <int BS>
-__global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A) {
+__global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
     // the lane path (one-warp blocks) and whole-block jobs take turns, so they share the space
     __shared__ union Shared {
         BlockShared<BS> block;
@@ -1368,17 +1400,29 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A
     const int in = A.parity, out = A.parity ^ 1;
     const uint32_t n_lane = A.g->job_ctr[in], n_big = A.g->job_big_ctr[in];
     Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
+    if (A.sort_smem) {  // every stage of the bitonic network then reads shared memory, not L2
+        extern __shared__ unsigned long long dyn_smem[];
+        const uint32_t P = pow2_at_least(A.cap > 0 ? A.cap : 1);
+        S.skey = dyn_smem;
+        S.sval = reinterpret_cast<uint32_t *>(dyn_smem + P);
+    }
     const bool screen = A.g->screen_bad == 0;
     unsigned long long my_build_cost = 0;  // this thread's sums (thread 0 for whole-block jobs)
     uint32_t my_max_n = 0;
-    if (BS == 32) {
-        const uint32_t items = n_big + (n_lane + 31) / 32;
-        for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
-            if (it < n_big) {
-                job_block<BS>(A, A.jobs_in[A.job_cap - 1 - it], sh, S, screen, my_build_cost, my_max_n);
-                continue;
-            }
-            const uint32_t base = (it - n_big) * 32, j = base + threadIdx.x;
+    // Work items: one-warp blocks take a second-list job or 32 lane-list jobs (the
+    // lanes' own ones first, then any that do not qualify, by the whole warp); wider
+    // blocks take one job of either list.  job_block has a single call site.
+    const uint32_t items = BS == 32 ? n_big + (n_lane + 31) / 32 : n_lane + n_big;
+    for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
+        uint32_t base = 0;   // the group's first lane-list job
+        unsigned rest = 1u;  // bit l: job base + l still to be done by the whole block
+        if (BS != 32) {
+            base = it < n_lane ? it : A.job_cap - 1 - (it - n_lane);
+        } else if (it < n_big) {
+            base = A.job_cap - 1 - it;
+        } else {
+            base = (it - n_big) * 32;
+            const uint32_t j = base + threadIdx.x;
             const bool valid = j < n_lane;
             bool mine = false;
             if (valid) {
@@ -1386,18 +1430,12 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : 1) k_phr_level(LevelArgs A
                 mine = lane_cut_job(A, n) && n <= A.nmax;
             }
             lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
-            unsigned rest = __ballot_sync(0xffffffffu, valid && !mine);
-            while (rest) {
-                const int l = __ffs(rest) - 1;
-                rest &= rest - 1;
-                job_block<BS>(A, A.jobs_in[base + l], sh, S, screen, my_build_cost, my_max_n);
-            }
+            rest = __ballot_sync(0xffffffffu, valid && !mine);
         }
-    } else {
-        const uint32_t items = n_lane + n_big;
-        for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
-            const uint32_t j = it < n_lane ? it : A.job_cap - 1 - (it - n_lane);
-            job_block<BS>(A, A.jobs_in[j], sh, S, screen, my_build_cost, my_max_n);
+        while (rest) {
+            const int l = __ffs(rest) - 1;
+            rest &= rest - 1;
+            job_block<BS>(A, A.jobs_in[base + l], sh, S, screen, my_build_cost, my_max_n);
         }
     }
     // the block's totals, one atomic each (per-split atomics on these counters contend)
@@ -1601,22 +1639,16 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     const uint64_t initial_cut = g.pool_ctr[0];
     size_t scratch_bytes = 0;
     int parity = 0;
-    // grids: the most blocks that are resident at once
-    int per_sm[3] = {0, 0, 0};  // one-warp, PT-thread and WIDE-thread blocks
-    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], k_phr_level<32>, 32, 0));
-    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], k_phr_level<PT>, PT, 0));
-    GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[2], k_phr_level<WIDE>, WIDE, 0));
-    const uint32_t max_grid[3] = {(uint32_t)(ctx->num_sms * std::max(1, per_sm[0])),
-                                  (uint32_t)(ctx->num_sms * std::max(1, per_sm[1])),
-                                  (uint32_t)(ctx->num_sms * std::max(1, per_sm[2]))};
+    // whole-block jobs sort in dynamic shared memory up to SORT_SMEM_MAX keys
+    GBT_CUDA(ctx, cudaFuncSetAttribute(k_phr_level<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       SORT_SMEM_MAX * 12));
+    GBT_CUDA(ctx, cudaFuncSetAttribute(k_phr_level<WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       SORT_SMEM_MAX * 12));
     int levels = 0;
     while (n_jobs > 0) {
         // one-warp blocks when every cut is small; WIDE-thread blocks for levels of a few
         // large cuts (the first ones), PT-thread blocks otherwise
         const int variant = nmax <= PHR_SMALL_CUT ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
-        // work items: one-warp blocks take a second-list job or 32 lane-list jobs
-        const uint32_t items = variant == 0 ? n_big + (n_lane + 31) / 32 : n_jobs;
-        const uint32_t grid = std::min<uint32_t>(items, max_grid[variant]);
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
         if (nmax > (1u << 28)) {
@@ -1624,11 +1656,22 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
             return gbt_fail(ctx, GBT_ENOMEM, "phr: cut too large");
         }
         const uint32_t cap = nmax << (bf > 2 ? bf - 2 : 0);
+        const uint32_t sort_p = pow2_at_least(cap > 0 ? cap : 1);
+        const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
+        // grid: at most the blocks that are resident at once
+        int per_sm = 0;
+        if (variant == 0) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32>, 32, 0));
+        else if (variant == 1) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<PT>, PT, dyn));
+        else GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<WIDE>, WIDE, dyn));
+        const uint32_t max_grid = (uint32_t)ctx->num_sms * (uint32_t)std::max(1, per_sm);
+        // work items: one-warp blocks take a second-list job or 32 lane-list jobs
+        const uint32_t items = variant == 0 ? n_big + (n_lane + 31) / 32 : n_jobs;
+        const uint32_t grid = std::min<uint32_t>(items, max_grid);
         const size_t per_block = gbt_align(scratch_bytes_for(cap));
         if (per_block * grid > scratch_bytes) {
             // sized for every block the variant can have resident, so that later
             // levels seldom need to grow it
-            const size_t need = per_block * max_grid[variant];
+            const size_t need = per_block * max_grid;
             if (scratch) {
                 cudaStreamSynchronize(st);
                 cudaFree(scratch);
@@ -1668,12 +1711,13 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         A.cap = cap;
         A.scratch = static_cast<unsigned char *>(scratch);
         A.scratch_per_block = per_block;
+        A.sort_smem = dyn ? 1u : 0u;
         A.bf = bf;
         A.n_prim = N;
         A.err = ctx->d_error;
         if (variant == 0) k_phr_level<32><<<grid, 32, 0, st>>>(A);
-        else if (variant == 1) k_phr_level<PT><<<grid, PT, 0, st>>>(A);
-        else k_phr_level<WIDE><<<grid, WIDE, 0, st>>>(A);
+        else if (variant == 1) k_phr_level<PT><<<grid, PT, dyn, st>>>(A);
+        else k_phr_level<WIDE><<<grid, WIDE, dyn, st>>>(A);
         GBT_CUDA(ctx, cudaGetLastError());
         GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaMemcpyAsync(&hb->flags, ctx->d_error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
