@@ -90,6 +90,23 @@ __device__ __forceinline__ double surface(const float *lo, const float *hi) {
 
 
 
+// The float64 paths below are taken rarely (inside the float32 screening
+// band, or without screening).  Kept out of line, so that the compiler branches
+// around them instead of predicating their float64 operations into every pass.
+__device__ __noinline__ bool surface_below(const float *lo, const float *hi, double thr) {
+    return surface(lo, hi) < thr;
+}
+
+// minCost's float64 cost of a split (phr.go:423-445): right box and count, left box and count.
+__device__ __noinline__ double split_cost64(float rl0, float rl1, float rl2, float rh0, float rh1, float rh2,
+                                            uint32_t rc, float ll0, float ll1, float ll2, float lh0, float lh1,
+                                            float lh2, uint32_t lc) {
+    const float rl[3] = {rl0, rl1, rl2}, rh[3] = {rh0, rh1, rh2};
+    const float ll[3] = {ll0, ll1, ll2}, lh[3] = {lh0, lh1, lh2};
+    const double rcost = __dmul_rn(surface(rl, rh), (double)rc);
+    return __dadd_rn(rcost, __dmul_rn(surface(ll, lh), (double)lc));
+}
+
 struct BoxAgg {
     float lo[3], hi[3];
     uint32_t c;
@@ -351,17 +368,17 @@ __device__ Scratch carve(unsigned char *base, uint32_t nmax) {
 // sort.SliceStable by barycenter component: bitonic sort of (key, input
 // position), so equal keys keep their input order.
 __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
-                                 uint32_t *out, const Scratch &s) {
+                                 uint32_t *out, unsigned long long *skey, uint32_t *sval) {
     uint32_t P = pow2_at_least(n);
     for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
         if (i < n) {
             // the float64 barycenter (lo + hi) * 0.5, computed exactly from the float32 bounds
             const AuxNode &x = aux[in[i]];
-            s.skey[i] = gbt_phr::key_of_bits(gbt_phr::bary_bits(x.lo[axis], x.hi[axis]));
+            skey[i] = gbt_phr::key_of_bits(gbt_phr::bary_bits(x.lo[axis], x.hi[axis]));
         } else {
-            s.skey[i] = ~0ULL;
+            skey[i] = ~0ULL;
         }
-        s.sval[i] = i;
+        sval[i] = i;
     }
     __syncthreads();
     for (uint32_t k = 2; k <= P; k <<= 1) {
@@ -369,22 +386,22 @@ __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t
             for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
                 uint32_t l = i ^ j;
                 if (l > i) {
-                    unsigned long long ki = s.skey[i], kl = s.skey[l];
-                    uint32_t vi = s.sval[i], vl = s.sval[l];
+                    unsigned long long ki = skey[i], kl = skey[l];
+                    uint32_t vi = sval[i], vl = sval[l];
                     bool gt = ki > kl || (ki == kl && vi > vl);
                     bool asc = (i & k) == 0;
                     if (asc == gt) {
-                        s.skey[i] = kl;
-                        s.skey[l] = ki;
-                        s.sval[i] = vl;
-                        s.sval[l] = vi;
+                        skey[i] = kl;
+                        skey[l] = ki;
+                        sval[i] = vl;
+                        sval[l] = vi;
                     }
                 }
             }
             __syncthreads();
         }
     }
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = in[s.sval[i]];
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = in[sval[i]];
     __syncthreads();
 }
 
@@ -466,13 +483,13 @@ __device__ void warp_sort_axis_e(const AuxNode *__restrict__ aux, const uint32_t
 
 // stable_sort_axis for a one-warp block: registers up to 256 nodes, else the
 // shared-scratch network.
-__device__ void warp_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
-                               uint32_t *out, const Scratch &s) {
+__device__ __noinline__ void warp_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
+                               uint32_t *out, unsigned long long *skey, uint32_t *sval) {
     if (n <= 32) warp_sort_axis_e<1>(aux, in, n, axis, out);
     else if (n <= 64) warp_sort_axis_e<2>(aux, in, n, axis, out);
     else if (n <= 128) warp_sort_axis_e<4>(aux, in, n, axis, out);
     else if (n <= 256) warp_sort_axis_e<8>(aux, in, n, axis, out);
-    else stable_sort_axis(aux, in, n, axis, out, s);
+    else stable_sort_axis(aux, in, n, axis, out, skey, sval);
 }
 
 struct SahResult {
@@ -486,7 +503,7 @@ struct SahResult {
 // only positions within the screening slack of the least float32 cost are
 // evaluated in float64 (phr_exact.cuh): the float64 minimum is among them, so
 // the result is the same.
-__device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n, const float *clo,
+__device__ __forceinline__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n, const float *clo,
                               const float *chi, const Scratch &s, BoxAgg *s_tmp, BoxAgg *s_rank, double *s_cost,
                               uint32_t *s_idx, bool screen, double *s_nosplit) {
     const int t = threadIdx.x;
@@ -546,10 +563,9 @@ __device__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *o
     uint32_t bi = 0xffffffffu;
     for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
         if (screen && !(cost32(i) <= limit)) continue;
-        float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
-        float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
-        double rcost = __dmul_rn(surface(rl, rh), (double)s.rc[i]);
-        double cost = __dadd_rn(rcost, __dmul_rn(surface(ll, lh), (double)s.lc[i]));
+        const double cost = split_cost64(s.rb[0][i], s.rb[1][i], s.rb[2][i], s.rb[3][i], s.rb[4][i], s.rb[5][i],
+                                         s.rc[i], s.lb[0][i], s.lb[1][i], s.lb[2][i], s.lb[3][i], s.lb[4][i],
+                                         s.lb[5][i], s.lc[i]);
         if (cost < best || (cost == best && i < bi)) {
             best = cost;
             bi = i;
@@ -772,25 +788,25 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
         if (threadIdx.x == 0) s_nosplit = __longlong_as_double(0x7ff8000000000000ll);  // NaN: not yet taken
         __syncthreads();
-        // SweepSAH: x from the cut order, y from the x order
-        if (BS == 32) warp_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
-        else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S);
-        if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
-        else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S);
+        // SweepSAH: x from the cut order, y from the x order, z from the y order
+        // when x is cheaper than y, else from the x order
+        if (BS == 32) warp_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S.skey, S.sval);
+        else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S.skey, S.sval);
+        if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S.skey, S.sval);
+        else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S.skey, S.sval);
         SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
         SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+        const bool x_first = xs.cost < ys.cost;
+        const uint32_t *zsrc = x_first ? S.ord[1] : S.ord[0];
+        if (BS == 32) warp_sort_axis(A.aux, zsrc, n, 2, S.ord[2], S.skey, S.sval);
+        else stable_sort_axis(A.aux, zsrc, n, 2, S.ord[2], S.skey, S.sval);
+        SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
         SahResult win;
         int warr;
-        if (xs.cost < ys.cost) {  // z from the y order
-            if (BS == 32) warp_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
-            else stable_sort_axis(A.aux, S.ord[1], n, 2, S.ord[2], S);
-            SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+        if (x_first) {
             if (xs.cost < zs.cost) { win = xs; warr = 0; }
             else { win = zs; warr = 2; }
-        } else {  // z from the x order
-            if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
-            else stable_sort_axis(A.aux, S.ord[0], n, 2, S.ord[2], S);
-            SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
+        } else {
             if (ys.cost < zs.cost) { win = ys; warr = 1; }
             else { win = zs; warr = 2; }
         }
@@ -853,7 +869,7 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
                     const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
                     if (screen && s32 < thr_lo) keep = true;
                     else if (screen && s32 > thr_hi) keep = false;
-                    else keep = surface(x.lo, x.hi) < thr;
+                    else keep = surface_below(x.lo, x.hi, thr);
                 }
                 S.flag[i] = keep ? 1u : 2u;
                 loc += S.flag[i];
@@ -988,17 +1004,14 @@ struct LaneCut {
     uint32_t n, total;   // nodes, sum of their subtree sizes
     float lo[3], hi[3];  // the cut's box
     float ns32;          // float32 cost of not splitting
-    double ns64;         // its float64 value, once taken
-    bool ns_has;
 };
 
-// A minCost result: split position (0: not splitting is cheapest) of order k.
+// A minCost result: split position (0: not splitting is cheapest) of order k,
+// with the float32 value of its cost.
 struct LanePick {
     float c32;
-    double c64;
     uint32_t split;
     int k;
-    bool has64;
 };
 
 __device__ __forceinline__ const AuxNode &lane_node(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
@@ -1025,9 +1038,10 @@ __device__ void lane_sort(const AuxNode *__restrict__ aux, LaneScratch &L, int s
     }
 }
 
+// The float64 costs are evaluated out of line (see surface_below).
 // minCost's float64 cost of splitting order k before position i (phr.go:423-445).
-__device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k, uint32_t n,
-                                    uint32_t i, int ln) {
+__device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+                                                 uint32_t n, uint32_t i, int ln) {
     LaneBox l, r;
     lbox_empty(l);
     lbox_empty(r);
@@ -1046,111 +1060,91 @@ __device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux
     return __dadd_rn(rcost, __dmul_rn(surface(l.lo, l.hi), (double)lc));
 }
 
-__device__ __forceinline__ void lane_make64(LanePick &p, const AuxNode *__restrict__ aux, const LaneScratch &L, LaneCut &c, int ln) {
-    if (p.has64) return;
-    if (p.split) {
-        p.c64 = lane_split_cost64(aux, L, p.k, c.n, p.split, ln);
-    } else {
-        if (!c.ns_has) {
-            c.ns64 = __dmul_rn(surface(c.lo, c.hi), (double)c.total);
-            c.ns_has = true;
-        }
-        p.c64 = c.ns64;
-    }
-    p.has64 = true;
+// The float64 cost of a pick: its split's, or not splitting's (phr.go:432-439).
+__device__ __forceinline__ double lane_pick_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L,
+                                                   const LaneCut &c, int k, uint32_t split, int ln) {
+    return split ? lane_split_cost64(aux, L, k, c.n, split, ln) : __dmul_rn(surface(c.lo, c.hi), (double)c.total);
 }
 
-// a.cost < b.cost in float64
-__device__ __forceinline__ bool lane_less(LanePick &a, LanePick &b, const AuxNode *__restrict__ aux, const LaneScratch &L,
-                          LaneCut &c, int ln) {
-    if (!(a.has64 && b.has64)) {
+__device__ __noinline__ bool lane_less64(const AuxNode *__restrict__ aux, const LaneScratch &L, LaneCut c, int ka,
+                                         uint32_t sa, int kb, uint32_t sb, int ln) {
+    return lane_pick_cost64(aux, L, c, ka, sa, ln) < lane_pick_cost64(aux, L, c, kb, sb, ln);
+}
+
+// a.cost < b.cost as the float64 values compare: decided by the float32 values
+// when they are further apart than the screening slack
+__device__ __forceinline__ bool lane_less(const LanePick &a, const LanePick &b, const AuxNode *__restrict__ aux,
+                                          const LaneScratch &L, const LaneCut &c, bool screen, int ln) {
+    if (screen) {
         if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
         if (__fmul_rn(b.c32, gbt_phr::SCREEN_SLACK) < a.c32) return false;
-        lane_make64(a, aux, L, c, ln);
-        lane_make64(b, aux, L, c, ln);
     }
-    return a.c64 < b.c64;
+    return lane_less64(aux, L, c, a.k, a.split, b.k, b.split, ln);
+}
+
+// The first position of least float64 cost among those whose float32 cost is
+// at most `lim` (all positions when lim is +inf).
+__device__ __noinline__ uint32_t lane_first_min64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+                                                  uint32_t n, float lim, bool all, int ln) {
+    double bc = INFINITY;
+    uint32_t bi = 1;
+    for (uint32_t i = 1; i < n; i++) {
+        if (!all && !(L.c32[i][ln] <= lim)) continue;
+        const double d = lane_split_cost64(aux, L, k, n, i, ln);
+        if (d < bc) {
+            bc = d;
+            bi = i;
+        }
+    }
+    return bi;
 }
 
 // minCost (phr.go:414-459) over order k: the first cheapest split position,
 // or not splitting when that is not cheaper.
-__device__ LanePick lane_min_cost(const AuxNode *__restrict__ aux, LaneScratch &L, int k, LaneCut &c, bool screen,
-                                  int ln) {
+__device__ LanePick lane_min_cost(const AuxNode *__restrict__ aux, LaneScratch &L, int k, const LaneCut &c,
+                                  bool screen, int ln) {
     const uint32_t n = c.n;
     LanePick best;
     best.k = k;
-    best.has64 = false;
-    best.c64 = 0.0;
-    if (screen) {
-        LaneBox r;
-        lbox_empty(r);
-        uint32_t rc = 0;
-        for (uint32_t i = n - 1; i >= 1; i--) {
-            const AuxNode &x = lane_node(aux, L, k, i, ln);
-            lbox_add(r, x);
-            rc += x.size;
-            L.c32[i][ln] = __fmul_rn(gbt_phr::surface32(r.lo, r.hi), gbt_phr::count_f32(rc));
-        }
-        LaneBox l;
-        lbox_empty(l);
-        uint32_t lc = 0, mi = 1;
-        float m = INFINITY;
-        for (uint32_t i = 1; i < n; i++) {
-            const AuxNode &x = lane_node(aux, L, k, i - 1, ln);
-            lbox_add(l, x);
-            lc += x.size;
-            const float cc = __fadd_rn(L.c32[i][ln], __fmul_rn(gbt_phr::surface32(l.lo, l.hi), gbt_phr::count_f32(lc)));
-            L.c32[i][ln] = cc;
-            if (cc < m) {
-                m = cc;
-                mi = i;
-            }
-        }
-        // positions whose float32 cost is within the slack of the least one
-        const float lim = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
-        uint32_t cand = 0;
-        for (uint32_t i = 1; i < n; i++) cand += L.c32[i][ln] <= lim ? 1u : 0u;
-        best.c32 = m;
-        best.split = mi;
-        if (cand > 1) {  // decided in float64 among the candidates, first minimum wins
-            double bc = INFINITY;
-            uint32_t bi = mi;
-            for (uint32_t i = 1; i < n; i++) {
-                if (!(L.c32[i][ln] <= lim)) continue;
-                const double d = lane_split_cost64(aux, L, k, n, i, ln);
-                if (d < bc) {
-                    bc = d;
-                    bi = i;
-                }
-            }
-            best.split = bi;
-            best.c32 = L.c32[bi][ln];
-            best.c64 = bc;
-            best.has64 = true;
-        }
-    } else {
-        double bc = INFINITY;
-        uint32_t bi = 1;
-        for (uint32_t i = 1; i < n; i++) {
-            const double d = lane_split_cost64(aux, L, k, n, i, ln);
-            if (d < bc) {
-                bc = d;
-                bi = i;
-            }
-        }
-        best.split = bi;
-        best.c32 = 0.f;
-        best.c64 = bc;
-        best.has64 = true;
+    // float32 costs of every split position
+    LaneBox r;
+    lbox_empty(r);
+    uint32_t rc = 0;
+    for (uint32_t i = n - 1; i >= 1; i--) {
+        const AuxNode &x = lane_node(aux, L, k, i, ln);
+        lbox_add(r, x);
+        rc += x.size;
+        L.c32[i][ln] = __fmul_rn(gbt_phr::surface32(r.lo, r.hi), gbt_phr::count_f32(rc));
     }
+    LaneBox l;
+    lbox_empty(l);
+    uint32_t lc = 0, mi = 1;
+    float m = INFINITY;
+    for (uint32_t i = 1; i < n; i++) {
+        const AuxNode &x = lane_node(aux, L, k, i - 1, ln);
+        lbox_add(l, x);
+        lc += x.size;
+        const float cc = __fadd_rn(L.c32[i][ln], __fmul_rn(gbt_phr::surface32(l.lo, l.hi), gbt_phr::count_f32(lc)));
+        L.c32[i][ln] = cc;
+        if (cc < m) {
+            m = cc;
+            mi = i;
+        }
+    }
+    // positions whose float32 cost is within the slack of the least one
+    const float lim = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
+    uint32_t cand = 0;
+    for (uint32_t i = 1; i < n; i++) cand += L.c32[i][ln] <= lim ? 1u : 0u;
+    best.split = mi;
+    if (!screen || cand > 1) {  // decided in float64 (among the candidates), first minimum wins
+        best.split = lane_first_min64(aux, L, k, n, lim, !screen, ln);
+    }
+    best.c32 = L.c32[best.split][ln];
     LanePick ns;
     ns.k = k;
     ns.split = 0;
     ns.c32 = c.ns32;
-    ns.has64 = false;
-    ns.c64 = 0.0;
-    if (!screen) lane_make64(ns, aux, L, c, ln);
-    if (lane_less(best, ns, aux, L, c, ln)) return best;
+    if (lane_less(best, ns, aux, L, c, screen, ln)) return best;
     return ns;
 }
 
@@ -1211,18 +1205,16 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
             c.hi[a] = job.hi[a];
         }
         c.ns32 = __fmul_rn(gbt_phr::surface32(c.lo, c.hi), gbt_phr::count_f32(c.total));
-        c.ns_has = false;
-        c.ns64 = 0.0;
         lane_sort(aux, L, -1, 0, 0, n, ln);
         LanePick xs = lane_min_cost(aux, L, 0, c, screen, ln);
         lane_sort(aux, L, 0, 1, 1, n, ln);
         LanePick ys = lane_min_cost(aux, L, 1, c, screen, ln);
         // z from the y order when x is cheaper than y, else from the x order
-        const bool x_first = lane_less(xs, ys, aux, L, c, ln);
+        const bool x_first = lane_less(xs, ys, aux, L, c, screen, ln);
         lane_sort(aux, L, x_first ? 1 : 0, 2, 2, n, ln);
         LanePick zs = lane_min_cost(aux, L, 2, c, screen, ln);
         LanePick other = x_first ? xs : ys;
-        const LanePick win = lane_less(other, zs, aux, L, c, ln) ? other : zs;
+        const LanePick win = lane_less(other, zs, aux, L, c, screen, ln) ? other : zs;
         my_build_cost += n;
         k = win.k;
         split = win.split;
@@ -1246,7 +1238,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
                         const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
                         if (screen && s32 < thr_lo) kept = true;
                         else if (screen && s32 > thr_hi) kept = false;
-                        else kept = surface(x.lo, x.hi) < thr;
+                        else kept = surface_below(x.lo, x.hi, thr);
                     }
                     if (kept) keep[s] |= 1u << (i - a);
                     tot[s] += kept ? 1u : 2u;

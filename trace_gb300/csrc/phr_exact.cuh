@@ -25,8 +25,11 @@
 
 #ifdef __CUDACC__
 #define GBT_HD __host__ __device__ __forceinline__
+// out of line: a rare path the compiler would otherwise predicate into every call
+#define GBT_HD_RARE static __host__ __device__ __noinline__
 #else
 #define GBT_HD inline
+#define GBT_HD_RARE static inline
 #endif
 
 namespace gbt_phr {
@@ -57,6 +60,12 @@ GBT_HD int clz64(uint64_t x) {
 #else
     return __builtin_clzll(x);
 #endif
+}
+
+// The rounded float64 form of bary_bits, for the operands it cannot sum exactly.
+GBT_HD_RARE uint64_t bary_bits_rounded(float a, float b) {
+    const double s = (double)a + (double)b;  // rounded (or inf/NaN): float64 as the reference
+    return f64_bits(s * 0.5);
 }
 
 // fl64(fl64((double)a + (double)b) * 0.5) as bits.
@@ -93,8 +102,7 @@ GBT_HD uint64_t bary_bits(float a, float b) {
             return (sign << 63) | ((uint64_t)(e2 - 1 + 1023) << 52) | frac;  // times 0.5
         }
     }
-    const double s = (double)a + (double)b;  // rounded (or inf/NaN): float64 as the reference
-    return f64_bits(s * 0.5);
+    return bary_bits_rounded(a, b);
 }
 
 // Orders like the float64 value (sort key of the bits).
