@@ -492,20 +492,76 @@ __device__ __noinline__ void warp_sort_axis(const AuxNode *__restrict__ aux, con
     else stable_sort_axis(aux, in, n, axis, out, skey, sval);
 }
 
+// A minCost result.  Its float64 cost is taken only when a comparison needs it
+// (sah_less): from the split's boxes and subtree sizes, or for not splitting
+// (split 0) from the cut's box (llo, lhi) and all of its subtree sizes (rc).
 struct SahResult {
-    double cost;
-    uint32_t split;  // 0: not splitting is cheapest
+    float c32;        // float32 value of the cost
+    uint32_t split;   // 0: not splitting is cheapest
+    uint32_t lc, rc;  // subtree sizes left and right of the split
     float llo[3], lhi[3], rlo[3], rhi[3];
 };
 
-// minCost (phr.go:414-459) over the order `ord`.
-// With `screen`, every split position's cost is first taken in float32 and
-// only positions within the screening slack of the least float32 cost are
-// evaluated in float64 (phr_exact.cuh): the float64 minimum is among them, so
-// the result is the same.
-__device__ __forceinline__ SahResult min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n, const float *clo,
-                              const float *chi, const Scratch &s, BoxAgg *s_tmp, BoxAgg *s_rank, double *s_cost,
-                              uint32_t *s_idx, bool screen, double *s_nosplit) {
+__device__ __noinline__ double nosplit_cost64(float l0, float l1, float l2, float h0, float h1, float h2,
+                                              uint32_t total) {
+    const float lo[3] = {l0, l1, l2}, hi[3] = {h0, h1, h2};
+    return __dmul_rn(surface(lo, hi), (double)total);
+}
+
+__device__ __forceinline__ double sah_cost64(const SahResult &r) {
+    if (r.split == 0) return nosplit_cost64(r.llo[0], r.llo[1], r.llo[2], r.lhi[0], r.lhi[1], r.lhi[2], r.rc);
+    return split_cost64(r.rlo[0], r.rlo[1], r.rlo[2], r.rhi[0], r.rhi[1], r.rhi[2], r.rc, r.llo[0], r.llo[1],
+                        r.llo[2], r.lhi[0], r.lhi[1], r.lhi[2], r.lc);
+}
+
+// a.cost < b.cost as the float64 values compare: decided by the float32 values
+// when they are further apart than the screening slack (phr_exact.cuh)
+__device__ __forceinline__ bool sah_less(const SahResult &a, const SahResult &b, bool screen) {
+    if (a.split == 0 && b.split == 0) return false;  // both are the cost of not splitting the cut
+    if (screen) {
+        if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
+        if (__fmul_rn(b.c32, gbt_phr::SCREEN_SLACK) < a.c32) return false;
+    }
+    return sah_cost64(a) < sah_cost64(b);
+}
+
+// Block-wide first minimum of (value, index) pairs; every thread gets it.
+__device__ __forceinline__ void block_argmin_f32(float &v, uint32_t &idx, float *s_v, uint32_t *s_i) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const uint32_t i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (v2 < v || (v2 == v && i2 < idx)) {
+            v = v2;
+            idx = i2;
+        }
+    }
+    const int t = threadIdx.x, nw = blockDim.x >> 5;
+    if ((t & 31) == 0) {
+        s_v[t >> 5] = v;
+        s_i[t >> 5] = idx;
+    }
+    __syncthreads();
+    for (int w = 0; w < nw; w++) {
+        const float v2 = s_v[w];
+        const uint32_t i2 = s_i[w];
+        if (v2 < v || (v2 == v && i2 < idx)) {
+            v = v2;
+            idx = i2;
+        }
+    }
+    __syncthreads();
+}
+
+// minCost (phr.go:414-459) over the order `ord`: the first split position of
+// least float64 cost, or not splitting when that is not cheaper.  Every
+// position's cost is taken in float32; with `screen` only the positions within
+// the screening slack of the least float32 cost are candidates, and a single
+// candidate needs no float64 at all (phr_exact.cuh).
+// The result goes to *s_out (shared memory, written by thread 0).
+__device__ __forceinline__ void min_cost(const AuxNode *__restrict__ aux, const uint32_t *ord, uint32_t n,
+                                         const float *clo, const float *chi, const Scratch &s, BoxAgg *s_tmp,
+                                         BoxAgg *s_rank, double *s_cost, uint32_t *s_idx, bool screen,
+                                         SahResult *s_out) {
     const int t = threadIdx.x;
     const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
     const uint32_t a = min(n, t * chunk), b = min(n, a + chunk);
@@ -540,78 +596,96 @@ __device__ __forceinline__ SahResult min_cost(const AuxNode *__restrict__ aux, c
         s.rc[i - 1] = suf.c;
     }
     __syncthreads();
-    // costs for every split position, first minimum wins
     auto cost32 = [&](uint32_t i) {
         const float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
         const float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
         return __fadd_rn(__fmul_rn(gbt_phr::surface32(rl, rh), gbt_phr::count_f32(s.rc[i])),
                          __fmul_rn(gbt_phr::surface32(ll, lh), gbt_phr::count_f32(s.lc[i])));
     };
-    float limit = INFINITY;  // positions with a float32 cost above this cannot be the minimum
-    if (screen) {
-        float m = INFINITY;
-        for (uint32_t i = 1 + t; i < n; i += blockDim.x) m = fminf(m, cost32(i));
-        for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        float *s_m = reinterpret_cast<float *>(s_cost);
-        if ((t & 31) == 0) s_m[t >> 5] = m;
-        __syncthreads();
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fminf(m, s_m[w]);
-        __syncthreads();
-        limit = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
-    }
-    double best = INFINITY;
-    uint32_t bi = 0xffffffffu;
+    float *s_f = reinterpret_cast<float *>(s_cost);
+    // least float32 cost, first position
+    float m = INFINITY;
+    uint32_t mi = 0xffffffffu;
     for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
-        if (screen && !(cost32(i) <= limit)) continue;
-        const double cost = split_cost64(s.rb[0][i], s.rb[1][i], s.rb[2][i], s.rb[3][i], s.rb[4][i], s.rb[5][i],
-                                         s.rc[i], s.lb[0][i], s.lb[1][i], s.lb[2][i], s.lb[3][i], s.lb[4][i],
-                                         s.lb[5][i], s.lc[i]);
-        if (cost < best || (cost == best && i < bi)) {
-            best = cost;
-            bi = i;
+        const float c = cost32(i);
+        if (c < m) {
+            m = c;
+            mi = i;
         }
     }
-    // the cost of not splitting, the same for every axis: taken once per cut (NaN until then)
-    if (t == 0 && !(*s_nosplit >= 0.0)) *s_nosplit = __dmul_rn(surface(clo, chi), (double)s.rc[0]);
-    s_cost[t] = best;
-    s_idx[t] = bi;
-    __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1) {
-        if (t < off) {
-            double c2 = s_cost[t + off];
-            uint32_t i2 = s_idx[t + off];
-            if (c2 < s_cost[t] || (c2 == s_cost[t] && i2 < s_idx[t])) {
-                s_cost[t] = c2;
-                s_idx[t] = i2;
+    block_argmin_f32(m, mi, s_f, s_idx);
+    const float lim = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
+    uint32_t cand = 0;
+    if (screen) {
+        for (uint32_t i = 1 + t; i < n; i += blockDim.x) cand += cost32(i) <= lim ? 1u : 0u;
+        for (int o = 16; o > 0; o >>= 1) cand += __shfl_xor_sync(0xffffffffu, cand, o);
+        if ((t & 31) == 0) s_idx[t >> 5] = cand;
+        __syncthreads();
+        cand = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) cand += s_idx[w];
+        __syncthreads();
+    }
+    uint32_t bidx = mi;
+    if (n > 1 && (!screen || cand > 1)) {
+        // float64 among the candidates (every position without screening), first minimum wins
+        double best = INFINITY;
+        uint32_t bi = 0xffffffffu;
+        for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
+            if (screen && !(cost32(i) <= lim)) continue;
+            const double cost = split_cost64(s.rb[0][i], s.rb[1][i], s.rb[2][i], s.rb[3][i], s.rb[4][i], s.rb[5][i],
+                                             s.rc[i], s.lb[0][i], s.lb[1][i], s.lb[2][i], s.lb[3][i], s.lb[4][i],
+                                             s.lb[5][i], s.lc[i]);
+            if (cost < best || (cost == best && i < bi)) {
+                best = cost;
+                bi = i;
             }
         }
+        s_cost[t] = best;
+        s_idx[t] = bi;
+        __syncthreads();
+        for (int off = blockDim.x / 2; off > 0; off >>= 1) {
+            if (t < off) {
+                double c2 = s_cost[t + off];
+                uint32_t i2 = s_idx[t + off];
+                if (c2 < s_cost[t] || (c2 == s_cost[t] && i2 < s_idx[t])) {
+                    s_cost[t] = c2;
+                    s_idx[t] = i2;
+                }
+            }
+            __syncthreads();
+        }
+        bidx = s_idx[0];
         __syncthreads();
     }
-    SahResult r;
-    const double nosplit = *s_nosplit;
-    double bc = s_cost[0];
-    uint32_t bidx = s_idx[0];
-    __syncthreads();
-    if (n > 1 && bc < nosplit) {
-        r.cost = bc;
-        r.split = bidx;
+    if (t == 0) {
+        SahResult sp, ns;  // the best split, and not splitting
+        ns.split = 0;
+        ns.lc = 0;
+        ns.rc = s.rc[0];
+        ns.c32 = __fmul_rn(gbt_phr::surface32(clo, chi), gbt_phr::count_f32(ns.rc));
         for (int k = 0; k < 3; k++) {
-            r.llo[k] = s.lb[k][bidx];
-            r.lhi[k] = s.lb[3 + k][bidx];
-            r.rlo[k] = s.rb[k][bidx];
-            r.rhi[k] = s.rb[3 + k][bidx];
+            ns.llo[k] = clo[k];
+            ns.lhi[k] = chi[k];
+            ns.rlo[k] = 0.f;
+            ns.rhi[k] = 0.f;
         }
-    } else {
-        r.cost = nosplit;
-        r.split = 0;
-        for (int k = 0; k < 3; k++) {
-            r.llo[k] = clo[k];
-            r.lhi[k] = chi[k];
-            r.rlo[k] = 0.f;
-            r.rhi[k] = 0.f;
+        bool split = false;
+        if (n > 1 && bidx < n) {
+            sp.split = bidx;
+            sp.c32 = cost32(bidx);
+            sp.lc = s.lc[bidx];
+            sp.rc = s.rc[bidx];
+            for (int k = 0; k < 3; k++) {
+                sp.llo[k] = s.lb[k][bidx];
+                sp.lhi[k] = s.lb[3 + k][bidx];
+                sp.rlo[k] = s.rb[k][bidx];
+                sp.rhi[k] = s.rb[3 + k][bidx];
+            }
+            split = sah_less(sp, ns, screen);
         }
+        *s_out = split ? sp : ns;
     }
-    return r;
+    __syncthreads();  // the result is out, and the next sweep may rewrite the scratch
 }
 
 struct Cut {  // a cut inside a job: a node list in the output pool, or a finished leaf
@@ -676,10 +750,10 @@ struct BlockShared {
     BoxAgg tmp[BS / 32];
     BoxAgg rank[BS];
     double cost[BS];
-    double nosplit;
     uint32_t idx[BS];
     uint32_t u[32];
     Cut cuts[4];
+    SahResult res[3];  // minCost of the x, y and z orders
     int32_t branch, ncuts;
     uint32_t off;
 };
@@ -713,7 +787,6 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
     BoxAgg *s_tmp = sh.tmp;
     BoxAgg *s_rank = sh.rank;
     double *s_cost = sh.cost;
-    double &s_nosplit = sh.nosplit;
     uint32_t *s_idx = sh.idx;
     uint32_t *s_u = sh.u;
     Cut *s_cuts = sh.cuts;
@@ -786,7 +859,6 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
             break;
         }
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) S.ids[i] = cut.src[i];
-        if (threadIdx.x == 0) s_nosplit = __longlong_as_double(0x7ff8000000000000ll);  // NaN: not yet taken
         __syncthreads();
         // SweepSAH: x from the cut order, y from the x order, z from the y order
         // when x is cheaper than y, else from the x order
@@ -794,22 +866,16 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
         else stable_sort_axis(A.aux, S.ids, n, 0, S.ord[0], S.skey, S.sval);
         if (BS == 32) warp_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S.skey, S.sval);
         else stable_sort_axis(A.aux, S.ord[0], n, 1, S.ord[1], S.skey, S.sval);
-        SahResult xs = min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-        SahResult ys = min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-        const bool x_first = xs.cost < ys.cost;
+        SahResult *res = sh.res;  // x, y, z
+        min_cost(A.aux, S.ord[0], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &res[0]);
+        min_cost(A.aux, S.ord[1], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &res[1]);
+        const bool x_first = sah_less(res[0], res[1], screen);
         const uint32_t *zsrc = x_first ? S.ord[1] : S.ord[0];
         if (BS == 32) warp_sort_axis(A.aux, zsrc, n, 2, S.ord[2], S.skey, S.sval);
         else stable_sort_axis(A.aux, zsrc, n, 2, S.ord[2], S.skey, S.sval);
-        SahResult zs = min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &s_nosplit);
-        SahResult win;
-        int warr;
-        if (x_first) {
-            if (xs.cost < zs.cost) { win = xs; warr = 0; }
-            else { win = zs; warr = 2; }
-        } else {
-            if (ys.cost < zs.cost) { win = ys; warr = 1; }
-            else { win = zs; warr = 2; }
-        }
+        min_cost(A.aux, S.ord[2], n, cut.lo, cut.hi, S, s_tmp, s_rank, s_cost, s_idx, screen, &res[2]);
+        const int warr = x_first ? (sah_less(res[0], res[2], screen) ? 0 : 2) : (sah_less(res[1], res[2], screen) ? 1 : 2);
+        const SahResult &win = res[warr];
         const uint32_t *ord = warr == 0 ? S.ord[0] : (warr == 1 ? S.ord[1] : S.ord[2]);
         if (win.split == 0) {
             // makeLeaf(left.bounding, left.nodes...) over the winning order
@@ -1075,9 +1141,19 @@ __device__ __noinline__ bool lane_less64(const AuxNode *__restrict__ aux, const 
 // when they are further apart than the screening slack
 __device__ __forceinline__ bool lane_less(const LanePick &a, const LanePick &b, const AuxNode *__restrict__ aux,
                                           const LaneScratch &L, const LaneCut &c, bool screen, int ln) {
+    if (a.split == 0 && b.split == 0) return false;  // both are the cost of not splitting
     if (screen) {
         if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
         if (__fmul_rn(b.c32, gbt_phr::SCREEN_SLACK) < a.c32) return false;
+    }
+    if (a.split && b.split) {
+        // two orders that split the cut into the same two sides (always so for two
+        // nodes) give bit-equal costs: the same unions, sizes and float64 sum
+        uint32_t ma = 0, mb = 0;
+        for (uint32_t i = 0; i < a.split; i++) ma |= 1u << L.ord[a.k][i][ln];
+        for (uint32_t i = 0; i < b.split; i++) mb |= 1u << L.ord[b.k][i][ln];
+        const uint32_t full = (1u << c.n) - 1u;
+        if (ma == mb || ma == (full ^ mb)) return false;
     }
     return lane_less64(aux, L, c, a.k, a.split, b.k, b.split, ln);
 }
