@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include "gbt_internal.cuh"
+#include "morton_exact.cuh"
 
 namespace {
 
@@ -206,35 +207,50 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
                                                 uint32_t n_tri, uint32_t n, const unsigned long long *__restrict__ acc,
                                                 uint64_t *__restrict__ codes) {
     __shared__ double s_e[9];  // lo.xyz, step.xyz, 1/step.xyz
+    __shared__ float s_f[15];  // lo.xyz and 1/step.xyz as float pairs, margin.xyz
     if (threadIdx.x < 3) {
         int k = threadIdx.x;
         double lo = ord_to_dbl(acc[k]), hi = ord_to_dbl(acc[3 + k]);
         double ext = __dsub_rn(hi, lo);                 // aabb.update width/height/depth
         double step = __ddiv_rn(ext, 2097151.0);        // extent / (MORTON_SIZE-1)
+        double rstep = __drcp_rn(step);
         s_e[k] = lo;
         s_e[3 + k] = step;
-        s_e[6 + k] = __drcp_rn(step);
+        s_e[6 + k] = rstep;
+        const gbt_morton::AxisF32x2 f = gbt_morton::axis_setup(lo, hi, rstep);
+        s_f[k] = f.lo_h;
+        s_f[3 + k] = f.lo_l;
+        s_f[6 + k] = f.rs_h;
+        s_f[9 + k] = f.rs_l;
+        s_f[12 + k] = f.margin;
     }
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double lo[3], hi[3];
+        uint64_t q[3];
         if (i < n_tri) {
             const float *t = verts + (size_t)i * 9;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 const float a = __ldg(t + k), b = __ldg(t + 3 + k), c = __ldg(t + 6 + k);
-                lo[k] = widen(fminf(fminf(a, b), c));
-                hi[k] = widen(fmaxf(fmaxf(a, b), c));
+                const float mn = fminf(fminf(a, b), c), mx = fmaxf(fmaxf(a, b), c);
+                const int64_t f = gbt_morton::quantise_f32x2(mn, mx, s_f[k], s_f[3 + k], s_f[6 + k], s_f[9 + k], s_f[12 + k]);
+                if (f >= 0) {
+                    q[k] = (uint64_t)f;
+                } else {  // the float64 path: the reference's operations
+                    const double cb = halve(__dadd_rn(widen(mn), widen(mx)));  // aabb barycenter
+                    const double dx = __longlong_as_double(__double_as_longlong(__dsub_rn(s_e[k], cb)) & 0x7fffffffffffffffll);
+                    q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
+                }
             }
         } else {
+            double lo[3], hi[3];
             prim_box_f64(verts, sph, n_tri, i, lo, hi);
-        }
-        uint64_t q[3];
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const double c = halve(__dadd_rn(lo[k], hi[k]));  // aabb barycenter
-            const double dx = __longlong_as_double(__double_as_longlong(__dsub_rn(s_e[k], c)) & 0x7fffffffffffffffll);
-            q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
+            for (int k = 0; k < 3; k++) {
+                const double cb = halve(__dadd_rn(lo[k], hi[k]));
+                const double dx = __longlong_as_double(__double_as_longlong(__dsub_rn(s_e[k], cb)) & 0x7fffffffffffffffll);
+                q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
+            }
         }
         codes[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
     }
