@@ -117,6 +117,10 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
  *                          the first render on a tree measures the packet
  *                          kernel faster on its camera rays (that render traces
  *                          them with both kernels and synchronises once)
+ *   GBT_OPT_KEEP_WORKSPACE 1 (default): a PHR refinement leaves its device
+ *                          workspace (about 600 bytes per auxiliary-tree
+ *                          triangle) on the context for the next one; 0 frees
+ *                          it now and after every refinement
  * The environment variables GBT_TRAVERSAL (persistent|simple|ww),
  * GBT_ANYHIT_LAST, GBT_PRIMARY_TILES (0|1) and GBT_PRIMARY_PACKETS (0|1|2) set
  * the initial values.
@@ -125,6 +129,7 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
 #define GBT_OPT_ANYHIT_LAST 1
 #define GBT_OPT_PRIMARY_TILES 2
 #define GBT_OPT_PRIMARY_PACKETS 3
+#define GBT_OPT_KEEP_WORKSPACE 4
 int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */

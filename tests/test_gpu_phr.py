@@ -36,6 +36,26 @@ def test_phr_matches_oracle_tree(ctx, name, make, alpha, delta, bf):
     assert g.Cost() == oc  # the device evaluates the recursion's float64 operations in its order
 
 
+def test_phr_workspace_kept_or_released_gives_the_same_tree(ctx):
+    """Refinements that reuse the context's workspace (default), grow it, and
+    free it after every build (GBT_OPT_KEEP_WORKSPACE 0) give the same tree."""
+    big = scenes.soup(50_000, seed=5)["verts"]
+    small = scenes.soup(3000, seed=7)["verts"]
+    aux_big = pt.DefaultLBVH(pt.DeviceScene(ctx, big))
+    aux_small = pt.DefaultLBVH(pt.DeviceScene(ctx, small))
+    ref_small = O.lbvh(small).phr(0.5, 6.0, 2).export()
+    ref_big = O.lbvh(big).phr(0.5, 6.0, 2).export()
+    try:
+        for keep in (1, 0):
+            ctx.set_option("keep_workspace", keep)
+            for aux, ref in ((aux_small, ref_small), (aux_big, ref_big), (aux_small, ref_small)):
+                g = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(aux)
+                ge = g.export()
+                assert canonical_equal(ge, ref), first_mismatch(ge, ref)
+    finally:
+        ctx.set_option("keep_workspace", 1)
+
+
 @pytest.mark.parametrize("alpha,delta,bf", [(0.5, 6.0, 2), (0.55, 9.0, 2), (0.5, 6.0, 4)])
 def test_phr_1m_soup(ctx, alpha, delta, bf):
     s = scenes.soup(1_000_000, seed=1)

@@ -41,6 +41,14 @@ int gbt_check_device_error(gbt_ctx *ctx, const char *what) {
     return gbt_fail(ctx, (flags & GBT_DEVERR_SPIN) ? GBT_ETIMEOUT : GBT_EDEVICE, m);
 }
 
+void *gbt_pinned(gbt_ctx *ctx) {
+    if (!ctx->h_pin && cudaMallocHost(&ctx->h_pin, GBT_PINNED_BYTES) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->h_pin = nullptr;
+    }
+    return ctx->h_pin;
+}
+
 int gbt_scratch(gbt_ctx *ctx, size_t bytes, void **out) {
     if (ctx->scratch_bytes < bytes) {
         if (ctx->scratch_pins > 0)
@@ -125,6 +133,8 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_out) cudaFree(ctx->d_out);
     if (ctx->bstate) cudaFree(ctx->bstate);
+    gbt_phr_release(ctx);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     for (auto &e : ctx->prof_ev) cudaEventDestroy(e);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -165,6 +175,14 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
     case GBT_OPT_PRIMARY_PACKETS:
         if (value < 0 || value > 2) return gbt_fail(ctx, GBT_EINVAL, "set_option: packets must be 0, 1 or 2");
         ctx->primary_packets = value;
+        return GBT_OK;
+    case GBT_OPT_KEEP_WORKSPACE:
+        if (value < 0 || value > 1) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 0 or 1");
+        ctx->keep_workspace = value;
+        if (!value) {
+            GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            gbt_phr_release(ctx);
+        }
         return GBT_OK;
     default:
         return gbt_fail(ctx, GBT_EINVAL, "set_option: unknown option " + std::to_string(option));
@@ -279,6 +297,13 @@ extern "C" int gbt_scene_destroy(gbt_scene *s) {
 extern "C" int gbt_bvh_destroy(gbt_bvh *b) {
     if (!b) return GBT_EINVAL;
     if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+    if (b->d_block) {
+        cudaFree(b->d_block);
+        b->d_nodes = nullptr;
+        b->d_prims = nullptr;
+        b->d_hdr = nullptr;
+        b->d_parent = nullptr;
+    }
     cudaFree(b->d_nodes);
     cudaFree(b->d_prims);
     cudaFree(b->d_hdr);

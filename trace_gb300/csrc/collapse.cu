@@ -97,17 +97,10 @@ __device__ void collapse_one(const float4 *__restrict__ bin, int2 e, int2 *__res
     reinterpret_cast<int4 *>(nd)[7] = make_int4(cnt[0], cnt[1], cnt[2], cnt[3]);
 }
 
-// One level, one thread per queued node.
-__global__ void k_collapse_level(const float4 *__restrict__ bin, const int2 *__restrict__ q_in,
-                                 const uint32_t *__restrict__ n_in, int2 *__restrict__ q_out, uint32_t *n_out,
-                                 uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < *n_in) collapse_one(bin, q_in[i], q_out, n_out, n_nodes4, out, cap, err);
-}
-
 // Counters of the graph form: [0], [1] the two queues' sizes, [2] 4-wide nodes, [3] the input
 // queue of the current level, [4] levels done.
 constexpr uint32_t MAX_LEVELS = 4096;  // a tree deeper than this is reported, not walked
+constexpr int COLLAPSE_BATCH = 8;      // levels launched per readback (gbt_collapse4)
 
 // One level of the graph form over a fixed grid: the input queue is ctr[3]'s.
 __global__ void k_collapse_level_gs(const float4 *__restrict__ bin, int2 *q0, int2 *q1, uint32_t *ctr,
@@ -145,9 +138,22 @@ __device__ void k_collapse_root_body(const BvhHeader *__restrict__ hdr, BvhHeade
     }
 }
 
-__global__ void k_collapse_root(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q, uint32_t *n_q,
-                                uint32_t *n_nodes4) {
-    k_collapse_root_body(hdr, hdr4, q, n_q, n_nodes4);
+// The graph form's counters set up outside a graph (gbt_collapse4).
+__global__ void k_collapse_root_gs(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q0, uint32_t *ctr) {
+    k_collapse_root_body(hdr, hdr4, q0, ctr + 0, ctr + 2);
+    ctr[1] = 0;
+    ctr[3] = 0;
+    ctr[4] = 0;
+}
+
+// k_collapse_advance outside a graph: the output queue becomes the input.  After the
+// last level the next ones find an empty queue and do nothing.
+__global__ void k_collapse_step(uint32_t *ctr, unsigned int *err) {
+    const uint32_t par = ctr[3], next = par ^ 1;
+    ctr[par] = 0;
+    ctr[3] = next;
+    const uint32_t levels = ++ctr[4];
+    if (ctr[next] > 0 && levels >= MAX_LEVELS) atomicOr(err, GBT_DEVERR_CAPACITY);
 }
 
 __global__ void k_collapse_root_graph(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q0, uint32_t *ctr,
@@ -196,19 +202,22 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
     int rc = gbt_scratch(ctx, 2 * qbytes + 256, &scr);
     if (rc) return rc;
     unsigned char *sb = static_cast<unsigned char *>(scr);
-    int2 *q[2] = {reinterpret_cast<int2 *>(sb), reinterpret_cast<int2 *>(sb + qbytes)};
-    uint32_t *ctr = reinterpret_cast<uint32_t *>(sb + 2 * qbytes);  // [0],[1] queue sizes, [2] node count
-    k_collapse_root<<<1, 1, 0, st>>>(bvh->d_hdr, bvh->d_hdr4, q[0], ctr + 0, ctr + 2);
-    uint32_t n_in = h.root_cnt == 0 ? 1u : 0u;
-    int par = 0;
-    while (n_in > 0) {
-        GBT_CUDA(ctx, cudaMemsetAsync(ctr + (par ^ 1), 0, sizeof(uint32_t), st));
-        k_collapse_level<<<(n_in + 127) / 128, 128, 0, st>>>(bvh->d_nodes, q[par], ctr + par, q[par ^ 1],
-                                                             ctr + (par ^ 1), ctr + 2, bvh->d_nodes4, cap, ctx->d_error);
+    int2 *q0 = reinterpret_cast<int2 *>(sb), *q1 = reinterpret_cast<int2 *>(sb + qbytes);
+    uint32_t *ctr = reinterpret_cast<uint32_t *>(sb + 2 * qbytes);  // the graph form's counters
+    uint32_t *hc = static_cast<uint32_t *>(gbt_pinned(ctx));
+    if (!hc) return gbt_fail(ctx, GBT_ENOMEM, "collapse: pinned host allocation");
+    k_collapse_root_gs<<<1, 1, 0, st>>>(bvh->d_hdr, bvh->d_hdr4, q0, ctr);
+    // levels in batches of COLLAPSE_BATCH launches between readbacks of the counters
+    for (;;) {
+        for (int b = 0; b < COLLAPSE_BATCH; b++) {
+            k_collapse_level_gs<<<(unsigned)ctx->num_sms * 4, 128, 0, st>>>(bvh->d_nodes, q0, q1, ctr, bvh->d_nodes4,
+                                                                            cap, ctx->d_error);
+            k_collapse_step<<<1, 1, 0, st>>>(ctr, ctx->d_error);
+        }
         GBT_CUDA(ctx, cudaGetLastError());
-        GBT_CUDA(ctx, cudaMemcpyAsync(&n_in, ctr + (par ^ 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        GBT_CUDA(ctx, cudaMemcpyAsync(hc, ctr, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaStreamSynchronize(st));
-        par ^= 1;
+        if (hc[hc[3] & 1u] == 0 || hc[4] >= MAX_LEVELS) break;
     }
     bvh->has_nodes4 = 1;
     return GBT_OK;

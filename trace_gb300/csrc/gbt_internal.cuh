@@ -59,7 +59,21 @@ struct gbt_ctx {
     // kernel the first render on a BVH measures faster for its camera rays
     int primary_packets = 2;
     cudaEvent_t tune_ev[3] = {nullptr, nullptr, nullptr};
+    // PHR workspace (phr.cu): the build's temporaries and its per-block scratch, kept for the
+    // next refinement unless GBT_OPT_KEEP_WORKSPACE is 0
+    void *phr_ws = nullptr;
+    size_t phr_ws_bytes = 0;
+    void *phr_scr = nullptr;
+    size_t phr_scr_bytes = 0;
+    int keep_workspace = 1;
+    void *h_pin = nullptr;  // small pinned host buffer for counter readbacks (gbt_pinned)
 };
+
+// A pinned host buffer of GBT_PINNED_BYTES owned by the context (allocated on first use).
+#define GBT_PINNED_BYTES 4096
+void *gbt_pinned(gbt_ctx *ctx);
+// Frees the PHR workspace kept on the context.
+void gbt_phr_release(gbt_ctx *ctx);
 
 // Record a profiling event pair around one traversal launch.
 void gbt_prof_begin(gbt_ctx *ctx);
@@ -118,6 +132,7 @@ struct gbt_bvh {
     uint32_t nodes4_cap = 0;
     int has_nodes4 = 0;
     int packet_choice = 0;          // camera-ray kernel measured for this tree: 0 not yet, 1 packets, 2 single rays
+    void *d_block = nullptr;        // when set: d_nodes, d_prims, d_parent and d_hdr are pieces of this allocation
 };
 
 // collapse.cu

@@ -31,6 +31,7 @@ constexpr uint32_t MAX_CUT_SIZE = 2500;  // phr.go:11
 constexpr int PT = 256;                  // threads per job block
 constexpr int WIDE = 512;                // threads per job block on levels of a few large cuts
 constexpr uint32_t SORT_SMEM_MAX = 8192; // largest padded cut sorted in shared memory (96 KB)
+constexpr int SPEC_LEVELS = 8;           // small-cut levels launched per readback
 #ifndef PHR_SMALL_CUT
 #define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
 #endif
@@ -72,6 +73,11 @@ struct PhrGlobals {
     // sweeps (2..LANE_CUT nodes, bf = 2) from the front (job_ctr), the others
     // from the back (job_big_ctr).
     uint32_t job_big_ctr[2];
+    // Levels run in batches launched without waiting (bookkeeping in k_phr_level):
+    uint32_t level_done;   // levels completed
+    uint32_t blocks_done;  // blocks of the running level that have finished
+    uint32_t stall;        // a launch found cuts beyond its capacity and did nothing
+    uint32_t err_copy;     // the device error word when the last level completed
 };
 
 // ---------------------------------------------------------------------------
@@ -720,8 +726,9 @@ struct LevelArgs {
     uint32_t *pool_out;
     PhrGlobals *g;
     int parity;
-    uint32_t pool_cap, job_cap, pnode_cap, nmax;
-    uint32_t cap;  // per-block scratch capacity in cut nodes: nmax * 2^(bf-2)
+    uint32_t pool_cap, job_cap, pnode_cap;
+    uint32_t level;  // the level this launch works on (it does nothing unless it is the next one)
+    uint32_t cap;    // per-block scratch capacity in cut nodes: at least the level's largest cut * 2^(bf-2)
     unsigned char *scratch;
     size_t scratch_per_block;
     uint32_t sort_smem;  // > 0: the block sort's keys and positions live in dynamic shared memory
@@ -782,8 +789,9 @@ __device__ __forceinline__ void store_job(const LevelArgs &A, const PJob &nj, ui
 // largest cut until BranchingFactor cuts, then the branch and its children.
 // Thread 0 accumulates the build cost and the largest new cut.
 template <int BS>
-__device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, BlockShared<BS> &sh, const Scratch &S, bool screen,
-                          unsigned long long &blk_build_cost, uint32_t &blk_max_n) {
+__device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, uint32_t nmax, BlockShared<BS> &sh,
+                                          const Scratch &S, bool screen, unsigned long long &blk_build_cost,
+                                          uint32_t &blk_max_n) {
     BoxAgg *s_tmp = sh.tmp;
     BoxAgg *s_rank = sh.rank;
     double *s_cost = sh.cost;
@@ -793,7 +801,7 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, B
     int32_t &s_branch = sh.branch, &s_ncuts = sh.ncuts;
     uint32_t &s_off = sh.off;
     const int out = A.parity ^ 1;
-    if (job.n > A.nmax) {
+    if (job.n > nmax) {
         if (threadIdx.x == 0) atomicOr(A.err, GBT_DEVERR_CAPACITY);
         return;
     }
@@ -1466,6 +1474,25 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_
     } smem;
     BlockShared<BS> &sh = smem.block;
     const int in = A.parity, out = A.parity ^ 1;
+    // Run only as the next level, after no stall and no device error, and only
+    // when the level's cuts fit this launch's scratch (else flag a stall: the
+    // host relaunches the level with a larger capacity).  Every block decides
+    // the same way, so a level runs whole or not at all.
+    __shared__ uint32_t s_go, s_nmax;
+    if (threadIdx.x == 0) {
+        const volatile PhrGlobals *vg = A.g;
+        uint32_t go = vg->stall == 0 && vg->level_done == A.level && *(volatile unsigned int *)A.err == 0;
+        const uint32_t nm = vg->max_n[in];
+        if (go && ((uint64_t)nm << (A.bf > 2 ? A.bf - 2 : 0)) > A.cap) {
+            atomicOr(&A.g->stall, 1u);
+            go = 0;
+        }
+        s_go = go;
+        s_nmax = nm;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    const uint32_t nmax = s_nmax;
     const uint32_t n_lane = A.g->job_ctr[in], n_big = A.g->job_big_ctr[in];
     Scratch S = carve(A.scratch + A.scratch_per_block * blockIdx.x, A.cap);
     if (A.sort_smem) {  // every stage of the bitonic network then reads shared memory, not L2
@@ -1495,7 +1522,7 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_
             bool mine = false;
             if (valid) {
                 const uint32_t n = A.jobs_in[j].n;
-                mine = lane_cut_job(A, n) && n <= A.nmax;
+                mine = lane_cut_job(A, n) && n <= nmax;
             }
             lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
             rest = __ballot_sync(0xffffffffu, valid && !mine);
@@ -1503,7 +1530,7 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_
         while (rest) {
             const int l = __ffs(rest) - 1;
             rest &= rest - 1;
-            job_block<BS>(A, A.jobs_in[base + l], sh, S, screen, my_build_cost, my_max_n);
+            job_block<BS>(A, A.jobs_in[base + l], nmax, sh, S, screen, my_build_cost, my_max_n);
         }
     }
     // the block's totals, one atomic each (per-split atomics on these counters contend)
@@ -1515,6 +1542,23 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_
         if (threadIdx.x == 0) {
             if (my_build_cost) atomicAdd(&A.g->build_cost, my_build_cost);
             if (my_max_n) atomicMax(&A.g->max_n[out], my_max_n);
+        }
+    }
+    // The last block to finish clears this level's input counters (the output
+    // counters of the level after next) and marks the level done.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&A.g->blocks_done, 1u) == gridDim.x - 1) {
+            __threadfence();
+            A.g->job_ctr[in] = 0;
+            A.g->job_big_ctr[in] = 0;
+            A.g->pool_ctr[in] = 0;
+            A.g->max_n[in] = 0;
+            A.g->err_copy = *(volatile unsigned int *)A.err;
+            A.g->blocks_done = 0;
+            __threadfence();
+            A.g->level_done = A.level + 1;
         }
     }
 }
@@ -1611,39 +1655,44 @@ struct Arena {
 
 int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, gbt_bvh *out) {
     cudaStream_t st = ctx->stream;
-    // the level loop reads the counters and the error word back through pinned memory
+    // the level loop reads the counters back through the context's pinned buffer
     struct Readback {
         PhrGlobals g;
-        unsigned int flags;
     };
-    Readback *hb = nullptr;
-    if (cudaMallocHost(&hb, sizeof(Readback)) != cudaSuccess) {
-        cudaGetLastError();
-        return gbt_fail(ctx, GBT_ENOMEM, "phr: pinned host allocation");
-    }
+    static_assert(sizeof(Readback) <= GBT_PINNED_BYTES, "readback exceeds the pinned buffer");
+    Readback *hb = static_cast<Readback *>(gbt_pinned(ctx));
+    if (!hb) return gbt_fail(ctx, GBT_ENOMEM, "phr: pinned host allocation");
     BvhHeader h;
     GBT_CUDA(ctx, cudaMemcpyAsync(&h, aux->d_hdr, sizeof(h), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));
     const uint32_t U = h.n_unique, N = aux->n_prim;
     const uint32_t n_aux = U > 0 ? 2 * U - 1 : 1;
-    void *arena_mem = nullptr, *scratch = nullptr;
+    // the temporaries live in the context's PHR workspace (grow-only, kept unless
+    // GBT_OPT_KEEP_WORKSPACE is 0)
     auto cleanup = [&]() {
-        cudaStreamSynchronize(st);
-        if (scratch) cudaFree(scratch);
-        if (arena_mem) cudaFree(arena_mem);
-        cudaFreeHost(hb);
+        if (!ctx->keep_workspace) {
+            cudaStreamSynchronize(st);
+            gbt_phr_release(ctx);
+        }
     };
     // outputs
     out->n_prim = N;
     const size_t per_node = bf == 2 ? 4 : 8;
     const uint32_t pnode_cap = 2 * n_aux + 2;
-    if (cudaMalloc(&out->d_prims, (size_t)N * 3 * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&out->d_nodes, (size_t)pnode_cap * per_node * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&out->d_parent, (size_t)pnode_cap * sizeof(int32_t)) != cudaSuccess ||
-        cudaMalloc(&out->d_hdr, sizeof(BvhHeader)) != cudaSuccess) {
-        cudaGetLastError();
-        cudaFreeHost(hb);
-        return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
+    {  // the tree's arrays in one allocation
+        const size_t b_prims = gbt_align((size_t)N * 3 * sizeof(float4));
+        const size_t b_nodes = gbt_align((size_t)pnode_cap * per_node * sizeof(float4));
+        const size_t b_parent = gbt_align((size_t)pnode_cap * sizeof(int32_t));
+        char *blk = nullptr;
+        if (cudaMalloc(&blk, b_prims + b_nodes + b_parent + sizeof(BvhHeader)) != cudaSuccess) {
+            cudaGetLastError();
+            return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
+        }
+        out->d_block = blk;
+        out->d_prims = reinterpret_cast<float4 *>(blk);
+        out->d_nodes = reinterpret_cast<float4 *>(blk + b_prims);
+        out->d_parent = reinterpret_cast<int32_t *>(blk + b_prims + b_nodes);
+        out->d_hdr = reinterpret_cast<BvhHeader *>(blk + b_prims + b_nodes + b_parent);
     }
     out->node_cap = pnode_cap;
     AuxNode *d_aux;
@@ -1664,13 +1713,19 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         for (int i = 0; i < 2; i++) ar.take(&d_jobs[i], job_cap);
         ar.take(&d_thr, 2 * DEPTH_TABLE);  // the table, then its float32 band edges
         if (pass == 0) {
-            if (cudaMalloc(&arena_mem, ar.used) != cudaSuccess) {
-                cudaGetLastError();
-                arena_mem = nullptr;
-                cleanup();
-                return gbt_fail(ctx, GBT_ENOMEM, "phr: device allocation of " + std::to_string(ar.used) + " bytes");
+            if (ctx->phr_ws_bytes < ar.used) {
+                cudaStreamSynchronize(st);
+                cudaFree(ctx->phr_ws);
+                ctx->phr_ws = nullptr;
+                ctx->phr_ws_bytes = 0;
+                if (cudaMalloc(&ctx->phr_ws, ar.used) != cudaSuccess) {
+                    cudaGetLastError();
+                    ctx->phr_ws = nullptr;
+                    return gbt_fail(ctx, GBT_ENOMEM, "phr: device allocation of " + std::to_string(ar.used) + " bytes");
+                }
+                ctx->phr_ws_bytes = ar.used;
             }
-            ar.base = static_cast<char *>(arena_mem);
+            ar.base = static_cast<char *>(ctx->phr_ws);
         }
     }
     // DefaultThreshold table (phr.go:356-358), host float64
@@ -1705,25 +1760,29 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     uint32_t n_lane = g.job_ctr[0], n_big = g.job_big_ctr[0], nmax = g.max_n[0];
     uint32_t n_jobs = n_lane + n_big;
     const uint64_t initial_cut = g.pool_ctr[0];
-    size_t scratch_bytes = 0;
-    int parity = 0;
     // whole-block jobs sort in dynamic shared memory up to SORT_SMEM_MAX keys
     GBT_CUDA(ctx, cudaFuncSetAttribute(k_phr_level<PT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        SORT_SMEM_MAX * 12));
     GBT_CUDA(ctx, cudaFuncSetAttribute(k_phr_level<WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        SORT_SMEM_MAX * 12));
-    int levels = 0;
+    // Levels whose cuts are all small run in batches of SPEC_LEVELS launches
+    // with one readback: the next levels' sizes are read on the device, and a
+    // launch whose level turns out to have larger cuts does nothing and flags
+    // a stall, after which that level is relaunched here with wider blocks.
+    uint32_t level = 0;
+    int parity = 0;
     while (n_jobs > 0) {
         // one-warp blocks when every cut is small; WIDE-thread blocks for levels of a few
         // large cuts (the first ones), PT-thread blocks otherwise
         const int variant = nmax <= PHR_SMALL_CUT ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
+        const int batch = variant == 0 ? SPEC_LEVELS : 1;
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
         if (nmax > (1u << 28)) {
             cleanup();
             return gbt_fail(ctx, GBT_ENOMEM, "phr: cut too large");
         }
-        const uint32_t cap = nmax << (bf > 2 ? bf - 2 : 0);
+        const uint32_t cap = (variant == 0 ? (uint32_t)PHR_SMALL_CUT : nmax) << (bf > 2 ? bf - 2 : 0);
         const uint32_t sort_p = pow2_at_least(cap > 0 ? cap : 1);
         const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
         // grid: at most the blocks that are resident at once
@@ -1732,76 +1791,85 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         else if (variant == 1) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<PT>, PT, dyn));
         else GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<WIDE>, WIDE, dyn));
         const uint32_t max_grid = (uint32_t)ctx->num_sms * (uint32_t)std::max(1, per_sm);
-        // work items: one-warp blocks take a second-list job or 32 lane-list jobs
+        // work items: one-warp blocks take a second-list job or 32 lane-list jobs; the
+        // batch's later levels are not known yet and get the full grid
         const uint32_t items = variant == 0 ? n_big + (n_lane + 31) / 32 : n_jobs;
-        const uint32_t grid = std::min<uint32_t>(items, max_grid);
+        const uint32_t grid0 = std::min<uint32_t>(items, max_grid);
         const size_t per_block = gbt_align(scratch_bytes_for(cap));
-        if (per_block * grid > scratch_bytes) {
+        const uint32_t blocks = batch > 1 ? max_grid : grid0;
+        if (per_block * blocks > ctx->phr_scr_bytes) {
             // sized for every block the variant can have resident, so that later
             // levels seldom need to grow it
             const size_t need = per_block * max_grid;
-            if (scratch) {
-                cudaStreamSynchronize(st);
-                cudaFree(scratch);
-                scratch = nullptr;
-            }
-            if (cudaMalloc(&scratch, need) != cudaSuccess) {
+            cudaStreamSynchronize(st);
+            cudaFree(ctx->phr_scr);
+            ctx->phr_scr = nullptr;
+            ctx->phr_scr_bytes = 0;
+            if (cudaMalloc(&ctx->phr_scr, need) != cudaSuccess) {
                 cudaGetLastError();
-                scratch = nullptr;
+                ctx->phr_scr = nullptr;
                 cleanup();
                 return gbt_fail(ctx, GBT_ENOMEM, "phr: scratch");
             }
-            scratch_bytes = need;
+            ctx->phr_scr_bytes = need;
         }
-        const int o = parity ^ 1;
-        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, job_ctr) + o * 4, 0, 4, st));
-        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, pool_ctr) + o * 4, 0, 4, st));
-        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, max_n) + o * 4, 0, 4, st));
-        GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, job_big_ctr) + o * 4, 0, 4, st));
-        LevelArgs A;
-        A.aux = d_aux;
-        A.aux_recs = aux->d_prims;
-        A.recs = out->d_prims;
-        A.pn = d_pn;
-        A.thr = d_thr;
-        A.thr_lo = reinterpret_cast<const float *>(d_thr + DEPTH_TABLE);
-        A.thr_hi = A.thr_lo + DEPTH_TABLE;
-        A.jobs_in = d_jobs[parity];
-        A.jobs_out = d_jobs[o];
-        A.pool_in = d_pool[parity];
-        A.pool_out = d_pool[o];
-        A.g = d_g;
-        A.parity = parity;
-        A.pool_cap = pool_cap;
-        A.job_cap = job_cap;
-        A.pnode_cap = pnode_cap;
-        A.nmax = nmax;
-        A.cap = cap;
-        A.scratch = static_cast<unsigned char *>(scratch);
-        A.scratch_per_block = per_block;
-        A.sort_smem = dyn ? 1u : 0u;
-        A.bf = bf;
-        A.n_prim = N;
-        A.err = ctx->d_error;
-        if (variant == 0) k_phr_level<32><<<grid, 32, 0, st>>>(A);
-        else if (variant == 1) k_phr_level<PT><<<grid, PT, dyn, st>>>(A);
-        else k_phr_level<WIDE><<<grid, WIDE, dyn, st>>>(A);
-        GBT_CUDA(ctx, cudaGetLastError());
+        void *scratch = ctx->phr_scr;
+        for (int bi = 0; bi < batch; bi++) {
+            const uint32_t lv = level + (uint32_t)bi;
+            const int par = (int)(lv & 1u), o = par ^ 1;
+            LevelArgs A;
+            A.aux = d_aux;
+            A.aux_recs = aux->d_prims;
+            A.recs = out->d_prims;
+            A.pn = d_pn;
+            A.thr = d_thr;
+            A.thr_lo = reinterpret_cast<const float *>(d_thr + DEPTH_TABLE);
+            A.thr_hi = A.thr_lo + DEPTH_TABLE;
+            A.jobs_in = d_jobs[par];
+            A.jobs_out = d_jobs[o];
+            A.pool_in = d_pool[par];
+            A.pool_out = d_pool[o];
+            A.g = d_g;
+            A.parity = par;
+            A.pool_cap = pool_cap;
+            A.job_cap = job_cap;
+            A.pnode_cap = pnode_cap;
+            A.level = lv;
+            A.cap = cap;
+            A.scratch = static_cast<unsigned char *>(scratch);
+            A.scratch_per_block = per_block;
+            A.sort_smem = dyn ? 1u : 0u;
+            A.bf = bf;
+            A.n_prim = N;
+            A.err = ctx->d_error;
+            const uint32_t grid = bi == 0 ? grid0 : max_grid;
+            if (variant == 0) k_phr_level<32><<<grid, 32, 0, st>>>(A);
+            else if (variant == 1) k_phr_level<PT><<<grid, PT, dyn, st>>>(A);
+            else k_phr_level<WIDE><<<grid, WIDE, dyn, st>>>(A);
+            GBT_CUDA(ctx, cudaGetLastError());
+        }
         GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
-        GBT_CUDA(ctx, cudaMemcpyAsync(&hb->flags, ctx->d_error, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaStreamSynchronize(st));
-        if (hb->flags) break;  // reported by the caller's device-error check
-        n_lane = g.job_ctr[o];
-        n_big = g.job_big_ctr[o];
+        if (g.err_copy) break;  // reported by the caller's device-error check
+        if (g.level_done == level) {  // the first launch of a batch always fits: nothing moved
+            unsigned int flags = 0;
+            GBT_CUDA(ctx, cudaMemcpy(&flags, ctx->d_error, sizeof(flags), cudaMemcpyDeviceToHost));
+            if (flags) break;  // an earlier device error: reported by the caller's check
+            cleanup();
+            return gbt_fail(ctx, GBT_EDEVICE, "phr: a level made no progress");
+        }
+        level = g.level_done;
+        parity = (int)(level & 1u);
+        if (g.stall) GBT_CUDA(ctx, cudaMemsetAsync(reinterpret_cast<char *>(d_g) + offsetof(PhrGlobals, stall), 0, 4, st));
+        n_lane = g.job_ctr[parity];
+        n_big = g.job_big_ctr[parity];
         if ((uint64_t)n_lane + n_big > job_cap) {  // the two lists met
             const unsigned int flags = GBT_DEVERR_CAPACITY;
             GBT_CUDA(ctx, cudaMemcpy(ctx->d_error, &flags, sizeof(flags), cudaMemcpyHostToDevice));
             break;
         }
         n_jobs = n_lane + n_big;
-        nmax = g.max_n[o];
-        parity = o;
-        levels++;
+        nmax = g.max_n[parity];
     }
     k_phr_finalize<<<(pnode_cap + 255) / 256, 256, 0, st>>>(d_pn, d_g, out->d_nodes, bf == 2 ? 2 : 4, out->d_hdr, N,
                                                             out->d_parent,
@@ -1813,4 +1881,13 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     out->build_cost = (int64_t)(initial_cut + g.build_cost);  // BuildWithCost (phr.go:154-192)
     cleanup();
     return GBT_OK;
+}
+
+void gbt_phr_release(gbt_ctx *ctx) {
+    cudaFree(ctx->phr_ws);
+    cudaFree(ctx->phr_scr);
+    ctx->phr_ws = nullptr;
+    ctx->phr_scr = nullptr;
+    ctx->phr_ws_bytes = 0;
+    ctx->phr_scr_bytes = 0;
 }

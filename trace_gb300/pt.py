@@ -72,7 +72,7 @@ class Context:
     def sync(self):
         self.check(self.L.gbt_ctx_sync(self.h), "sync")
 
-    OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2, "primary_packets": 3}
+    OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2, "primary_packets": 3, "keep_workspace": 4}
 
     def set_option(self, name, value):
         """Execution option of later calls (gbt_ctx_set_option); results do not depend on it."""
