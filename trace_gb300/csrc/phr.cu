@@ -2,16 +2,21 @@
 //
 //   k_aux_build      unified view of the LBVH (inner nodes and leaves) with
 //                    boxes, subtree sizes (bvh.go:159-167) and primitive ranges
+//   k_phr_screen     whether every box coordinate lies in the range where the
+//                    float32 screening of phr_exact.cuh holds
 //   k_initial_cut    findInitialCut (phr.go:257-311), breadth-first in FIFO
 //                    order with the MAX_CUT_SIZE cap, one block
-//   k_phr_level      buildSubTree (phr.go:92-152), one block per cut, one
-//                    launch per tree level:
+//   k_phr_level      buildSubTree (phr.go:92-152), one launch per tree level:
 //                      SweepSAH (phr.go:368-405): three stable sorts by
 //                      barycenter, chained x -> y -> z as the Go code chains
-//                      them, each followed by minCost (phr.go:414-459), an
-//                      exact float64 sweep done as a prefix/suffix scan of
-//                      boxes and subtree sizes plus an argmin;
-//                      refined (phr.go:313-338) and makeLeaf (phr.go:340-352)
+//                      them, each followed by minCost (phr.go:414-459): a
+//                      prefix/suffix sweep of boxes and subtree sizes whose
+//                      costs are taken in float32 and decided exactly, with
+//                      float64 only where the float32 values cannot settle a
+//                      comparison (phr_exact.cuh);
+//                      refined (phr.go:313-338) and makeLeaf (phr.go:340-352).
+//                    Cuts of 2..LANE_CUT nodes (bf = 2) are swept by one lane
+//                    each, larger ones by a warp, the largest by a block.
 //   k_phr_finalize   the N-ary tree into 64-byte binary or 128-byte 4-wide nodes
 //
 // The result is the oracle's tree exactly: same splits, same tie orders, same
