@@ -48,10 +48,16 @@ constexpr uint32_t LANE_CUT = 16;
 // Longer record ranges of the lane path's leaves are copied by the whole warp.
 constexpr uint32_t LANE_COPY = 8;
 
+// An auxiliary-tree node in two parts: what every sweep reads (32 bytes, one
+// sector) and what only leaves and refinements read.
 struct AuxNode {
     float lo[3], hi[3];
-    uint32_t size, first, count;
-    int32_t c0, c1;
+    uint32_t size;  // subtree size (bvh.go:159-167)
+    int32_t c0;     // first child, -1 for a leaf
+};
+struct AuxCold {
+    uint32_t first, count;  // the subtree's primitive records
+    int32_t c1;             // second child
     uint32_t pad;
 };
 
@@ -207,7 +213,8 @@ __device__ uint32_t block_scan_u32(uint32_t v, uint32_t *s_tmp, uint32_t *total)
 // ---------------------------------------------------------------------------
 __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                             const uint32_t *__restrict__ subtree, const uint2 *__restrict__ range,
-                            const uint32_t *__restrict__ run, AuxNode *aux, uint32_t U, uint32_t n_prim) {
+                            const uint32_t *__restrict__ run, AuxNode *aux, AuxCold *auxc, uint32_t U,
+                            uint32_t n_prim) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) {  // the root's own box lives in the header
         uint32_t rid = hdr->root_cnt > 0 ? 0u : (uint32_t)hdr->root_ref;
@@ -218,9 +225,10 @@ __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__r
         }
         if (hdr->root_cnt > 0) {
             a.size = 1;
-            a.first = 0;
-            a.count = n_prim;
-            a.c0 = a.c1 = -1;
+            a.c0 = -1;
+            auxc[rid].first = 0;
+            auxc[rid].count = n_prim;
+            auxc[rid].c1 = -1;
         }
     }
     if (U < 2 || k >= U - 1) return;
@@ -238,18 +246,19 @@ __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__r
         a.lo[0] = xy.x; a.hi[0] = xy.y; a.lo[1] = xy.z; a.hi[1] = xy.w; a.lo[2] = zl; a.hi[2] = zh;
         if (cnt > 0) {
             a.size = 1;
-            a.first = (uint32_t)ref;
-            a.count = (uint32_t)cnt;
-            a.c0 = a.c1 = -1;
+            a.c0 = -1;
+            auxc[id].first = (uint32_t)ref;
+            auxc[id].count = (uint32_t)cnt;
+            auxc[id].c1 = -1;
         }
     }
     AuxNode &me = aux[k];
     me.c0 = ids[0];
-    me.c1 = ids[1];
     me.size = subtree[k];
     uint2 lr = range[k];
-    me.first = run[lr.x];
-    me.count = run[lr.y + 1] - run[lr.x];
+    auxc[k].c1 = ids[1];
+    auxc[k].first = run[lr.x];
+    auxc[k].count = run[lr.y + 1] - run[lr.x];
 }
 
 // Whether every box coordinate lies in the float32 screening range (phr_exact.cuh);
@@ -266,7 +275,8 @@ __global__ void k_phr_screen(const AuxNode *__restrict__ aux, uint32_t n_aux, Ph
 // ---------------------------------------------------------------------------
 // initial cut: FIFO breadth-first expansion with the MAX_CUT_SIZE cap
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_initial_cut(const AuxNode *__restrict__ aux, int32_t root, double thr0,
+__global__ void __launch_bounds__(1024) k_initial_cut(const AuxNode *__restrict__ aux,
+                                                      const AuxCold *__restrict__ auxc, int32_t root, double thr0,
                                                       uint32_t *front_a, uint32_t *front_b, uint32_t *cut,
                                                       PJob *job0, PhrGlobals *g, uint32_t cap) {
     __shared__ uint32_t s_tmp[32];
@@ -292,7 +302,7 @@ __global__ void __launch_bounds__(1024) k_initial_cut(const AuxNode *__restrict_
             if (term && ncut + t_ex < cap) cut[ncut + t_ex] = id;
             if (expand && nnext + 2 * e_ex + 1 < cap) {
                 next[nnext + 2 * e_ex] = (uint32_t)aux[id].c0;
-                next[nnext + 2 * e_ex + 1] = (uint32_t)aux[id].c1;
+                next[nnext + 2 * e_ex + 1] = (uint32_t)auxc[id].c1;
             }
             counter += tot_att;
             ncut += tot_term;
@@ -720,6 +730,7 @@ __device__ void copy_records(const float4 *__restrict__ src, float4 *__restrict_
 
 struct LevelArgs {
     const AuxNode *aux;
+    const AuxCold *auxc;
     const float4 *aux_recs;
     float4 *recs;
     PNode *pn;
@@ -814,19 +825,20 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
         if (threadIdx.x == 0) {
             uint32_t id = A.pool_in[job.off];
             const AuxNode &a = A.aux[id];
+            const AuxCold &ac = A.auxc[id];
             int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
             if (p >= 0) {
-                uint32_t ro = atomicAdd(&A.g->rec_ctr, a.count);
+                uint32_t ro = atomicAdd(&A.g->rec_ctr, ac.count);
                 PNode &q = A.pn[p];
                 for (int k = 0; k < 3; k++) { q.lo[k] = a.lo[k]; q.hi[k] = a.hi[k]; }
                 q.leaf = 1;
                 q.nchild = 0;
                 q.rec_off = ro;
-                q.rec_cnt = a.count;
+                q.rec_cnt = ac.count;
                 attach(A, job.parent, job.slot, p);
                 s_off = ro;
-                s_u[0] = a.first;
-                s_u[1] = a.count;
+                s_u[0] = ac.first;
+                s_u[1] = ac.count;
             }
         }
         __syncthreads();
@@ -895,12 +907,12 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
             uint32_t loc = 0;
             const uint32_t chunk = (n + blockDim.x - 1) / blockDim.x;
             const uint32_t a = min(n, threadIdx.x * chunk), b = min(n, a + chunk);
-            for (uint32_t i = a; i < b; i++) loc += A.aux[ord[i]].count;
+            for (uint32_t i = a; i < b; i++) loc += A.auxc[ord[i]].count;
             uint32_t tot;
             uint32_t ex = block_scan_u32(loc, s_u, &tot);
             for (uint32_t i = a; i < b; i++) {
                 S.flag[i] = ex;
-                ex += A.aux[ord[i]].count;
+                ex += A.auxc[ord[i]].count;
             }
             if (threadIdx.x == 0) {
                 int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
@@ -920,7 +932,7 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
             }
             __syncthreads();
             for (uint32_t i = 0; i < n; i++) {
-                const AuxNode &x = A.aux[ord[i]];
+                const AuxCold &x = A.auxc[ord[i]];
                 copy_records(A.aux_recs, A.recs, x.first, x.count, s_off + S.flag[i], A.n_prim, A.err);
             }
             __syncthreads();
@@ -958,7 +970,7 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
             const float *blo = side ? win.rlo : win.llo, *bhi = side ? win.rhi : win.lhi;
             if (tot == 1) {  // a one-node cut becomes a leaf of everything below it
                 if (threadIdx.x == 0) {
-                    const AuxNode &x = A.aux[sr[0]];
+                    const AuxCold &x = A.auxc[sr[0]];
                     int32_t p = new_pnode(A.g, A.pnode_cap, A.err);
                     s_off = atomicAdd(&A.g->rec_ctr, x.count);
                     s_u[8] = x.first;
@@ -997,7 +1009,7 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
                             ex += 1;
                         } else {
                             A.pool_out[o + ex] = (uint32_t)x.c0;
-                            A.pool_out[o + ex + 1] = (uint32_t)x.c1;
+                            A.pool_out[o + ex + 1] = (uint32_t)A.auxc[sr[i]].c1;
                             ex += 2;
                         }
                     }
@@ -1096,6 +1108,11 @@ struct LanePick {
 __device__ __forceinline__ const AuxNode &lane_node(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
                                                     uint32_t i, int ln) {
     return aux[L.id[L.ord[k][i][ln]][ln]];
+}
+
+__device__ __forceinline__ const AuxCold &lane_cold(const AuxCold *__restrict__ auxc, const LaneScratch &L, int k,
+                                                    uint32_t i, int ln) {
+    return auxc[L.id[L.ord[k][i][ln]][ln]];
 }
 
 // sort.SliceStable by barycenter component `axis`: insertion sort of the
@@ -1309,7 +1326,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
         split = win.split;
         if (split == 0) {  // makeLeaf over the winning order
             n_pn = 2;
-            for (uint32_t i = 0; i < n; i++) n_rec += lane_node(aux, L, k, i, ln).count;
+            for (uint32_t i = 0; i < n; i++) n_rec += lane_cold(A.auxc, L, k, i, ln).count;
         } else {  // refined(left), refined(right)
             const int32_t depth = job.depth;
             const int di = min(depth, DEPTH_TABLE - 1);
@@ -1334,7 +1351,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
                 }
                 if (tot[s] == 1) {  // a one-node cut becomes a leaf of everything below it
                     n_pn++;
-                    n_rec += lane_node(aux, L, k, a, ln).count;
+                    n_rec += lane_cold(A.auxc, L, k, a, ln).count;
                 } else {
                     n_pool += tot[s];
                     if (lane_cut_job(A, tot[s])) n_lane_jobs++;
@@ -1386,7 +1403,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
             q.rec_cnt = n_rec;
             A.pn[b].child[0] = p;
             for (uint32_t i = 0; i < n; i++) {
-                const AuxNode &x = lane_node(aux, L, k, i, ln);
+                const AuxCold &x = lane_cold(A.auxc, L, k, i, ln);
                 if (x.count <= LANE_COPY) lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
                 else long_copy = true;
                 rec += x.count;
@@ -1400,7 +1417,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
                 lbox_empty(box);
                 for (uint32_t i = a; i < e; i++) lbox_add(box, lane_node(aux, L, k, i, ln));
                 if (tot[s] == 1) {
-                    const AuxNode &x = lane_node(aux, L, k, a, ln);
+                    const AuxCold &x = lane_cold(A.auxc, L, k, a, ln);
                     const int32_t p = (int32_t)pn++;
                     PNode &q = A.pn[p];
                     for (int d = 0; d < 3; d++) {
@@ -1432,9 +1449,8 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
                         if (keep[s] >> (i - a) & 1u) {
                             A.pool_out[pool++] = id;
                         } else {
-                            const AuxNode &x = aux[id];
-                            A.pool_out[pool++] = (uint32_t)x.c0;
-                            A.pool_out[pool++] = (uint32_t)x.c1;
+                            A.pool_out[pool++] = (uint32_t)aux[id].c0;
+                            A.pool_out[pool++] = (uint32_t)A.auxc[id].c1;
                         }
                     }
                     if (lane_cut_job(A, tot[s])) A.jobs_out[qs++] = nj;
@@ -1458,7 +1474,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
         for (uint32_t q = 0; q < walk; q++) {
             if (sp != 0 && (q ? t1 : t0) != 1) continue;  // that side is a cut, not a leaf
             const uint32_t pos = sp == 0 ? q : (q ? sp : 0);
-            const AuxNode &x = aux[L.id[L.ord[kl][pos][l]][l]];
+            const AuxCold &x = A.auxc[L.id[L.ord[kl][pos][l]][l]];
             if (x.count > LANE_COPY) copy_records(A.aux_recs, A.recs, x.first, x.count, r, A.n_prim, A.err);
             r += x.count;
         }
@@ -1701,6 +1717,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     }
     out->node_cap = pnode_cap;
     AuxNode *d_aux;
+    AuxCold *d_auxc;
     PNode *d_pn;
     PhrGlobals *d_g;
     uint32_t *d_front[2], *d_pool[2];
@@ -1711,6 +1728,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     for (int pass = 0; pass < 2; pass++) {  // sizes, then pointers
         ar.used = 0;
         ar.take(&d_aux, n_aux);
+        ar.take(&d_auxc, n_aux);
         ar.take(&d_pn, pnode_cap);
         ar.take(&d_g, 1);
         for (int i = 0; i < 2; i++) ar.take(&d_front[i], 2 * (size_t)n_aux + 2);
@@ -1753,11 +1771,12 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, offsetof(PhrGlobals, root), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_pn, 0, (size_t)pnode_cap * sizeof(PNode), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_aux, 0, (size_t)n_aux * sizeof(AuxNode), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(d_auxc, 0, (size_t)n_aux * sizeof(AuxCold), st));
     k_aux_build<<<(U + 255) / 256 + 1, 256, 0, st>>>(aux->d_hdr, aux->d_nodes, aux->d_size, aux->d_range, aux->d_run,
-                                                     d_aux, U, N);
+                                                     d_aux, d_auxc, U, N);
     k_phr_screen<<<ctx->num_sms * 4, 256, 0, st>>>(d_aux, n_aux, d_g);
     const int32_t root = h.root_cnt > 0 ? 0 : h.root_ref;
-    k_initial_cut<<<1, 1024, 0, st>>>(d_aux, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
+    k_initial_cut<<<1, 1024, 0, st>>>(d_aux, d_auxc, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
     GBT_CUDA(ctx, cudaGetLastError());
     GBT_CUDA(ctx, cudaMemcpyAsync(&hb->g, d_g, sizeof(PhrGlobals), cudaMemcpyDeviceToHost, st));
     GBT_CUDA(ctx, cudaStreamSynchronize(st));  // also: the threshold table's pageable source is consumed
@@ -1824,6 +1843,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
             const int par = (int)(lv & 1u), o = par ^ 1;
             LevelArgs A;
             A.aux = d_aux;
+            A.auxc = d_auxc;
             A.aux_recs = aux->d_prims;
             A.recs = out->d_prims;
             A.pn = d_pn;
