@@ -109,7 +109,7 @@ __device__ __forceinline__ int trace_path(const BvhHeader &hdr, const float4 *no
 }
 
 template <int W>
-__global__ void __launch_bounds__(128) k_adj_forward(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+__global__ void __launch_bounds__(128, 8) k_adj_forward(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                      const float4 *__restrict__ recs, const float *__restrict__ normals,
                                                      CamF cam, ShadeParams sp, const float *__restrict__ albedo,
                                                      const float *__restrict__ emission, double *__restrict__ part,
@@ -180,7 +180,7 @@ __device__ __forceinline__ float4 group_sum(uint32_t peers, float4 v) {
 }
 
 template <int W>
-__global__ void __launch_bounds__(128) k_adj_backward(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+__global__ void __launch_bounds__(128, 8) k_adj_backward(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                       const float4 *__restrict__ recs, const float *__restrict__ normals,
                                                       CamF cam, ShadeParams sp, const float *__restrict__ albedo,
                                                       const float *__restrict__ emission, const float *__restrict__ dimg,
