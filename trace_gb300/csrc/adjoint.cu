@@ -39,9 +39,11 @@ constexpr int MAXV = 16;  // path vertices kept for replay (max_depth <= 14)
 constexpr int SH = 12;  // traversal stack entries per thread kept in shared memory (4-wide trees)
 using Stack4 = SharedTopStack<96, SH>;
 
+// any: only hit or miss is needed (the query past MaxDepth, render.go:210-212);
+// on 4-wide trees it stops at the first hit found, with the same hit-or-miss answer.
 template <int W>
 __device__ __forceinline__ Hit closest(const BvhHeader &hdr, const float4 *nodes, const float4 *recs, float3 o,
-                                       float3 d, float tmin, unsigned int *err, Stack4 &st) {
+                                       float3 d, float tmin, bool any, unsigned int *err, Stack4 &st) {
     Ray r;
     r.o = o;
     r.d = d;
@@ -49,6 +51,7 @@ __device__ __forceinline__ Hit closest(const BvhHeader &hdr, const float4 *nodes
     r.tmax = __int_as_float(0x7f800000);
     finish_ray(r);
     if constexpr (W == 2) return closest_hit2<64>(hdr, nodes, recs, r, err);
+    else if (any) return closest_hit4_with<false, Stack4, true>(hdr, nodes, recs, r, err, nullptr, st);
     else return closest_hit4_with<false>(hdr, nodes, recs, r, err, nullptr, st);
 }
 
@@ -60,6 +63,16 @@ __device__ __forceinline__ Hit closest(const BvhHeader &hdr, const float4 *nodes
     st.se = s_se_ + threadIdx.x;               \
     st.st = s_st_ + threadIdx.x;               \
     st.stride = 128
+
+// The pixel of thread slot i: the 32 slots of a warp take an 8x4 pixel tile
+// (path_id's map over one frame), so that a warp's camera rays are coherent;
+// slots past the image stay past it.
+__device__ __forceinline__ uint32_t adj_pixel(const ShadeParams &sp, uint32_t i) {
+    if (i >= sp.npix) return i;
+    ShadeParams t = sp;
+    t.tiles = 1u;
+    return path_id(t, i);
+}
 
 struct Vertex {
     int tri;
@@ -83,7 +96,7 @@ __device__ __forceinline__ int trace_path(const BvhHeader &hdr, const float4 *no
     miss = f3(0.f, 0.f, 0.f);
     int nv = 0;
     for (int level = 0;; level++) {
-        Hit h = closest<W>(hdr, nodes, recs, o, d, tmin, err, st);
+        Hit h = closest<W>(hdr, nodes, recs, o, d, tmin, level > sp.max_depth, err, st);
         if (h.rec < 0) {
             miss = miss_colour(sp, d);
             L = add3(L, emul3(T, miss));
@@ -114,7 +127,7 @@ __global__ void __launch_bounds__(128, 8) k_adj_forward(const BvhHeader *__restr
                                                      CamF cam, ShadeParams sp, const float *__restrict__ albedo,
                                                      const float *__restrict__ emission, double *__restrict__ part,
                                                      unsigned int *err, unsigned long long *rays) {
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t pix = adj_pixel(sp, blockIdx.x * blockDim.x + threadIdx.x);
     const uint32_t c = blockIdx.y, nc = gridDim.y;  // this thread's chunk of the pixel's samples
     const uint32_t s_lo = (uint32_t)((uint64_t)sp.spp * c / nc), s_hi = (uint32_t)((uint64_t)sp.spp * (c + 1) / nc);
     const BvhHeader H = *hdr;
@@ -186,7 +199,7 @@ __global__ void __launch_bounds__(128, 8) k_adj_backward(const BvhHeader *__rest
                                                       const float *__restrict__ emission, const float *__restrict__ dimg,
                                                       float *__restrict__ g_albedo, float *__restrict__ g_emission,
                                                       unsigned int *err) {
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t pix = adj_pixel(sp, blockIdx.x * blockDim.x + threadIdx.x);
     const bool live = pix < sp.npix;
     const BvhHeader H = *hdr;
     ADJ_STACK(st);

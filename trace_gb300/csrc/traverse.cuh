@@ -341,7 +341,8 @@ __device__ __forceinline__ int2 step4(const float4 *__restrict__ nodes, int2 nod
 }
 
 // One ray through a 4-wide tree: the sorting-network step with the given stack.
-template <bool COUNT, class StackT>
+// ANY: stop at the first hit found (a query that only needs hit or miss).
+template <bool COUNT, class StackT, bool ANY = false>
 __device__ __forceinline__ Hit closest_hit4_with(const BvhHeader &hdr, const float4 *__restrict__ nodes,
                                                  const float4 *__restrict__ recs, const Ray &r, unsigned int *err,
                                                  Work *work, StackT &st) {
@@ -361,6 +362,7 @@ __device__ __forceinline__ Hit closest_hit4_with(const BvhHeader &hdr, const flo
         } else if (node.y > 0) {
             if (COUNT) work->prims += (uint32_t)node.y;
             leaf(recs, node.x, node.y, r, h);
+            if (ANY && h.rec >= 0) break;
             node = st.pop(sp, h.t);
         } else {
             break;
