@@ -1486,13 +1486,25 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
 // of the second list, swept by the whole warp, or 32 jobs of the lane list,
 // one per lane; a job of the lane list whose cut does not qualify (the root
 // job) is swept by the whole warp after them.
+// Shared memory of a level block: with the lane path, its scratch and the
+// whole-block state take turns, so they share the space.
+template <int BS, bool LANES>
+struct LevelSmem {
+    BlockShared<BS> block;
+};
 template <int BS>
-__global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
-    // the lane path (one-warp blocks) and whole-block jobs take turns, so they share the space
-    __shared__ union Shared {
+struct LevelSmem<BS, true> {
+    union {
         BlockShared<BS> block;
         LaneScratch lane;
-    } smem;
+    };
+};
+
+// LANES: one-warp blocks with the lane path (bf = 2); without it (bf > 2) a
+// one-warp block holds less state and more of them are resident.
+template <int BS, bool LANES = (BS == 32)>
+__global__ void __launch_bounds__(BS, BS == 32 ? (LANES ? 20 : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
+    __shared__ LevelSmem<BS, LANES> smem;
     BlockShared<BS> &sh = smem.block;
     const int in = A.parity, out = A.parity ^ 1;
     // Run only as the next level, after no stall and no device error, and only
@@ -1528,25 +1540,27 @@ __global__ void __launch_bounds__(BS, BS == 32 ? 20 : (BS == PT ? 2 : 1)) k_phr_
     // Work items: one-warp blocks take a second-list job or 32 lane-list jobs (the
     // lanes' own ones first, then any that do not qualify, by the whole warp); wider
     // blocks take one job of either list.  job_block has a single call site.
-    const uint32_t items = BS == 32 ? n_big + (n_lane + 31) / 32 : n_lane + n_big;
+    const uint32_t items = LANES ? n_big + (n_lane + 31) / 32 : n_lane + n_big;
     for (uint32_t it = blockIdx.x; it < items; it += gridDim.x) {
         uint32_t base = 0;   // the group's first lane-list job
         unsigned rest = 1u;  // bit l: job base + l still to be done by the whole block
-        if (BS != 32) {
+        if constexpr (!LANES) {
             base = it < n_lane ? it : A.job_cap - 1 - (it - n_lane);
-        } else if (it < n_big) {
-            base = A.job_cap - 1 - it;
         } else {
-            base = (it - n_big) * 32;
-            const uint32_t j = base + threadIdx.x;
-            const bool valid = j < n_lane;
-            bool mine = false;
-            if (valid) {
-                const uint32_t n = A.jobs_in[j].n;
-                mine = lane_cut_job(A, n) && n <= nmax;
+            if (it < n_big) {
+                base = A.job_cap - 1 - it;
+            } else {
+                base = (it - n_big) * 32;
+                const uint32_t j = base + threadIdx.x;
+                const bool valid = j < n_lane;
+                bool mine = false;
+                if (valid) {
+                    const uint32_t n = A.jobs_in[j].n;
+                    mine = lane_cut_job(A, n) && n <= nmax;
+                }
+                lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
+                rest = __ballot_sync(0xffffffffu, valid && !mine);
             }
-            lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
-            rest = __ballot_sync(0xffffffffu, valid && !mine);
         }
         while (rest) {
             const int l = __ffs(rest) - 1;
@@ -1811,13 +1825,14 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
         // grid: at most the blocks that are resident at once
         int per_sm = 0;
-        if (variant == 0) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32>, 32, 0));
+        if (variant == 0 && bf == 2) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, true>, 32, 0));
+        else if (variant == 0) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, false>, 32, 0));
         else if (variant == 1) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<PT>, PT, dyn));
         else GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<WIDE>, WIDE, dyn));
         const uint32_t max_grid = (uint32_t)ctx->num_sms * (uint32_t)std::max(1, per_sm);
-        // work items: one-warp blocks take a second-list job or 32 lane-list jobs; the
-        // batch's later levels are not known yet and get the full grid
-        const uint32_t items = variant == 0 ? n_big + (n_lane + 31) / 32 : n_jobs;
+        // work items: one-warp blocks with lanes (bf = 2) take a second-list job or 32
+        // lane-list jobs; the batch's later levels are not known yet and get the full grid
+        const uint32_t items = variant == 0 && bf == 2 ? n_big + (n_lane + 31) / 32 : n_jobs;
         const uint32_t grid0 = std::min<uint32_t>(items, max_grid);
         const size_t per_block = gbt_align(scratch_bytes_for(cap));
         const uint32_t blocks = batch > 1 ? max_grid : grid0;
@@ -1868,7 +1883,8 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
             A.n_prim = N;
             A.err = ctx->d_error;
             const uint32_t grid = bi == 0 ? grid0 : max_grid;
-            if (variant == 0) k_phr_level<32><<<grid, 32, 0, st>>>(A);
+            if (variant == 0 && bf == 2) k_phr_level<32, true><<<grid, 32, 0, st>>>(A);
+            else if (variant == 0) k_phr_level<32, false><<<grid, 32, 0, st>>>(A);
             else if (variant == 1) k_phr_level<PT><<<grid, PT, dyn, st>>>(A);
             else k_phr_level<WIDE><<<grid, WIDE, dyn, st>>>(A);
             GBT_CUDA(ctx, cudaGetLastError());
