@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(1024) k_initial_cut(const AuxNode *__restrict_
 }
 
 // ---------------------------------------------------------------------------
-// one tree level: one block per cut
+// one tree level: per-block scratch of the whole-block and warp sweeps
 // ---------------------------------------------------------------------------
 struct Scratch {
     uint32_t *ids, *ord[3];
