@@ -121,6 +121,10 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
  *                          workspace (about 600 bytes per auxiliary-tree
  *                          triangle) on the context for the next one; 0 frees
  *                          it now and after every refinement
+ *   GBT_OPT_PHR_SMALL_CUT  1..256 (default 256): PHR levels whose cuts are all
+ *                          at most this many nodes run with one-warp blocks in
+ *                          batches of launches; a launch that meets a larger
+ *                          cut is repeated with wider blocks
  * The environment variables GBT_TRAVERSAL (persistent|simple|ww),
  * GBT_ANYHIT_LAST, GBT_PRIMARY_TILES (0|1) and GBT_PRIMARY_PACKETS (0|1|2) set
  * the initial values.
@@ -130,6 +134,7 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
 #define GBT_OPT_PRIMARY_TILES 2
 #define GBT_OPT_PRIMARY_PACKETS 3
 #define GBT_OPT_KEEP_WORKSPACE 4
+#define GBT_OPT_PHR_SMALL_CUT 5
 int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */

@@ -36,6 +36,23 @@ def test_phr_matches_oracle_tree(ctx, name, make, alpha, delta, bf):
     assert g.Cost() == oc  # the device evaluates the recursion's float64 operations in its order
 
 
+@pytest.mark.parametrize("small_cut", [4, 16, 64])
+def test_phr_level_batches_and_relaunches_give_the_same_tree(ctx, small_cut):
+    """With a low threshold for one-warp levels, batched launches meet levels
+    with larger cuts, flag a stall and are relaunched with wider blocks; the
+    tree stays the oracle's (branching 2 and 4)."""
+    verts = scenes.soup(50_000, seed=5)["verts"]
+    aux = pt.DefaultLBVH(pt.DeviceScene(ctx, verts))
+    try:
+        ctx.set_option("phr_small_cut", small_cut)
+        for bf in (2, 4):
+            g = pt.NewPHRBuilder(0.5, 6.0, bf).BuildFromAuxilary(aux)
+            ge, oe = g.export(), O.lbvh(verts).phr(0.5, 6.0, bf).export()
+            assert canonical_equal(ge, oe), first_mismatch(ge, oe)
+    finally:
+        ctx.set_option("phr_small_cut", 256)
+
+
 def test_phr_workspace_kept_or_released_gives_the_same_tree(ctx):
     """Refinements that reuse the context's workspace (default), grow it, and
     free it after every build (GBT_OPT_KEEP_WORKSPACE 0) give the same tree."""

@@ -176,6 +176,10 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
         if (value < 0 || value > 2) return gbt_fail(ctx, GBT_EINVAL, "set_option: packets must be 0, 1 or 2");
         ctx->primary_packets = value;
         return GBT_OK;
+    case GBT_OPT_PHR_SMALL_CUT:
+        if (value < 1 || value > GBT_PHR_SMALL_CUT) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 1..256");
+        ctx->phr_small_cut = value;
+        return GBT_OK;
     case GBT_OPT_KEEP_WORKSPACE:
         if (value < 0 || value > 1) return gbt_fail(ctx, GBT_EINVAL, "set_option: value must be 0 or 1");
         ctx->keep_workspace = value;

@@ -20,6 +20,8 @@
 // bounds one wait at roughly a quarter of a second.
 #define GBT_SPIN_LIMIT (1u << 22)
 
+#define GBT_PHR_SMALL_CUT 256
+
 struct gbt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -66,6 +68,8 @@ struct gbt_ctx {
     void *phr_scr = nullptr;
     size_t phr_scr_bytes = 0;
     int keep_workspace = 1;
+    // largest cut of a PHR level run with one-warp blocks (GBT_OPT_PHR_SMALL_CUT, 1..GBT_PHR_SMALL_CUT)
+    int phr_small_cut = GBT_PHR_SMALL_CUT;
     void *h_pin = nullptr;  // small pinned host buffer for counter readbacks (gbt_pinned)
 };
 

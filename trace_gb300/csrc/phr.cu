@@ -37,9 +37,6 @@ constexpr int PT = 256;                  // threads per job block
 constexpr int WIDE = 512;                // threads per job block on levels of a few large cuts
 constexpr uint32_t SORT_SMEM_MAX = 8192; // largest padded cut sorted in shared memory (96 KB)
 constexpr int SPEC_LEVELS = 8;           // small-cut levels launched per readback
-#ifndef PHR_SMALL_CUT
-#define PHR_SMALL_CUT 256                // largest cut of a level run with one-warp blocks
-#endif
 constexpr int DEPTH_TABLE = 4096;
 // Cuts of at most this many nodes are swept by a single lane (bf = 2): most
 // cuts are that small (on a 1M-triangle soup 93% of the splits sort 2-16
@@ -1812,7 +1809,8 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     while (n_jobs > 0) {
         // one-warp blocks when every cut is small; WIDE-thread blocks for levels of a few
         // large cuts (the first ones), PT-thread blocks otherwise
-        const int variant = nmax <= PHR_SMALL_CUT ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
+        const uint32_t small_cut = (uint32_t)ctx->phr_small_cut;
+        const int variant = nmax <= small_cut ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
         const int batch = variant == 0 ? SPEC_LEVELS : 1;
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
@@ -1820,7 +1818,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
             cleanup();
             return gbt_fail(ctx, GBT_ENOMEM, "phr: cut too large");
         }
-        const uint32_t cap = (variant == 0 ? (uint32_t)PHR_SMALL_CUT : nmax) << (bf > 2 ? bf - 2 : 0);
+        const uint32_t cap = (variant == 0 ? small_cut : nmax) << (bf > 2 ? bf - 2 : 0);
         const uint32_t sort_p = pow2_at_least(cap > 0 ? cap : 1);
         const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
         // grid: at most the blocks that are resident at once

@@ -72,7 +72,8 @@ class Context:
     def sync(self):
         self.check(self.L.gbt_ctx_sync(self.h), "sync")
 
-    OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2, "primary_packets": 3, "keep_workspace": 4}
+    OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2, "primary_packets": 3, "keep_workspace": 4,
+               "phr_small_cut": 5}
 
     def set_option(self, name, value):
         """Execution option of later calls (gbt_ctx_set_option); results do not depend on it."""
