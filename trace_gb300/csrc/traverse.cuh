@@ -84,7 +84,7 @@ __device__ __forceinline__ void test_record(const float4 *__restrict__ recs, int
         float3 pv = cross3(r.d, e2);
         float det = dot3(e1, pv);
         if (fabsf(det) <= 1e-7f) return;
-        float inv = 1.0f / det;
+        float inv = __frcp_rn(det);  // the correctly rounded 1 / det
         float3 tv = sub3(r.o, v0);
         float u = dot3(tv, pv) * inv;
         if (u < 0.f || u > 1.f) return;
