@@ -42,6 +42,8 @@ constexpr int DEPTH_TABLE = 4096;
 // cuts are that small (on a 1M-triangle soup 93% of the splits sort 2-16
 // nodes), and a warp then works on 32 of them at once.
 constexpr uint32_t LANE_CUT = 16;
+// Largest branching factor the lane path serves (its per-lane cut table).
+constexpr int MAX_BF_LANES = 4;
 // Longer record ranges of the lane path's leaves are copied by the whole warp.
 constexpr uint32_t LANE_COPY = 8;
 
@@ -778,9 +780,10 @@ struct BlockShared {
     uint32_t off;
 };
 
-// Whether a job goes to the lane list: bf = 2 and a cut of 2..LANE_CUT nodes.
+// Whether a job goes to the lane list: a cut of 2..LANE_CUT >> (bf - 2) nodes
+// (every cut its splits sort then fits a lane's scratch).
 __device__ __forceinline__ bool lane_cut_job(const LevelArgs &A, uint32_t n) {
-    return A.bf == 2 && n >= 2 && n <= LANE_CUT;
+    return n >= 2 && A.bf <= MAX_BF_LANES && n <= (LANE_CUT >> (A.bf - 2));
 }
 
 // Index in jobs_out for one new job of the given list (0xffffffff: no room).
@@ -1284,6 +1287,77 @@ __device__ void lane_copy_records(const float4 *__restrict__ src, float4 *__rest
 // One job per lane for the lanes with `mine`; every lane of the warp calls
 // this (the allocations are warp-wide).  Each lane accumulates its build cost
 // and largest new cut.
+// SweepSAH (phr.go:368-405) of the lane's cut in L.id: x from the cut order,
+// y from the x order, z from the y order when x is cheaper than y, else from
+// the x order; the winning order and split (0: not splitting).
+__device__ __forceinline__ LanePick lane_sweep_sah(const AuxNode *__restrict__ aux, LaneScratch &L, const LaneCut &c,
+                                                   bool screen, int ln) {
+    const uint32_t n = c.n;
+    lane_sort(aux, L, -1, 0, 0, n, ln);
+    LanePick xs = lane_min_cost(aux, L, 0, c, screen, ln);
+    lane_sort(aux, L, 0, 1, 1, n, ln);
+    LanePick ys = lane_min_cost(aux, L, 1, c, screen, ln);
+    const bool x_first = lane_less(xs, ys, aux, L, c, screen, ln);
+    lane_sort(aux, L, x_first ? 1 : 0, 2, 2, n, ln);
+    LanePick zs = lane_min_cost(aux, L, 2, c, screen, ln);
+    LanePick other = x_first ? xs : ys;
+    return lane_less(other, zs, aux, L, c, screen, ln) ? other : zs;
+}
+
+// refined (phr.go:313-338) of both sides of a split of order k: per side the
+// nodes kept (bit per position) and the refined size (a node replaced by its
+// two children counts 2), against the threshold of the cut's depth.
+__device__ __forceinline__ void lane_refine(const LevelArgs &A, const LaneScratch &L, int k, uint32_t split,
+                                            uint32_t n, int32_t depth, bool screen, int ln, uint32_t (&tot)[2],
+                                            uint32_t (&keep)[2]) {
+    const int di = min(depth, DEPTH_TABLE - 1);
+    if (depth >= DEPTH_TABLE - 1) atomicOr(A.err, GBT_DEVERR_CAPACITY);
+    const double thr = A.thr[di];
+    const float thr_lo = A.thr_lo[di], thr_hi = A.thr_hi[di];
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        const uint32_t a = s ? split : 0, e = s ? n : split;
+        for (uint32_t i = a; i < e; i++) {
+            const AuxNode &x = lane_node(A.aux, L, k, i, ln);
+            bool kept = x.c0 < 0;
+            if (!kept) {
+                const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
+                if (screen && s32 < thr_lo) kept = true;
+                else if (screen && s32 > thr_hi) kept = false;
+                else kept = surface_below(x.lo, x.hi, thr);
+            }
+            if (kept) keep[s] |= 1u << (i - a);
+            tot[s] += kept ? 1u : 2u;
+        }
+    }
+}
+
+// The long record ranges of the lanes' leaves (split 0: every node of order k
+// in one leaf; else the sides that became leaves), lane by lane, copied by
+// the whole warp in the order the lane allocated them from rec_start.
+__device__ __forceinline__ void lane_long_copies(const LevelArgs &A, const LaneScratch &L, bool long_copy,
+                                                 uint32_t rec_start, uint32_t split, uint32_t n, int k, uint32_t tot0,
+                                                 uint32_t tot1) {
+    unsigned pending = __ballot_sync(0xffffffffu, long_copy);
+    while (pending) {
+        const int l = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t r0 = __shfl_sync(0xffffffffu, rec_start, l), sp = __shfl_sync(0xffffffffu, split, l);
+        const uint32_t nl = __shfl_sync(0xffffffffu, n, l);
+        const int kl = __shfl_sync(0xffffffffu, k, l);
+        const uint32_t t0 = __shfl_sync(0xffffffffu, tot0, l), t1 = __shfl_sync(0xffffffffu, tot1, l);
+        uint32_t r = r0;
+        const uint32_t walk = sp == 0 ? nl : 2;
+        for (uint32_t q = 0; q < walk; q++) {
+            if (sp != 0 && (q ? t1 : t0) != 1) continue;  // that side is a cut, not a leaf
+            const uint32_t pos = sp == 0 ? q : (q ? sp : 0);
+            const AuxCold &x = A.auxc[L.id[L.ord[kl][pos][l]][l]];
+            if (x.count > LANE_COPY) copy_records(A.aux_recs, A.recs, x.first, x.count, r, A.n_prim, A.err);
+            r += x.count;
+        }
+    }
+}
+
 __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch &L, bool screen,
                           unsigned long long &my_build_cost, uint32_t &my_max_n) {
     const int ln = threadIdx.x & 31;
@@ -1308,16 +1382,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
             c.hi[a] = job.hi[a];
         }
         c.ns32 = __fmul_rn(gbt_phr::surface32(c.lo, c.hi), gbt_phr::count_f32(c.total));
-        lane_sort(aux, L, -1, 0, 0, n, ln);
-        LanePick xs = lane_min_cost(aux, L, 0, c, screen, ln);
-        lane_sort(aux, L, 0, 1, 1, n, ln);
-        LanePick ys = lane_min_cost(aux, L, 1, c, screen, ln);
-        // z from the y order when x is cheaper than y, else from the x order
-        const bool x_first = lane_less(xs, ys, aux, L, c, screen, ln);
-        lane_sort(aux, L, x_first ? 1 : 0, 2, 2, n, ln);
-        LanePick zs = lane_min_cost(aux, L, 2, c, screen, ln);
-        LanePick other = x_first ? xs : ys;
-        const LanePick win = lane_less(other, zs, aux, L, c, screen, ln) ? other : zs;
+        const LanePick win = lane_sweep_sah(aux, L, c, screen, ln);
         my_build_cost += n;
         k = win.k;
         split = win.split;
@@ -1325,27 +1390,11 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
             n_pn = 2;
             for (uint32_t i = 0; i < n; i++) n_rec += lane_cold(A.auxc, L, k, i, ln).count;
         } else {  // refined(left), refined(right)
-            const int32_t depth = job.depth;
-            const int di = min(depth, DEPTH_TABLE - 1);
-            if (depth >= DEPTH_TABLE - 1) atomicOr(A.err, GBT_DEVERR_CAPACITY);
-            const double thr = A.thr[di];
-            const float thr_lo = A.thr_lo[di], thr_hi = A.thr_hi[di];
+            lane_refine(A, L, k, split, n, job.depth, screen, ln, tot, keep);
             n_pn = 1;
 #pragma unroll
             for (int s = 0; s < 2; s++) {
-                const uint32_t a = s ? split : 0, e = s ? n : split;
-                for (uint32_t i = a; i < e; i++) {
-                    const AuxNode &x = lane_node(aux, L, k, i, ln);
-                    bool kept = x.c0 < 0;
-                    if (!kept) {
-                        const float s32 = screen ? gbt_phr::surface32(x.lo, x.hi) : 0.f;
-                        if (screen && s32 < thr_lo) kept = true;
-                        else if (screen && s32 > thr_hi) kept = false;
-                        else kept = surface_below(x.lo, x.hi, thr);
-                    }
-                    if (kept) keep[s] |= 1u << (i - a);
-                    tot[s] += kept ? 1u : 2u;
-                }
+                const uint32_t a = s ? split : 0;
                 if (tot[s] == 1) {  // a one-node cut becomes a leaf of everything below it
                     n_pn++;
                     n_rec += lane_cold(A.auxc, L, k, a, ln).count;
@@ -1457,24 +1506,228 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
             }
         }
     }
-    // the long record ranges, lane by lane, copied by the whole warp in the same walk order
-    unsigned pending = __ballot_sync(0xffffffffu, long_copy);
-    while (pending) {
-        const int l = __ffs(pending) - 1;
-        pending &= pending - 1;
-        const uint32_t r0 = __shfl_sync(0xffffffffu, rec_start, l), sp = __shfl_sync(0xffffffffu, split, l);
-        const uint32_t nl = __shfl_sync(0xffffffffu, n, l);
-        const int kl = __shfl_sync(0xffffffffu, k, l);
-        const uint32_t t0 = __shfl_sync(0xffffffffu, tot[0], l), t1 = __shfl_sync(0xffffffffu, tot[1], l);
-        uint32_t r = r0;
-        const uint32_t walk = sp == 0 ? nl : 2;
-        for (uint32_t q = 0; q < walk; q++) {
-            if (sp != 0 && (q ? t1 : t0) != 1) continue;  // that side is a cut, not a leaf
-            const uint32_t pos = sp == 0 ? q : (q ? sp : 0);
-            const AuxCold &x = A.auxc[L.id[L.ord[kl][pos][l]][l]];
-            if (x.count > LANE_COPY) copy_records(A.aux_recs, A.recs, x.first, x.count, r, A.n_prim, A.err);
-            r += x.count;
+    lane_long_copies(A, L, long_copy, rec_start, split, n, k, tot[0], tot[1]);
+}
+
+// The lane path for bf > 2: a job is up to bf - 1 splits (buildSubTree's
+// loop, phr.go:92-152: split the largest cut, the first of equal ones, until
+// bf cuts).  The lanes of a warp take their jobs' splits in rounds, with one
+// allocation per round; a cut a split makes goes to the output pool at once
+// (as in job_block), and the lane's next round reads it back from there.  A
+// job qualifies when its cut has at most LANE_CUT >> (bf - 2) nodes, so that
+// every cut it sorts fits the lane scratch (a refinement at most doubles one).
+struct LaneCuts {  // per lane, index-major
+    uint32_t off[MAX_BF_LANES][32];    // pool offset; bit 31: in the output pool
+    uint32_t n[MAX_BF_LANES][32];      // nodes; 1 for a leaf
+    float box[6][MAX_BF_LANES][32];    // lo.xyz, hi.xyz
+    int32_t depth[MAX_BF_LANES][32];
+    int32_t leaf[MAX_BF_LANES][32];    // >= 0: the leaf's PNode; -1: a cut
+};
+
+__device__ void lane_jobs_multi(const LevelArgs &A, uint32_t j, bool mine, LaneScratch &L, LaneCuts &C, bool screen,
+                                unsigned long long &my_build_cost, uint32_t &my_max_n) {
+    const int ln = threadIdx.x & 31;
+    const AuxNode *__restrict__ aux = A.aux;
+    const int out = A.parity ^ 1;
+    int ncuts = 0;
+    int32_t branch = -1;
+    bool ok = mine;
+    if (mine) {
+        const PJob &job = A.jobs_in[j];
+        C.off[0][ln] = job.off;
+        C.n[0][ln] = job.n;
+        for (int a = 0; a < 3; a++) {
+            C.box[a][0][ln] = job.lo[a];
+            C.box[3 + a][0][ln] = job.hi[a];
         }
+        C.depth[0][ln] = job.depth;
+        C.leaf[0][ln] = -1;
+        ncuts = 1;
+    }
+    for (int round = 0; round < A.bf - 1; round++) {  // the same count for every lane
+        int mi = 0;
+        uint32_t n = 0;
+        if (ok)
+            for (int i = 0; i < ncuts; i++) {
+                const uint32_t ni = C.n[i][ln];
+                if (ni > n) {
+                    n = ni;
+                    mi = i;
+                }
+            }
+        if (ok && n > LANE_CUT) {  // cannot happen for a qualifying job; the scratch holds LANE_CUT
+            atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            ok = false;
+        }
+        const bool act = ok && n > 1;
+        uint32_t n_pn = (round == 0 && ok) ? 1u : 0u;  // the branch comes with the first round
+        uint32_t n_rec = 0, n_pool = 0, split = 0, tot[2] = {0, 0}, keep[2] = {0, 0};
+        int k = 0;
+        if (act) {
+            const uint32_t off = C.off[mi][ln];
+            const uint32_t *src = (off >> 31) ? A.pool_out : A.pool_in;
+            LaneCut c;
+            c.n = n;
+            c.total = 0;
+            for (uint32_t i = 0; i < n; i++) {
+                const uint32_t id = src[(off & 0x7fffffffu) + i];
+                L.id[i][ln] = id;
+                c.total += aux[id].size;
+            }
+            for (int a = 0; a < 3; a++) {
+                c.lo[a] = C.box[a][mi][ln];
+                c.hi[a] = C.box[3 + a][mi][ln];
+            }
+            c.ns32 = __fmul_rn(gbt_phr::surface32(c.lo, c.hi), gbt_phr::count_f32(c.total));
+            const LanePick win = lane_sweep_sah(aux, L, c, screen, ln);
+            my_build_cost += n;
+            k = win.k;
+            split = win.split;
+            if (split == 0) {  // makeLeaf over the winning order
+                n_pn += 1;
+                for (uint32_t i = 0; i < n; i++) n_rec += lane_cold(A.auxc, L, k, i, ln).count;
+            } else {
+                lane_refine(A, L, k, split, n, C.depth[mi][ln], screen, ln, tot, keep);
+#pragma unroll
+                for (int s = 0; s < 2; s++) {
+                    if (tot[s] == 1) {
+                        n_pn++;
+                        n_rec += lane_cold(A.auxc, L, k, s ? split : 0, ln).count;
+                    } else {
+                        n_pool += tot[s];
+                    }
+                }
+            }
+        }
+        uint32_t pn = warp_alloc(&A.g->pnode_ctr, n_pn, ln);
+        uint32_t rec = warp_alloc(&A.g->rec_ctr, n_rec, ln);
+        uint32_t pool = warp_alloc(&A.g->pool_ctr[out], n_pool, ln);
+        if (ok && ((uint64_t)pn + n_pn > A.pnode_cap || (uint64_t)pool + n_pool > A.pool_cap)) {
+            atomicOr(A.err, GBT_DEVERR_CAPACITY);
+            ok = false;
+        }
+        const uint32_t rec_start = rec;
+        bool long_copy = false;
+        if (ok && round == 0) {  // the branch node of this job
+            const PJob &job = A.jobs_in[j];
+            branch = (int32_t)pn++;
+            PNode &q = A.pn[branch];
+            for (int a = 0; a < 3; a++) {
+                q.lo[a] = job.lo[a];
+                q.hi[a] = job.hi[a];
+            }
+            q.leaf = 0;
+            q.nchild = 0;
+            attach(A, job.parent, job.slot, branch);
+        }
+        if (ok && act) {
+            if (split == 0) {
+                const int32_t p = (int32_t)pn++;
+                PNode &q = A.pn[p];
+                for (int a = 0; a < 3; a++) {
+                    q.lo[a] = C.box[a][mi][ln];
+                    q.hi[a] = C.box[3 + a][mi][ln];
+                }
+                q.leaf = 1;
+                q.nchild = 0;
+                q.rec_off = rec;
+                q.rec_cnt = n_rec;
+                for (uint32_t i = 0; i < n; i++) {
+                    const AuxCold &x = lane_cold(A.auxc, L, k, i, ln);
+                    if (x.count <= LANE_COPY) lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+                    else long_copy = true;
+                    rec += x.count;
+                }
+                C.n[mi][ln] = 1;
+                C.leaf[mi][ln] = p;
+            } else {
+                const int32_t depth = C.depth[mi][ln] + 1;
+#pragma unroll
+                for (int s = 0; s < 2; s++) {
+                    const uint32_t a = s ? split : 0, e = s ? n : split;
+                    const int slot = s ? ncuts : mi;
+                    LaneBox box;  // the side's box: union of its nodes before refinement
+                    lbox_empty(box);
+                    for (uint32_t i = a; i < e; i++) lbox_add(box, lane_node(aux, L, k, i, ln));
+                    for (int d = 0; d < 3; d++) {
+                        C.box[d][slot][ln] = box.lo[d];
+                        C.box[3 + d][slot][ln] = box.hi[d];
+                    }
+                    C.depth[slot][ln] = depth;
+                    if (tot[s] == 1) {
+                        const AuxCold &x = lane_cold(A.auxc, L, k, a, ln);
+                        const int32_t p = (int32_t)pn++;
+                        PNode &q = A.pn[p];
+                        for (int d = 0; d < 3; d++) {
+                            q.lo[d] = box.lo[d];
+                            q.hi[d] = box.hi[d];
+                        }
+                        q.leaf = 1;
+                        q.nchild = 0;
+                        q.rec_off = rec;
+                        q.rec_cnt = x.count;
+                        if (x.count <= LANE_COPY) lane_copy_records(A.aux_recs, A.recs, x.first, x.count, rec, A.n_prim, A.err);
+                        else long_copy = true;
+                        rec += x.count;
+                        C.n[slot][ln] = 1;
+                        C.leaf[slot][ln] = p;
+                    } else {
+                        C.off[slot][ln] = pool | 0x80000000u;
+                        C.n[slot][ln] = tot[s];
+                        C.leaf[slot][ln] = -1;
+                        for (uint32_t i = a; i < e; i++) {
+                            const uint32_t id = L.id[L.ord[k][i][ln]][ln];
+                            if (keep[s] >> (i - a) & 1u) {
+                                A.pool_out[pool++] = id;
+                            } else {
+                                A.pool_out[pool++] = (uint32_t)aux[id].c0;
+                                A.pool_out[pool++] = (uint32_t)A.auxc[id].c1;
+                            }
+                        }
+                    }
+                }
+                ncuts++;
+            }
+        }
+        lane_long_copies(A, L, long_copy, rec_start, split, n, k, tot[0], tot[1]);
+    }
+    // the branch's children: leaves, and a job for each cut
+    uint32_t n_lane_jobs = 0, n_big_jobs = 0;
+    if (ok)
+        for (int i = 0; i < ncuts; i++)
+            if (C.leaf[i][ln] < 0) {
+                if (lane_cut_job(A, C.n[i][ln])) n_lane_jobs++;
+                else n_big_jobs++;
+            }
+    uint32_t qs = warp_alloc(&A.g->job_ctr[out], n_lane_jobs, ln);
+    uint32_t qb = warp_alloc(&A.g->job_big_ctr[out], n_big_jobs, ln);
+    if (ok && ((uint64_t)qs + n_lane_jobs > A.job_cap || (uint64_t)qb + n_big_jobs > A.job_cap)) {
+        atomicOr(A.err, GBT_DEVERR_CAPACITY);
+        ok = false;
+    }
+    if (!ok) return;
+    PNode &B = A.pn[branch];
+    B.nchild = ncuts;
+    for (int i = 0; i < ncuts; i++) {
+        const int32_t lf = C.leaf[i][ln];
+        if (lf >= 0) {
+            B.child[i] = lf;
+            continue;
+        }
+        PJob nj;
+        nj.off = C.off[i][ln] & 0x7fffffffu;
+        nj.n = C.n[i][ln];
+        for (int d = 0; d < 3; d++) {
+            nj.lo[d] = C.box[d][i][ln];
+            nj.hi[d] = C.box[3 + d][i][ln];
+        }
+        nj.depth = C.depth[i][ln];
+        nj.parent = branch;
+        nj.slot = i;
+        nj.pad = 0;
+        if (lane_cut_job(A, nj.n)) A.jobs_out[qs++] = nj;
+        else A.jobs_out[A.job_cap - 1 - qb++] = nj;
+        my_max_n = max(my_max_n, nj.n);
     }
 }
 
@@ -1483,25 +1736,38 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
 // of the second list, swept by the whole warp, or 32 jobs of the lane list,
 // one per lane; a job of the lane list whose cut does not qualify (the root
 // job) is swept by the whole warp after them.
-// Shared memory of a level block: with the lane path, its scratch and the
+// Shared memory of a level block: with a lane path, its scratch and the
 // whole-block state take turns, so they share the space.
-template <int BS, bool LANES>
+template <int BS, int LMODE>
 struct LevelSmem {
     BlockShared<BS> block;
 };
 template <int BS>
-struct LevelSmem<BS, true> {
+struct LevelSmem<BS, 1> {
     union {
         BlockShared<BS> block;
         LaneScratch lane;
     };
 };
+struct LaneMulti {
+    LaneScratch lane;
+    LaneCuts cuts;
+};
+template <int BS>
+struct LevelSmem<BS, 2> {
+    union {
+        BlockShared<BS> block;
+        LaneMulti lm;
+    };
+};
 
-// LANES: one-warp blocks with the lane path (bf = 2); without it (bf > 2) a
-// one-warp block holds less state and more of them are resident.
-template <int BS, bool LANES = (BS == 32)>
-__global__ void __launch_bounds__(BS, BS == 32 ? (LANES ? 20 : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
-    __shared__ LevelSmem<BS, LANES> smem;
+// LMODE (one-warp blocks): 1 the lane path for bf = 2, 2 the lane path for
+// bf > 2 in rounds, 0 none (a one-warp block then holds less state and more
+// of them are resident).
+template <int BS, int LMODE = (BS == 32 ? 1 : 0)>
+__global__ void __launch_bounds__(BS, BS == 32 ? (LMODE ? 20 : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
+    constexpr bool LANES = LMODE != 0;
+    __shared__ LevelSmem<BS, LMODE> smem;
     BlockShared<BS> &sh = smem.block;
     const int in = A.parity, out = A.parity ^ 1;
     // Run only as the next level, after no stall and no device error, and only
@@ -1555,7 +1821,8 @@ __global__ void __launch_bounds__(BS, BS == 32 ? (LANES ? 20 : 32) : (BS == PT ?
                     const uint32_t n = A.jobs_in[j].n;
                     mine = lane_cut_job(A, n) && n <= nmax;
                 }
-                lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
+                if constexpr (LMODE == 1) lane_jobs(A, j, mine, smem.lane, screen, my_build_cost, my_max_n);
+                else lane_jobs_multi(A, j, mine, smem.lm.lane, smem.lm.cuts, screen, my_build_cost, my_max_n);
                 rest = __ballot_sync(0xffffffffu, valid && !mine);
             }
         }
@@ -1806,6 +2073,9 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     // a stall, after which that level is relaunched here with wider blocks.
     uint32_t level = 0;
     int parity = 0;
+    // lane path of one-warp levels: bf = 2 one split per lane; bf 3..4 rounds of splits (their
+    // cut table marks output-pool offsets with bit 31)
+    const int lmode = bf == 2 ? 1 : (bf <= MAX_BF_LANES && pool_cap < 0x80000000u ? 2 : 0);
     while (n_jobs > 0) {
         // one-warp blocks when every cut is small; WIDE-thread blocks for levels of a few
         // large cuts (the first ones), PT-thread blocks otherwise
@@ -1823,14 +2093,15 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
         // grid: at most the blocks that are resident at once
         int per_sm = 0;
-        if (variant == 0 && bf == 2) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, true>, 32, 0));
-        else if (variant == 0) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, false>, 32, 0));
+        if (variant == 0 && lmode == 1) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, 1>, 32, 0));
+        else if (variant == 0 && lmode == 2) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, 2>, 32, 0));
+        else if (variant == 0) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<32, 0>, 32, 0));
         else if (variant == 1) GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<PT>, PT, dyn));
         else GBT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_phr_level<WIDE>, WIDE, dyn));
         const uint32_t max_grid = (uint32_t)ctx->num_sms * (uint32_t)std::max(1, per_sm);
         // work items: one-warp blocks with lanes (bf = 2) take a second-list job or 32
         // lane-list jobs; the batch's later levels are not known yet and get the full grid
-        const uint32_t items = variant == 0 && bf == 2 ? n_big + (n_lane + 31) / 32 : n_jobs;
+        const uint32_t items = variant == 0 && lmode ? n_big + (n_lane + 31) / 32 : n_jobs;
         const uint32_t grid0 = std::min<uint32_t>(items, max_grid);
         const size_t per_block = gbt_align(scratch_bytes_for(cap));
         const uint32_t blocks = batch > 1 ? max_grid : grid0;
@@ -1881,8 +2152,9 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
             A.n_prim = N;
             A.err = ctx->d_error;
             const uint32_t grid = bi == 0 ? grid0 : max_grid;
-            if (variant == 0 && bf == 2) k_phr_level<32, true><<<grid, 32, 0, st>>>(A);
-            else if (variant == 0) k_phr_level<32, false><<<grid, 32, 0, st>>>(A);
+            if (variant == 0 && lmode == 1) k_phr_level<32, 1><<<grid, 32, 0, st>>>(A);
+            else if (variant == 0 && lmode == 2) k_phr_level<32, 2><<<grid, 32, 0, st>>>(A);
+            else if (variant == 0) k_phr_level<32, 0><<<grid, 32, 0, st>>>(A);
             else if (variant == 1) k_phr_level<PT><<<grid, PT, dyn, st>>>(A);
             else k_phr_level<WIDE><<<grid, WIDE, dyn, st>>>(A);
             GBT_CUDA(ctx, cudaGetLastError());
