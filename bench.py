@@ -504,10 +504,16 @@ def run_profile_case(args):
         print("profile case lbvh: 3 builds of %d triangles" % s["verts"].shape[0])
         return 0
     if args.profile == "phr":
+        params = (PHR[0], PHR[1], args.phr_bf)
+        times = []
         for _ in range(3):
-            pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux).close()
-        ctx.sync()
-        print("profile case phr: 3 PHR%s builds of %d triangles" % (str(PHR), s["verts"].shape[0]))
+            t0 = time.perf_counter()
+            b = pt.NewPHRBuilder(*params).BuildFromAuxilary(aux)
+            ctx.sync()
+            times.append((time.perf_counter() - t0) * 1e3)
+            b.close()
+        print("profile case phr: 3 PHR%s builds of %d triangles, wall ms %s" % (
+            str(params), s["verts"].shape[0], " ".join("%.2f" % t for t in times)))
         return 0
     bvh = pt.NewPHRBuilder(*PHR).BuildFromAuxilary(aux) if args.bvh == "phr" else aux
     ctx.check(ctx.L.gbt_bvh_set_layout(ctx.h, bvh.h, args.layout), "layout")
@@ -536,6 +542,8 @@ def main():
     ap.add_argument("--profile", choices=["render", "lbvh", "phr"], default=None,
                     help="run a small fixed case for an ncu capture and exit: 3 frames (render), 3 LBVH builds "
                          "or 3 PHR refinements of the LBVH")
+    ap.add_argument("--phr-bf", type=int, default=PHR[2], choices=[2, 3, 4],
+                    help="branching factor of --profile phr")
     ap.add_argument("--profile-scene", choices=["soup", "terrain"], default="soup",
                     help="scene of --profile lbvh: the 1M soup or the 8.4M-triangle terrain")
     ap.add_argument("--workload", choices=["soup", "batch", "adjoint", "terrain", "lbvh"], default="soup",
