@@ -42,6 +42,8 @@ constexpr int DEPTH_TABLE = 4096;
 // cuts are that small (on a 1M-triangle soup 93% of the splits sort 2-16
 // nodes), and a warp then works on 32 of them at once.
 constexpr uint32_t LANE_CUT = 16;
+// The same for the lane path of bf > 2, whose jobs' later cuts can double.
+constexpr uint32_t LANE_CUT_MULTI = 32;
 // Largest branching factor the lane path serves (its per-lane cut table).
 constexpr int MAX_BF_LANES = 4;
 // Longer record ranges of the lane path's leaves are copied by the whole warp.
@@ -780,10 +782,11 @@ struct BlockShared {
     uint32_t off;
 };
 
-// Whether a job goes to the lane list: a cut of 2..LANE_CUT >> (bf - 2) nodes
-// (every cut its splits sort then fits a lane's scratch).
+// Whether a job goes to the lane list: a cut of 2..LANE_CUT nodes (bf = 2), or
+// of 2..LANE_CUT_MULTI >> (bf - 2) nodes (bf > 2: every cut its splits sort
+// then fits a lane's scratch).
 __device__ __forceinline__ bool lane_cut_job(const LevelArgs &A, uint32_t n) {
-    return n >= 2 && A.bf <= MAX_BF_LANES && n <= (LANE_CUT >> (A.bf - 2));
+    return n >= 2 && A.bf <= MAX_BF_LANES && n <= (A.bf == 2 ? LANE_CUT : (LANE_CUT_MULTI >> (A.bf - 2)));
 }
 
 // Index in jobs_out for one new job of the given list (0xffffffff: no room).
@@ -1065,14 +1068,18 @@ __device__ __forceinline__ void job_block(const LevelArgs &A, const PJob &job, u
 // just those candidates; without screening every cost is float64.
 
 // Per-lane scratch, index-major so that the lanes of a warp use different banks.
-struct LaneScratch {
+template <uint32_t CUT_>
+struct LaneScratchT {
+    static constexpr uint32_t CUT = CUT_;  // the largest cut a lane sorts
     union {
-        unsigned long long key[LANE_CUT][32];  // sort keys
-        float c32[LANE_CUT][32];               // float32 split costs of a sweep
+        unsigned long long key[CUT][32];  // sort keys
+        float c32[CUT][32];               // float32 split costs of a sweep
     };
-    uint32_t id[LANE_CUT][32];       // the cut's node ids, in cut order
-    uint8_t ord[3][LANE_CUT][32];    // x, y, z orders: positions into id
+    uint32_t id[CUT][32];       // the cut's node ids, in cut order
+    uint8_t ord[3][CUT][32];    // x, y, z orders: positions into id
 };
+using LaneScratch = LaneScratchT<LANE_CUT>;             // bf = 2
+using LaneScratchMulti = LaneScratchT<LANE_CUT_MULTI>;  // bf > 2
 
 struct LaneBox {
     float lo[3], hi[3];
@@ -1105,19 +1112,22 @@ struct LanePick {
     int k;
 };
 
-__device__ __forceinline__ const AuxNode &lane_node(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+template <class LS>
+__device__ __forceinline__ const AuxNode &lane_node(const AuxNode *__restrict__ aux, const LS &L, int k,
                                                     uint32_t i, int ln) {
     return aux[L.id[L.ord[k][i][ln]][ln]];
 }
 
-__device__ __forceinline__ const AuxCold &lane_cold(const AuxCold *__restrict__ auxc, const LaneScratch &L, int k,
+template <class LS>
+__device__ __forceinline__ const AuxCold &lane_cold(const AuxCold *__restrict__ auxc, const LS &L, int k,
                                                     uint32_t i, int ln) {
     return auxc[L.id[L.ord[k][i][ln]][ln]];
 }
 
 // sort.SliceStable by barycenter component `axis`: insertion sort of the
 // order `src` (-1: the cut order) into `dst`; equal keys keep their order.
-__device__ void lane_sort(const AuxNode *__restrict__ aux, LaneScratch &L, int src, int dst, int axis, uint32_t n,
+template <class LS>
+__device__ void lane_sort(const AuxNode *__restrict__ aux, LS &L, int src, int dst, int axis, uint32_t n,
                           int ln) {
     for (uint32_t i = 0; i < n; i++) {
         const uint32_t p = src < 0 ? i : L.ord[src][i][ln];
@@ -1136,7 +1146,8 @@ __device__ void lane_sort(const AuxNode *__restrict__ aux, LaneScratch &L, int s
 
 // The float64 costs are evaluated out of line (see surface_below).
 // minCost's float64 cost of splitting order k before position i (phr.go:423-445).
-__device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+template <class LS>
+__device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux, const LS &L, int k,
                                                  uint32_t n, uint32_t i, int ln) {
     LaneBox l, r;
     lbox_empty(l);
@@ -1157,20 +1168,23 @@ __device__ __noinline__ double lane_split_cost64(const AuxNode *__restrict__ aux
 }
 
 // The float64 cost of a pick: its split's, or not splitting's (phr.go:432-439).
-__device__ __forceinline__ double lane_pick_cost64(const AuxNode *__restrict__ aux, const LaneScratch &L,
+template <class LS>
+__device__ __forceinline__ double lane_pick_cost64(const AuxNode *__restrict__ aux, const LS &L,
                                                    const LaneCut &c, int k, uint32_t split, int ln) {
     return split ? lane_split_cost64(aux, L, k, c.n, split, ln) : __dmul_rn(surface(c.lo, c.hi), (double)c.total);
 }
 
-__device__ __noinline__ bool lane_less64(const AuxNode *__restrict__ aux, const LaneScratch &L, LaneCut c, int ka,
+template <class LS>
+__device__ __noinline__ bool lane_less64(const AuxNode *__restrict__ aux, const LS &L, LaneCut c, int ka,
                                          uint32_t sa, int kb, uint32_t sb, int ln) {
     return lane_pick_cost64(aux, L, c, ka, sa, ln) < lane_pick_cost64(aux, L, c, kb, sb, ln);
 }
 
 // a.cost < b.cost as the float64 values compare: decided by the float32 values
 // when they are further apart than the screening slack
+template <class LS>
 __device__ __forceinline__ bool lane_less(const LanePick &a, const LanePick &b, const AuxNode *__restrict__ aux,
-                                          const LaneScratch &L, const LaneCut &c, bool screen, int ln) {
+                                          const LS &L, const LaneCut &c, bool screen, int ln) {
     if (a.split == 0 && b.split == 0) return false;  // both are the cost of not splitting
     if (screen) {
         if (__fmul_rn(a.c32, gbt_phr::SCREEN_SLACK) < b.c32) return true;
@@ -1182,7 +1196,7 @@ __device__ __forceinline__ bool lane_less(const LanePick &a, const LanePick &b, 
         uint32_t ma = 0, mb = 0;
         for (uint32_t i = 0; i < a.split; i++) ma |= 1u << L.ord[a.k][i][ln];
         for (uint32_t i = 0; i < b.split; i++) mb |= 1u << L.ord[b.k][i][ln];
-        const uint32_t full = (1u << c.n) - 1u;
+        const uint32_t full = c.n >= 32 ? 0xffffffffu : (1u << c.n) - 1u;
         if (ma == mb || ma == (full ^ mb)) return false;
     }
     return lane_less64(aux, L, c, a.k, a.split, b.k, b.split, ln);
@@ -1190,7 +1204,8 @@ __device__ __forceinline__ bool lane_less(const LanePick &a, const LanePick &b, 
 
 // The first position of least float64 cost among those whose float32 cost is
 // at most `lim` (all positions when lim is +inf).
-__device__ __noinline__ uint32_t lane_first_min64(const AuxNode *__restrict__ aux, const LaneScratch &L, int k,
+template <class LS>
+__device__ __noinline__ uint32_t lane_first_min64(const AuxNode *__restrict__ aux, const LS &L, int k,
                                                   uint32_t n, float lim, bool all, int ln) {
     double bc = INFINITY;
     uint32_t bi = 1;
@@ -1207,7 +1222,8 @@ __device__ __noinline__ uint32_t lane_first_min64(const AuxNode *__restrict__ au
 
 // minCost (phr.go:414-459) over order k: the first cheapest split position,
 // or not splitting when that is not cheaper.
-__device__ LanePick lane_min_cost(const AuxNode *__restrict__ aux, LaneScratch &L, int k, const LaneCut &c,
+template <class LS>
+__device__ LanePick lane_min_cost(const AuxNode *__restrict__ aux, LS &L, int k, const LaneCut &c,
                                   bool screen, int ln) {
     const uint32_t n = c.n;
     LanePick best;
@@ -1290,7 +1306,8 @@ __device__ void lane_copy_records(const float4 *__restrict__ src, float4 *__rest
 // SweepSAH (phr.go:368-405) of the lane's cut in L.id: x from the cut order,
 // y from the x order, z from the y order when x is cheaper than y, else from
 // the x order; the winning order and split (0: not splitting).
-__device__ __forceinline__ LanePick lane_sweep_sah(const AuxNode *__restrict__ aux, LaneScratch &L, const LaneCut &c,
+template <class LS>
+__device__ __forceinline__ LanePick lane_sweep_sah(const AuxNode *__restrict__ aux, LS &L, const LaneCut &c,
                                                    bool screen, int ln) {
     const uint32_t n = c.n;
     lane_sort(aux, L, -1, 0, 0, n, ln);
@@ -1307,7 +1324,8 @@ __device__ __forceinline__ LanePick lane_sweep_sah(const AuxNode *__restrict__ a
 // refined (phr.go:313-338) of both sides of a split of order k: per side the
 // nodes kept (bit per position) and the refined size (a node replaced by its
 // two children counts 2), against the threshold of the cut's depth.
-__device__ __forceinline__ void lane_refine(const LevelArgs &A, const LaneScratch &L, int k, uint32_t split,
+template <class LS>
+__device__ __forceinline__ void lane_refine(const LevelArgs &A, const LS &L, int k, uint32_t split,
                                             uint32_t n, int32_t depth, bool screen, int ln, uint32_t (&tot)[2],
                                             uint32_t (&keep)[2]) {
     const int di = min(depth, DEPTH_TABLE - 1);
@@ -1335,7 +1353,8 @@ __device__ __forceinline__ void lane_refine(const LevelArgs &A, const LaneScratc
 // The long record ranges of the lanes' leaves (split 0: every node of order k
 // in one leaf; else the sides that became leaves), lane by lane, copied by
 // the whole warp in the order the lane allocated them from rec_start.
-__device__ __forceinline__ void lane_long_copies(const LevelArgs &A, const LaneScratch &L, bool long_copy,
+template <class LS>
+__device__ __forceinline__ void lane_long_copies(const LevelArgs &A, const LS &L, bool long_copy,
                                                  uint32_t rec_start, uint32_t split, uint32_t n, int k, uint32_t tot0,
                                                  uint32_t tot1) {
     unsigned pending = __ballot_sync(0xffffffffu, long_copy);
@@ -1524,7 +1543,7 @@ struct LaneCuts {  // per lane, index-major
     int32_t leaf[MAX_BF_LANES][32];    // >= 0: the leaf's PNode; -1: a cut
 };
 
-__device__ void lane_jobs_multi(const LevelArgs &A, uint32_t j, bool mine, LaneScratch &L, LaneCuts &C, bool screen,
+__device__ void lane_jobs_multi(const LevelArgs &A, uint32_t j, bool mine, LaneScratchMulti &L, LaneCuts &C, bool screen,
                                 unsigned long long &my_build_cost, uint32_t &my_max_n) {
     const int ln = threadIdx.x & 31;
     const AuxNode *__restrict__ aux = A.aux;
@@ -1555,7 +1574,7 @@ __device__ void lane_jobs_multi(const LevelArgs &A, uint32_t j, bool mine, LaneS
                     mi = i;
                 }
             }
-        if (ok && n > LANE_CUT) {  // cannot happen for a qualifying job; the scratch holds LANE_CUT
+        if (ok && n > LANE_CUT_MULTI) {  // cannot happen for a qualifying job; the scratch holds LANE_CUT_MULTI
             atomicOr(A.err, GBT_DEVERR_CAPACITY);
             ok = false;
         }
@@ -1750,7 +1769,7 @@ struct LevelSmem<BS, 1> {
     };
 };
 struct LaneMulti {
-    LaneScratch lane;
+    LaneScratchMulti lane;
     LaneCuts cuts;
 };
 template <int BS>
