@@ -1533,7 +1533,7 @@ __device__ void lane_jobs(const LevelArgs &A, uint32_t j, bool mine, LaneScratch
 // bf cuts).  The lanes of a warp take their jobs' splits in rounds, with one
 // allocation per round; a cut a split makes goes to the output pool at once
 // (as in job_block), and the lane's next round reads it back from there.  A
-// job qualifies when its cut has at most LANE_CUT >> (bf - 2) nodes, so that
+// job qualifies when its cut has at most LANE_CUT_MULTI >> (bf - 2) nodes, so that
 // every cut it sorts fits the lane scratch (a refinement at most doubles one).
 struct LaneCuts {  // per lane, index-major
     uint32_t off[MAX_BF_LANES][32];    // pool offset; bit 31: in the output pool
