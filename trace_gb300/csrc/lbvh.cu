@@ -642,12 +642,100 @@ __device__ __forceinline__ int32_t exch_acq_rel(int32_t *p, int32_t v) {
     return old;
 }
 
-__global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
-                                              const uint32_t *__restrict__ run, const uint64_t *__restrict__ ukey,
-                                              const float4 *__restrict__ recs, float4 *nodes, int32_t *other,
-                                              uint32_t *subtree, int32_t *parent_of, uint2 *range, uint32_t n) {
+// Emission block: the leaves of one block of threads and the inner nodes whose
+// whole range lies inside them.  Such a node's two children both come from
+// the block, so their hand-off goes through shared memory; the others go
+// through the global hand-off word.
+constexpr int EMIT_THREADS = 256;
+
+// A node that k_emit hands to k_emit_top: its box, distinct-code range and index.
+struct EmitState {
+    float lo[3], hi[3];
+    uint32_t l, r, ref, pad0;
+    uint32_t pad[2];
+};
+
+// Second child at a node reached through the global hand-off word: fold in the
+// sibling's slot (release by the sibling's exchange, acquire by this one's).
+__device__ __forceinline__ void emit_merge_global(const float4 *nd, int slot, float3 &lo, float3 &hi) {
+    const float4 sb = __ldcg(nd + (slot ^ 1));
+    const float2 sz = __ldcg(reinterpret_cast<const float2 *>(nd + 2) + (slot ^ 1));
+    lo = make_float3(fminf(lo.x, sb.x), fminf(lo.y, sb.z), fminf(lo.z, sz.x));
+    hi = make_float3(fmaxf(hi.x, sb.y), fmaxf(hi.y, sb.w), fmaxf(hi.z, sz.y));
+}
+
+__device__ __forceinline__ void slot_write(float4 *nd, int slot, float3 lo, float3 hi, int32_t ref, int32_t cnt) {
+    nd[slot] = make_float4(lo.x, hi.x, lo.y, hi.y);
+    reinterpret_cast<float2 *>(nd + 2)[slot] = make_float2(lo.z, hi.z);
+    reinterpret_cast<int2 *>(nd + 3)[slot] = make_int2(ref, cnt);
+}
+
+__device__ __forceinline__ float4 lds_f4(const float4 *p) {
+    float4 v;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a) : "memory");
+    return v;
+}
+
+// Number of nodes (leaves included) under a node of distinct-code range [l, r].
+__device__ __forceinline__ uint32_t range_size(uint32_t l, uint32_t r) { return 2u * (r - l) + 1u; }
+
+__global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
+                                                       const uint32_t *__restrict__ run,
+                                                       const uint64_t *__restrict__ ukey,
+                                                       const float4 *__restrict__ recs, float4 *nodes, int32_t *other,
+                                                       uint32_t *subtree, int32_t *parent_of, uint2 *range,
+                                                       uint32_t n, EmitState *top, uint32_t *top_n, uint32_t top_cap,
+                                                       unsigned int *err) {
+    constexpr int B = EMIT_THREADS, NW = B / 32;
+    // s_d[i]: common prefix length at the split k0-1+i | k0+i (i = 0..B), -1 past
+    // either end of the codes.  s_loc[t]: inner node k0+t has its whole range in
+    // this block's leaves [k0, k0+B).  A node k covers the widest range around
+    // split k whose splits all share at least its prefix length, so its range
+    // stays inside iff a shorter prefix occurs among the block's splits on both
+    // sides of k (the splits k0-1 and k0+B-1 at the block's edges included).
+    __shared__ int s_d[B + 1];
+    __shared__ int s_suf[B];
+    __shared__ int s_wpre[NW], s_wsuf[NW];
+    __shared__ int32_t s_oth[B];
+    __shared__ float4 s_r0[2][B];  // per inner node, per child slot: lo.xyz, hi.x
+    __shared__ float4 s_r1[2][B];  //                                 hi.yz, ref, count
+    __shared__ uint8_t s_loc[B];
     const uint32_t U = hdr_in->n_unique;
-    uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t k0 = blockIdx.x * B;
+    for (int i = t; i <= B; i += B) {
+        const long long j = (long long)k0 - 1 + i;  // split j | j+1
+        s_d[i] = (j >= 0 && j + 1 < (long long)U) ? prefix_len(ukey, (uint32_t)j, (uint32_t)j + 1) : -1;
+    }
+    s_oth[t] = -1;
+    __syncthreads();
+    // pre = min s_d[0..t]; suf = min s_d[t+1..B-1+1] (inclusive scans, warp shuffles + warp totals)
+    int pre = s_d[t], suf = s_d[t + 1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, pre, o), b = __shfl_down_sync(0xffffffffu, suf, o);
+        if (lane >= o) pre = min(pre, a);
+        if (lane + o < 32) suf = min(suf, b);
+    }
+    if (lane == 31) s_wpre[w] = pre;
+    if (lane == 0) s_wsuf[w] = suf;
+    __syncthreads();
+    for (int k = 0; k < NW; k++) {
+        if (k < w) pre = min(pre, s_wpre[k]);
+        if (k > w) suf = min(suf, s_wsuf[k]);
+    }
+    s_suf[t] = suf;  // min s_d[t+1..B]
+    __syncthreads();
+    {
+        // node k0+t is split t+1: shorter prefixes needed in s_d[0..t] and s_d[t+2..B]
+        const int dk = s_d[t + 1];
+        const int right = t + 1 < B ? s_suf[t + 1] : 64;
+        s_loc[t] = (dk >= 0 && pre < dk && right < dk) ? 1 : 0;
+    }
+    __syncthreads();
+
+    const uint32_t u = k0 + t;
     if (u >= U || u >= n) return;
     uint32_t first = run[u], last = run[u + 1];
     float3 lo, hi;
@@ -659,7 +747,6 @@ __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader
         hi = make_float3(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z));
     }
     int32_t ref = (int32_t)first, cnt = (int32_t)(last - first);
-    uint32_t size = 1;
     uint32_t l = u, r = u;
     for (;;) {
         if (l == 0 && r == U - 1) {
@@ -670,31 +757,104 @@ __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader
             if (cnt == 0) parent_of[ref] = -1;
             return;
         }
-        bool left = (l == 0) || (r != U - 1 && prefix_len(ukey, r, r + 1) > prefix_len(ukey, l - 1, l));
-        uint32_t p = left ? r : l - 1;
-        int slot = left ? 0 : 1;
+        // prefix lengths at the splits r|r+1 and l-1|l (this block's from shared memory)
+        const int dr = (r == U - 1) ? -1
+                       : (r + 1 >= k0 && r + 1 <= k0 + B) ? s_d[r + 1 - k0] : prefix_len(ukey, r, r + 1);
+        const int dl = (l == 0) ? -1 : (l >= k0 && l <= k0 + B) ? s_d[l - k0] : prefix_len(ukey, l - 1, l);
+        const bool left = dr > dl;
+        const uint32_t p = left ? r : l - 1;
+        const int slot = left ? 0 : 1;
         float4 *nd = nodes + 4 * (size_t)p;
-        nd[slot] = make_float4(lo.x, hi.x, lo.y, hi.y);
-        reinterpret_cast<float2 *>(nd + 2)[slot] = make_float2(lo.z, hi.z);
-        reinterpret_cast<int2 *>(nd + 3)[slot] = make_int2(ref, cnt);
+        const uint32_t q = p - k0;
+        if (p >= k0 && q < (uint32_t)B && s_loc[q]) {
+            // both children are this block's: hand over through shared memory; the
+            // second child writes the whole node
+            s_r0[slot][q] = make_float4(lo.x, lo.y, lo.z, hi.x);
+            s_r1[slot][q] = make_float4(hi.y, hi.z, __int_as_float(ref), __int_as_float(cnt));
+            __threadfence_block();
+            const int32_t o = atomicExch(&s_oth[q], (int32_t)(left ? l : r));
+            if (o < 0) return;  // first child here: the sibling finishes the node
+            __threadfence_block();
+            const float4 a = lds_f4(&s_r0[slot ^ 1][q]), b = lds_f4(&s_r1[slot ^ 1][q]);
+            const float3 slo = make_float3(a.x, a.y, a.z), shi = make_float3(a.w, b.x, b.y);
+            const int32_t sref = __float_as_int(b.z), scnt = __float_as_int(b.w);
+            const float3 lo0 = left ? lo : slo, hi0 = left ? hi : shi, lo1 = left ? slo : lo, hi1 = left ? shi : hi;
+            nd[0] = make_float4(lo0.x, hi0.x, lo0.y, hi0.y);
+            nd[1] = make_float4(lo1.x, hi1.x, lo1.y, hi1.y);
+            nd[2] = make_float4(lo0.z, hi0.z, lo1.z, hi1.z);
+            reinterpret_cast<int4 *>(nd)[3] =
+                left ? make_int4(ref, cnt, sref, scnt) : make_int4(sref, scnt, ref, cnt);
+            if (cnt == 0) parent_of[ref] = (int32_t)p;
+            if (scnt == 0) parent_of[sref] = (int32_t)p;
+            lo = make_float3(fminf(lo.x, slo.x), fminf(lo.y, slo.y), fminf(lo.z, slo.z));
+            hi = make_float3(fmaxf(hi.x, shi.x), fmaxf(hi.y, shi.y), fmaxf(hi.z, shi.z));
+            if (left) r = (uint32_t)o;
+            else l = (uint32_t)o;
+            subtree[p] = range_size(l, r);
+            range[p] = make_uint2(l, r);  // distinct-code range of inner node p
+            ref = (int32_t)p;
+            cnt = 0;
+            continue;
+        }
+        // Node p spans blocks.  Its second child arrives here only when both children
+        // are this kernel's (p is the split at a block edge, one per edge); the node
+        // then goes to k_emit_top, which climbs the rest of the tree.
+        slot_write(nd, slot, lo, hi, ref, cnt);
         if (cnt == 0) parent_of[ref] = (int32_t)p;
-        // release: this child's slot is visible before the hand-off word; acquire: the
-        // sibling's slot, written before its own exchange, is read after this one
-        int32_t o = exch_acq_rel(&other[p], (int32_t)(left ? l : r));
-        if (o < 0) return;  // first child here: the sibling finishes the node
-        float4 sb = __ldcg(nd + (slot ^ 1));
-        float2 sz = __ldcg(reinterpret_cast<const float2 *>(nd + 2) + (slot ^ 1));
-        int2 sr = __ldcg(reinterpret_cast<const int2 *>(nd + 3) + (slot ^ 1));
-        lo = make_float3(fminf(lo.x, sb.x), fminf(lo.y, sb.z), fminf(lo.z, sz.x));
-        hi = make_float3(fmaxf(hi.x, sb.y), fmaxf(hi.y, sb.w), fmaxf(hi.z, sz.y));
-        uint32_t sib = sr.y > 0 ? 1u : __ldcg(subtree + sr.x);
-        size = 1 + size + sib;
-        subtree[p] = size;
+        const int32_t o = exch_acq_rel(&other[p], (int32_t)(left ? l : r));
+        if (o < 0) return;
+        emit_merge_global(nd, slot, lo, hi);
         if (left) r = (uint32_t)o;
         else l = (uint32_t)o;
-        range[p] = make_uint2(l, r);  // distinct-code range of inner node p
+        subtree[p] = range_size(l, r);
+        range[p] = make_uint2(l, r);
+        const uint32_t k = atomicAdd(top_n, 1u);
+        if (k >= top_cap) {
+            atomicOr(err, GBT_DEVERR_CAPACITY);
+            return;
+        }
+        top[k] = EmitState{{lo.x, lo.y, lo.z}, {hi.x, hi.y, hi.z}, l, r, p, 0u, {0u, 0u}};
+        return;
+    }
+}
+
+// The nodes that span blocks: one thread per node k_emit handed over, climbing
+// with the global hand-off word (the same walk as k_emit, by split prefixes
+// read from the codes).
+__global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t *__restrict__ ukey, float4 *nodes,
+                                                  int32_t *other, uint32_t *subtree, int32_t *parent_of,
+                                                  uint2 *range, const EmitState *__restrict__ top,
+                                                  const uint32_t *top_n, uint32_t top_cap) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*top_n, top_cap)) return;
+    const uint32_t U = hdr->n_unique;
+    const EmitState e = top[i];
+    float3 lo = make_float3(e.lo[0], e.lo[1], e.lo[2]), hi = make_float3(e.hi[0], e.hi[1], e.hi[2]);
+    uint32_t l = e.l, r = e.r;
+    int32_t ref = (int32_t)e.ref;
+    for (;;) {
+        if (l == 0 && r == U - 1) {
+            hdr->root_ref = ref;
+            hdr->root_cnt = 0;
+            hdr->root_lo[0] = lo.x; hdr->root_lo[1] = lo.y; hdr->root_lo[2] = lo.z; hdr->root_lo[3] = 0.f;
+            hdr->root_hi[0] = hi.x; hdr->root_hi[1] = hi.y; hdr->root_hi[2] = hi.z; hdr->root_hi[3] = 0.f;
+            parent_of[ref] = -1;
+            return;
+        }
+        const bool left = (l == 0) || (r != U - 1 && prefix_len(ukey, r, r + 1) > prefix_len(ukey, l - 1, l));
+        const uint32_t p = left ? r : l - 1;
+        const int slot = left ? 0 : 1;
+        float4 *nd = nodes + 4 * (size_t)p;
+        slot_write(nd, slot, lo, hi, ref, 0);
+        parent_of[ref] = (int32_t)p;
+        const int32_t o = exch_acq_rel(&other[p], (int32_t)(left ? l : r));
+        if (o < 0) return;
+        emit_merge_global(nd, slot, lo, hi);
+        if (left) r = (uint32_t)o;
+        else l = (uint32_t)o;
+        subtree[p] = range_size(l, r);
+        range[p] = make_uint2(l, r);
         ref = (int32_t)p;
-        cnt = 0;
     }
 }
 
@@ -703,12 +863,20 @@ __global__ void __launch_bounds__(256) k_emit(const BvhHeader *hdr_in, BvhHeader
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static size_t lbvh_scratch_layout(uint32_t n, size_t *acc_off, SortScratch *ss, size_t *rle_off) {
+// Emission blocks: one per EMIT_THREADS distinct codes; at most one node per
+// block edge goes to k_emit_top.
+static uint32_t emit_blocks(uint32_t n) { return (n + EMIT_THREADS - 1) / EMIT_THREADS; }
+
+static size_t lbvh_scratch_layout(uint32_t n, size_t *acc_off, SortScratch *ss, size_t *rle_off,
+                                  size_t *top_off = nullptr) {
     *acc_off = 0;
     *ss = sort_layout(n, gbt_align(6 * sizeof(unsigned long long)));
     *rle_off = ss->total;
     uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
-    return gbt_align(*rle_off + (size_t)(rt + 1) * sizeof(uint32_t));
+    const size_t t = gbt_align(*rle_off + (size_t)(rt + 1) * sizeof(uint32_t));
+    if (top_off) *top_off = t;
+    // counter (16 bytes), then the hand-over list
+    return gbt_align(t + 16 + (size_t)emit_blocks(n) * sizeof(EmitState));
 }
 
 size_t gbt_lbvh_scratch_bytes(uint32_t n) {
@@ -742,9 +910,9 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     const uint32_t n_tri = sc->n_tri, n = sc->n_tri + sc->n_sph;
     if (n == 0) return gbt_fail(ctx, GBT_EINVAL, "empty scene");
     if (n >= (1u << 30)) return gbt_fail(ctx, GBT_EINVAL, "scene larger than 2^30 primitives");
-    size_t acc_off, rle_off;
+    size_t acc_off, rle_off, top_off;
     SortScratch ss;
-    size_t need = lbvh_scratch_layout(n, &acc_off, &ss, &rle_off);
+    size_t need = lbvh_scratch_layout(n, &acc_off, &ss, &rle_off, &top_off);
     void *scr = nullptr;
     int rc = gbt_scratch(ctx, need, &scr);
     if (rc) return rc;
@@ -767,9 +935,16 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr);
     k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey);
     k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims);
+    uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
+    EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
+    const uint32_t eb = emit_blocks(n);
     GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
-    k_emit<<<(n + 255) / 256, 256, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
-                                            bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n);
+    GBT_CUDA(ctx, cudaMemsetAsync(top_n, 0, sizeof(uint32_t), st));
+    k_emit<<<eb, EMIT_THREADS, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
+                                        bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n, top, top_n, eb,
+                                        ctx->d_error);
+    k_emit_top<<<(eb + 127) / 128, 128, 0, st>>>(bvh->d_hdr, bvh->d_ukey, bvh->d_nodes, bvh->d_other, bvh->d_size,
+                                                 bvh->d_parent, bvh->d_range, top, top_n, eb);
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }
