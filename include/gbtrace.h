@@ -229,7 +229,9 @@ int gbt_trace_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t 
 
 /* ---- renderer (render.go:91-129 ImageRenderer.RenderToBuffer) -------- */
 /* rgb: width*height*3 floats, row y=0 is the bottom row (buffer.go:47-49
- * order); each pixel is the mean of spp samples. */
+ * order); each pixel is the mean of spp samples.  A page-locked rgb
+ * (gbt_host_alloc, cudaMallocHost, cudaHostRegister) is written by the
+ * frame's last kernel directly; other host memory gets a copy. */
 /* pkg/pt/render.go:137-197 HeatMapRenderer.RenderToBuffer: per pixel the
  * pixel-centre ray's BVH.traversalSteps (bvh.go:21-44: inner nodes whose box
  * is intersected, children popped last-first, culled by the closest hit so

@@ -150,3 +150,31 @@ def test_measured_packet_choice_keeps_the_image(ctx):
         assert st0["rays_traced"] == st1["rays_traced"] == st2["rays_traced"]
     finally:
         ctx.set_option("primary_packets", 2)
+
+
+def test_render_into_page_locked_image_equals_copy(ctx):
+    """gbt_render writes a page-locked host image from the frame's last kernel and
+    copies into other host memory; the same seed gives the same image bits (spp 1:
+    one path per pixel, so each shading launch adds at most once to a pixel)."""
+    import ctypes as C
+
+    from trace_gb300 import _lib
+
+    s = scenes.cornell()
+    w, h = 64, 48
+    rd = s["render"]
+    cam = dict(s["camera"], aspect=w / h)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    g = pt.DefaultLBVH(ds)
+    ref, _ = g.render(cam, w, h, 1, rd["max_depth"], rd["miss_mode"], rd["miss_color"], seed=7)
+    hp = C.c_void_p()
+    ctx.check(ctx.L.gbt_host_alloc(ctx.h, w * h * 3 * 4, C.byref(hp)), "host_alloc")
+    try:
+        img = np.ctypeslib.as_array(C.cast(hp, C.POINTER(C.c_float)), shape=(h, w, 3))
+        img[...] = -1.0
+        p = _lib.RenderParams(w, h, 1, rd["max_depth"], rd["miss_mode"], (C.c_float * 3)(*rd["miss_color"]), 7)
+        st = _lib.RenderStats()
+        ctx.check(ctx.L.gbt_render(ctx.h, g.h, C.byref(pt.make_camera(cam)), C.byref(p), hp, C.byref(st)), "render")
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    finally:
+        ctx.check(ctx.L.gbt_host_free(ctx.h, hp), "host_free")

@@ -690,7 +690,20 @@ extern "C" int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, con
     if (!ctx || !bvh || !cam || !p || !rgb) return GBT_EINVAL;
     if (p->width < 2 || p->height < 2) return gbt_fail(ctx, GBT_EINVAL, "render: width and height must be >= 2");
     size_t bytes = (size_t)p->width * p->height * 3 * sizeof(float);
-    if (ctx->d_out_bytes < bytes) {
+    // A page-locked host image (cudaMallocHost, cudaHostAlloc or cudaHostRegister)
+    // is mapped into the device's address space: the last kernel of the frame
+    // writes it directly, with no copy of the image afterwards.  Other host
+    // memory receives the image by a copy from a device buffer.
+    float *direct = nullptr;
+    {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, rgb) == cudaSuccess) {
+            if (pa.type == cudaMemoryTypeHost && pa.devicePointer) direct = static_cast<float *>(pa.devicePointer);
+        } else {
+            cudaGetLastError();
+        }
+    }
+    if (!direct && ctx->d_out_bytes < bytes) {
         cudaStreamSynchronize(ctx->stream);
         cudaFree(ctx->d_out);
         ctx->d_out = nullptr;
@@ -698,12 +711,12 @@ extern "C" int gbt_render(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, con
         GBT_TRY(dalloc(ctx, &ctx->d_out, bytes / sizeof(float)));
         ctx->d_out_bytes = bytes;
     }
-    float *d = ctx->d_out;
+    float *d = direct ? direct : ctx->d_out;
     cudaEventRecord(ctx->ev[0], ctx->stream);
     int rc = gbt_render_enqueue(ctx, bvh, cam, p, d);
     cudaEventRecord(ctx->ev[1], ctx->stream);
     cudaError_t e = cudaSuccess;
-    if (!rc) e = cudaMemcpyAsync(rgb, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    if (!rc && !direct) e = cudaMemcpyAsync(rgb, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
     if (!rc && !e) rc = gbt_check_device_error(ctx, "render");
     cudaStreamSynchronize(ctx->stream);
     if (e) return gbt_cuda_fail(ctx, e, "render copy");
