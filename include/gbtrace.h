@@ -207,8 +207,10 @@ int gbt_lbvh_sorted(gbt_ctx *ctx, gbt_bvh *bvh, uint64_t *codes, int32_t *idx);
  * call sorts n 63-bit Morton codes ascending with their input positions as
  * values (stable: equal codes keep input order), exactly as the pairs
  * gbt_lbvh_build produces, and allocates nothing: the caller passes the device
- * input (d_codes_in, not modified) and outputs (d_codes_out, d_idx_out, n
- * entries each); the scratch is a fixed static device array of about 4 MiB
+ * input (d_codes_in) and outputs (d_codes_out, d_idx_out, n entries each).
+ * The input must not overlap either output; it is then left unmodified (the
+ * first sort pass writes the outputs while later passes still need the
+ * input's order).  The scratch is a fixed static device array of about 4 MiB
  * that every GPU loading the library holds until exit, so
  * n <= GBT_NOALLOC_MAX_PAIRS, else GBT_EINVAL.  No context is needed: work is
  * queued on `stream` (a cudaStream_t, NULL for the default stream) of the

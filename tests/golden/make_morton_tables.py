@@ -3,15 +3,17 @@ there as a comment) into tests/golden/morton256.json.
 
 These 3 x 256 entries are the only known-answer vectors the reference ships
 for the LBVH path: morton256_x[b] is splitBy3(b), _y is that shifted by 1,
-_z by 2.  Run in a checkout that has the reference mounted; the committed
-JSON is what the tests read.
+_z by 2.  Usage: python make_morton_tables.py <path to pkg/pt/morton.go of the
+reference>; the committed JSON is what the tests read.
 """
 import json
 import os
 import re
 import sys
 
-SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/pkg/pt/morton.go"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_morton_tables.py <path to the reference's pkg/pt/morton.go>")
+SRC = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "morton256.json")
 
 text = open(SRC).read()

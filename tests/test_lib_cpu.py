@@ -69,6 +69,34 @@ def test_obj_parse_fan_triangulation_and_negative_indices(tmp_path):
     assert np.all(np.abs(np.abs(verts) - 0.5) < 1e-7)
 
 
+def test_reference_cube_obj():
+    """The reference's own fixture (assets/cube.obj, copied to tests/golden/): 12 triangles
+    with per-face normals (obj.go:19-140), checked against a direct reading of the file."""
+    path = os.path.join(ROOT, "tests", "golden", "cube.obj")
+    g = pt.ParseFromPath(path)
+    assert g.has_normals
+    v, vn, want_v, want_n = [None], [None], [], []
+    for line in open(path):
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "v":
+            v.append([float(x) for x in f[1:4]])
+        elif f[0] == "vn":
+            vn.append([float(x) for x in f[1:4]])
+        elif f[0] == "f":
+            idx = [tuple(int(k) for k in a.split("/")) for a in f[1:]]
+            assert len(idx) == 3  # the fixture is all triangles
+            want_v.append(sum((v[i[0]] for i in idx), []))
+            want_n.append(sum((vn[i[2]] for i in idx), []))
+    assert g.verts.shape == (12, 9)
+    np.testing.assert_array_equal(g.verts, np.asarray(want_v, np.float32))
+    np.testing.assert_array_equal(g.normals, np.asarray(want_n, np.float32))
+    # each face's three normals agree and are axis-aligned unit vectors
+    n3 = g.normals.reshape(12, 3, 3)
+    assert np.all(n3 == n3[:, :1]) and np.all(np.abs(n3).sum(axis=2) == 1)
+
+
 def test_obj_parse_without_normals_and_errors(tmp_path):
     p = tmp_path / "tri.obj"
     p.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
