@@ -252,6 +252,48 @@ int gbt_render_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gb
                      float *d_rgb);
 int gbt_render_last_stats(gbt_ctx *ctx, gbt_render_stats *stats);
 
+/* ---- render targets (pkg/pt/buffer.go) -------------------------------
+ * A device-resident Buffer that RenderToBuffer adds samples to, and its
+ * ToImage.  Rows are in buffer order (row y = 0 first, the bottom row of the
+ * view: buffer.go:47-49).
+ *   GBT_BUFFER_PIXEL  NewPxlBuffer (buffer.go:34-45): each pixel is the running
+ *                     mean of every sample added to it, across calls
+ *                     (Pixel.addSample, buffer.go:19-26)
+ *   GBT_BUFFER_FRAME  NewFrameBuffer (buffer.go:83-89): each pixel holds the
+ *                     last sample written (buffer.go:91-93), i.e. one sample of
+ *                     the last call's last pass; only that pass is traced
+ * The reference seeds every RenderToBuffer call from the clock
+ * (render.go:117); call k on a buffer draws with params->seed + k *
+ * 0x9E3779B97F4A7C15, so repeated calls with the same parameters add new
+ * samples.  The first call into a PIXEL buffer gives gbt_render's image. */
+typedef struct gbt_buffer gbt_buffer;
+#define GBT_BUFFER_PIXEL 0
+#define GBT_BUFFER_FRAME 1
+int gbt_buffer_create(gbt_ctx *ctx, int32_t kind, int32_t width, int32_t height, gbt_buffer **out);
+int gbt_buffer_destroy(gbt_buffer *buffer);
+/* ImageRenderer.RenderToBuffer (render.go:91-129) into `buffer`; params->width
+ * and height must be the buffer's.  The _async form only enqueues. */
+int gbt_render_to_buffer(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+                         gbt_buffer *buffer, gbt_render_stats *stats);
+int gbt_render_to_buffer_async(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const gbt_render_params *params,
+                               gbt_buffer *buffer);
+/* Buffer.addSample (buffer.go:8-12) of a whole image: d_rgb (device,
+ * width*height*3 floats) holds the mean of `samples` samples per pixel.  A
+ * PIXEL buffer blends it into its running mean with weight samples / (samples
+ * held + samples); a FRAME buffer takes it.  Enqueue only.  It is how
+ * HeatMapRenderer.RenderToBuffer (render.go:155-197, one sample per pixel)
+ * writes into a buffer. */
+int gbt_buffer_add_async(gbt_ctx *ctx, gbt_buffer *buffer, const float *d_rgb, int32_t samples);
+/* The buffer's colours (rgb: width*height*3 floats, may be NULL) and the
+ * samples per pixel it holds (samples, may be NULL). */
+int gbt_buffer_read(gbt_ctx *ctx, gbt_buffer *buffer, float *rgb, uint64_t *samples);
+/* PixelBuffer.ToImage / FrameBuffer.ToImage (buffer.go:60-69, 104-116):
+ * rgba, width*height*4 bytes, image row 0 first.  Each channel is
+ * uint8(Clamp(sqrt(c), 0, 1) * 255) in float64 (Color.goColor, math.go:20-25),
+ * alpha 255.  Buffer row r lands on image row height - r, so buffer row 0 is
+ * dropped and image row 0 stays (0, 0, 0, 0), as in the reference. */
+int gbt_buffer_to_image(gbt_ctx *ctx, gbt_buffer *buffer, uint8_t *rgba);
+
 /* ---- batched rendering (no counterpart in the reference, which renders one
  * scene per RenderToBuffer call, render.go:91-129) ------------------------ */
 typedef struct {

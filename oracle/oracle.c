@@ -1707,3 +1707,36 @@ int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bv
     *out = o;
     return ORC_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* ToImage (buffer.go:60-69, 104-116) and Color.goColor (math.go:20-25)      */
+/* ------------------------------------------------------------------------ */
+/* Clamp (util.go:32-40): NaN compares false both ways and passes through */
+static double orc_clamp(double v, double lo, double hi) {
+    if (v < lo) return lo;
+    if (v > hi) return hi;
+    return v;
+}
+
+/* uint8(Clamp(math.Sqrt(c), 0, 1) * 255): Go truncates toward zero; a NaN gives 0 on
+ * amd64 and arm64 alike */
+static uint8_t orc_go_channel(double c) {
+    double v = orc_clamp(sqrt(c), 0.0, 1.0) * 255.0;
+    if (v != v) return 0;
+    return (uint8_t)(int)v;
+}
+
+void orc_to_image(const float *rgb, int32_t width, int32_t height, uint8_t *rgba) {
+    /* image.NewRGBA starts zeroed; img.Set outside the rectangle is a no-op */
+    memset(rgba, 0, (size_t)width * height * 4);
+    for (int64_t i = 0; i < (int64_t)width * height; i++) {
+        int64_t x = i % width;
+        int64_t y = height - i / width; /* buffer.go:65: row 0 maps to y = height, outside */
+        if (y < 0 || y >= height) continue;
+        uint8_t *px = rgba + 4 * (y * width + x);
+        px[0] = orc_go_channel((double)rgb[3 * i]);
+        px[1] = orc_go_channel((double)rgb[3 * i + 1]);
+        px[2] = orc_go_channel((double)rgb[3 * i + 2]);
+        px[3] = 255;
+    }
+}

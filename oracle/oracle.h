@@ -105,6 +105,9 @@ void orc_heatmap(const orc_bvh *b, const orc_camera_desc *cam, int32_t width, in
 
 /* ---- PHR ---- */
 /* stats: initial cut size, largest cut, nodes, leaves, BuildWithCost's build cost */
+/* buffer.go:60-69 / 104-116 ToImage over a buffer of width*height*3 colours (row y = 0
+ * first): rgba width*height*4 bytes, image row 0 first, Color.goColor (math.go:20-25). */
+void orc_to_image(const float *rgb, int32_t width, int32_t height, uint8_t *rgba);
 int orc_phr_build(const orc_bvh *aux, double alpha, double delta, int bf, orc_bvh **out, int64_t stats[5]);
 
 #ifdef __cplusplus

@@ -62,6 +62,7 @@ def lib():
         L.orc_adjoint.restype = C.c_int
         L.orc_adjoint.argtypes = [P, P, P, P, P, P, P, P, P]
         L.orc_heatmap.argtypes = [P, P, i32, i32, i32, C.c_int, P, P]
+        L.orc_to_image.argtypes = [P, i32, i32, P]
         L.orc_phr_build.restype = C.c_int
         L.orc_phr_build.argtypes = [P, d, d, C.c_int, C.POINTER(P), P]
         _lib = L
@@ -255,6 +256,15 @@ class BVH:
         b.stats = dict(initial_cut=int(stats[0]), max_cut=int(stats[1]), nodes=int(stats[2]), leaves=int(stats[3]),
                        build_cost=int(stats[4]))
         return b
+
+
+def to_image(rgb):
+    """ToImage (buffer.go:60-69) of a (height, width, 3) float32 buffer: (height, width, 4) uint8."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    h, w, _ = rgb.shape
+    out = np.empty((h, w, 4), np.uint8)
+    lib().orc_to_image(_p(rgb), w, h, _p(out))
+    return out
 
 
 def lbvh(verts, spheres=None, threads=os.cpu_count() or 1):

@@ -277,3 +277,42 @@ def test_render_reflective_and_refractive_exact(kind):
     a, le = np.asarray(s["mat_color"][0]), s["mat_color"][1][0]
     want = a * le if kind == "mirror" else a * a * le
     np.testing.assert_allclose(img.reshape(-1, 3), np.broadcast_to(want, (256, 3)), rtol=1e-9)
+
+
+def _to_image_py(rgb):
+    """buffer.go:60-69 with math.go:20-25, written out pixel by pixel: the row of buffer
+    index i is height - i // width (row 0 falls outside the image); each channel is
+    uint8(Clamp(sqrt(c), 0, 1) * 255) with Go's truncation (NaN -> 0)."""
+    import math
+
+    h, w, _ = rgb.shape
+    out = np.zeros((h, w, 4), np.uint8)
+    flat = rgb.reshape(-1, 3)
+    for i in range(w * h):
+        x, y = i % w, h - i // w
+        if not (0 <= y < h):
+            continue
+        px = []
+        for c in flat[i]:
+            s = math.sqrt(float(c)) if float(c) >= 0 else float("nan")
+            s = 0.0 if s < 0.0 else (1.0 if s > 1.0 else s)
+            v = s * 255.0
+            px.append(0 if v != v else int(v))
+        out[y, x] = px + [255]
+    return out
+
+
+def test_oracle_to_image_matches_python_restatement():
+    rng = np.random.default_rng(3)
+    h, w = 7, 5
+    rgb = rng.uniform(-0.2, 1.3, (h, w, 3)).astype(np.float32)
+    # exact squares of k/255 and their neighbours, where the truncation turns
+    k = np.arange(0, 256, dtype=np.float64) / 255.0
+    sq = (k * k).astype(np.float32)
+    edge = np.concatenate([sq, np.nextafter(sq, np.float32(-1)), np.nextafter(sq, np.float32(2)),
+                           np.array([np.nan, np.inf, -np.inf, -0.0, 0.0, 1.0, 4.0], np.float32)])
+    rgb2 = np.resize(edge, 16 * 17 * 3).reshape(16, 17, 3)
+    for img in (rgb, rgb2):
+        got = O.to_image(img)
+        assert np.array_equal(got, _to_image_py(img))
+        assert np.all(got[0] == 0)  # image row 0 is never written

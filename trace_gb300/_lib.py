@@ -29,6 +29,8 @@ EXPORTS = [
     "gbt_render_batch_async", "gbt_render_batch_plain_async", "gbt_batch_autotune", "gbt_batch_graph_create",
     "gbt_graph_launch", "gbt_graph_destroy",
     "gbt_adjoint_forward_async", "gbt_adjoint_backward_async", "gbt_l2_loss_async",
+    "gbt_buffer_create", "gbt_buffer_destroy", "gbt_render_to_buffer", "gbt_render_to_buffer_async",
+    "gbt_buffer_read", "gbt_buffer_to_image", "gbt_buffer_add_async",
 ]
 
 
@@ -132,6 +134,13 @@ def load():
         "gbt_adjoint_forward_async": ([P, P, P, P, P, P, P], C.c_int),
         "gbt_adjoint_backward_async": ([P, P, P, P, P, P, P, P, P], C.c_int),
         "gbt_l2_loss_async": ([P, P, P, u32, P, P], C.c_int),
+        "gbt_buffer_create": ([P, i32, i32, i32, PP], C.c_int),
+        "gbt_buffer_destroy": ([P], C.c_int),
+        "gbt_render_to_buffer": ([P, P, P, P, P, P], C.c_int),
+        "gbt_render_to_buffer_async": ([P, P, P, P, P], C.c_int),
+        "gbt_buffer_read": ([P, P, P, C.POINTER(C.c_uint64)], C.c_int),
+        "gbt_buffer_to_image": ([P, P, P], C.c_int),
+        "gbt_buffer_add_async": ([P, P, P, i32], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libgbtrace.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["api.cu", "lbvh.cu", "traverse.cu", "render.cu", "batch.cu", "adjoint.cu", "phr.cu", "collapse.cu", "heatmap.cu", "cost.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "buffer.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, "--expt-relaxed-constexpr"]
 

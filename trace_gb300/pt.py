@@ -520,11 +520,32 @@ def NewDefaultCamera(aspect, fov):
     return Camera(aspect, fov, CameraTransformation((0, 0, 0), (1, 0, 0), (0, 1, 0)))
 
 
-@dataclass
-class PixelBuffer:
-    width: int
-    height: int
-    data: np.ndarray = field(default=None, repr=False)
+class _Buffer:
+    """A device-resident render target (gbt_buffer).  The device side is created on the first
+    RenderToBuffer, on the BVH's context, unless a context is given here.  `data` is the
+    host copy of the colours (height, width, 3), row y = 0 first (buffer.go:47-49),
+    refreshed after every RenderToBuffer."""
+
+    KIND = 0
+
+    def __init__(self, width, height, ctx=None):
+        self.width, self.height = int(width), int(height)
+        self.data = np.zeros((self.height, self.width, 3), np.float32)
+        self.samples = 0
+        self.ctx = None
+        self.h = None
+        if ctx is not None:
+            self._bind(ctx)
+
+    def _bind(self, ctx):
+        if self.h is not None:
+            if ctx is not self.ctx:
+                raise GbtError(-1, "buffer belongs to another context")
+            return
+        h = C.c_void_p()
+        ctx.check(ctx.L.gbt_buffer_create(ctx.h, self.KIND, self.width, self.height, C.byref(h)), "buffer_create")
+        self.ctx, self.h = ctx, h
+        ctx._adopt(self)
 
     def Width(self):
         return self.width
@@ -532,13 +553,63 @@ class PixelBuffer:
     def Height(self):
         return self.height
 
+    def _render(self, bvh, cam, params):
+        self._bind(bvh.ctx)
+        st = _lib.RenderStats()
+        c = self.ctx
+        c.check(c.L.gbt_render_to_buffer(c.h, bvh.h, C.byref(cam), C.byref(params), self.h, C.byref(st)),
+                "render_to_buffer")
+        n = C.c_uint64()
+        c.check(c.L.gbt_buffer_read(c.h, self.h, _p(self.data), C.byref(n)), "buffer_read")
+        self.samples = int(n.value)
+        return st
 
-def NewPxlBuffer(width, height):
-    return PixelBuffer(width, height, np.zeros((height, width, 3), np.float32))
+    def ToImage(self):
+        """buffer.go:60-69 / 104-116: (height, width, 4) uint8 RGBA, image row 0 first."""
+        if self.h is None:
+            raise GbtError(-1, "ToImage: the buffer has no device side yet (give NewPxlBuffer a context or render "
+                               "into it first)")
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        self.ctx.check(self.ctx.L.gbt_buffer_to_image(self.ctx.h, self.h, _p(out)), "buffer_to_image")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            if self.ctx.alive:
+                self.ctx.L.gbt_buffer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
-def NewFrameBuffer(width, height):
-    return PixelBuffer(width, height, np.zeros((height, width, 3), np.float32))
+class PixelBuffer(_Buffer):
+    """buffer.go:28-58: each pixel is the running mean of every sample added, across calls."""
+    KIND = 0
+
+
+class FrameBuffer(_Buffer):
+    """buffer.go:71-116: each pixel holds the last sample written."""
+    KIND = 1
+
+
+def NewPxlBuffer(width, height, ctx=None):
+    return PixelBuffer(width, height, ctx)  # buffer.go:39-45
+
+
+def NewPxlBufferAR(height, aspect, ctx=None):
+    return PixelBuffer(int(float(height) * aspect), height, ctx)  # buffer.go:34-37
+
+
+def NewFrameBuffer(width, height, ctx=None):
+    return FrameBuffer(width, height, ctx)  # buffer.go:83-89
+
+
+def NewFrameBufferAR(height, aspect, ctx=None):
+    return FrameBuffer(int(float(height) * aspect), height, ctx)  # buffer.go:78-81
 
 
 @dataclass
@@ -554,12 +625,24 @@ class ImageRenderer:
     Verbose: bool = False
     last_stats: dict = None
 
-    def RenderToBuffer(self, buff: PixelBuffer):
-        img, st = self.Bvh.render(self.Camera.desc(), buff.width, buff.height, self.Spp, self.MaxDepth, self.Miss,
-                                  self.MissColor, self.Seed)
-        buff.data[...] = img
-        self.last_stats = st
+    def RenderToBuffer(self, buff):
+        """Adds Spp samples per pixel to buff (a PixelBuffer keeps the running mean of all of
+        them, a FrameBuffer the last one)."""
+        cam = make_camera(self.Camera.desc())
+        p = _lib.RenderParams(buff.width, buff.height, int(self.Spp), int(self.MaxDepth), int(self.Miss),
+                              (C.c_float * 3)(*self.MissColor), int(self.Seed))
+        st = buff._render(self.Bvh, cam, p)
+        self.last_stats = dict(rays_traced=st.rays_traced, paths=st.paths, ms=st.ms_total)
         return buff
+
+    def GetBvh(self):
+        return self.Bvh
+
+    def SetBvh(self, bvh):
+        self.Bvh = bvh
+
+    def GetCamera(self):
+        return self.Camera
 
 
 def NewDefaultRenderer(bvh, camera):
@@ -579,14 +662,25 @@ class HeatMapRenderer:
     Threshold: int
     last_counts: np.ndarray = field(default=None, repr=False)
 
-    def RenderToBuffer(self, buff: PixelBuffer):
+    def RenderToBuffer(self, buff):
+        """One sample per pixel added to buff (render.go:155-197 calls addSample once per pixel)."""
         ctx = self.Bvh.ctx
         cam = make_camera(self.Camera.desc() if isinstance(self.Camera, Camera) else self.Camera)
-        rgb = np.empty((buff.height, buff.width, 3), np.float32)
-        counts = np.empty((buff.height, buff.width), np.int32)
-        ctx.check(ctx.L.gbt_heatmap(ctx.h, self.Bvh.h, C.byref(cam), buff.width, buff.height, int(self.Threshold),
-                                    _p(rgb), _p(counts)), "heatmap")
-        buff.data[...] = rgb
+        w, h = buff.width, buff.height
+        counts = np.empty((h, w), np.int32)
+        buff._bind(ctx)
+        d_rgb, d_cnt = ctx.alloc(w * h * 3 * 4), ctx.alloc(w * h * 4)
+        try:
+            ctx.check(ctx.L.gbt_heatmap_async(ctx.h, self.Bvh.h, C.byref(cam), w, h, int(self.Threshold),
+                                              C.c_void_p(d_rgb), C.c_void_p(d_cnt)), "heatmap")
+            ctx.check(ctx.L.gbt_buffer_add_async(ctx.h, buff.h, C.c_void_p(d_rgb), 1), "buffer_add")
+            ctx.d2h(counts, d_cnt)
+            n = C.c_uint64()
+            ctx.check(ctx.L.gbt_buffer_read(ctx.h, buff.h, _p(buff.data), C.byref(n)), "buffer_read")
+            buff.samples = int(n.value)
+        finally:
+            ctx.free(d_rgb)
+            ctx.free(d_cnt)
         self.last_counts = counts
         return buff
 
