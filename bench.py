@@ -44,6 +44,10 @@ W, H, SPP, MAX_DEPTH = 1920, 1080, 1, 0
 N_TRI = 1_000_000
 PHR = (0.5, 6.0, 2)
 WORKLOAD = "soup1M_1920x1080_primary+1bounce_spp1"
+# the workload both arms time (the GPU arm and --impl reference print the same dict)
+CONFIG = {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP, "max_depth": MAX_DEPTH,
+          "miss": "white", "bvh": "phr(alpha=0.5,delta=6,bf=2)", "frame": "full 1920x1080 frame per step",
+          "l2": "GPU arm: flushed before every timed step (256 MiB write); CPU arm: no flush"}
 
 # Algorithmic bytes of one LBVH build per triangle, by kernel:
 #   bounds 36 (read vertices) + morton 44 (read 36, write 8-byte key)
@@ -158,8 +162,8 @@ class ClockSampler:
 
 def cpu_baseline(scene, seconds=8.0, threads=None):
     """The oracle's renderer (a C restatement of render.go:91-129) on a bounded
-    sample of the frame: 480x270 frames of the same view, repeated for about
-    `seconds`, all host threads."""
+    sample of the workload: full 1920x1080 frames of the same view, repeated
+    for about `seconds`, all host threads."""
     from oracle import oracle as O
 
     threads = threads or (os.cpu_count() or 1)
@@ -168,21 +172,23 @@ def cpu_baseline(scene, seconds=8.0, threads=None):
     ph = o.phr(*PHR)
     build_s = time.perf_counter() - t0
     rays, el, frames, seed = 0, 0.0, 0, 1
-    sw, sh = 480, 270
     while el < seconds or frames == 0:
         t = time.perf_counter()
-        ph.render(scene, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=seed, threads=threads)
+        ph.render(scene, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH, seed=seed, threads=threads)
         el += time.perf_counter() - t
         rays += ph.last_rays
         frames += 1
         seed += 1
     return {"value": rays / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": "%d frames of %dx%d (same camera, spp %d, MaxDepth %d) on the PHR tree; %d rays in %.2f s; "
-                      "CPU LBVH+PHR build %.2f s untimed" % (frames, sw, sh, SPP, MAX_DEPTH, rays, el, build_s)}
+            "sample": "%d full %dx%d frames (same camera, spp %d, MaxDepth %d) on the PHR tree; %d rays in %.2f s; "
+                      "CPU LBVH+PHR build %.2f s untimed" % (frames, W, H, SPP, MAX_DEPTH, rays, el, build_s)}
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the reference's CPU path on the host cores."""
+    """--impl reference: the reference's CPU path on the host cores, on the same
+    workload (full 1920x1080 frames of the PHR tree), every host thread.  The Go
+    reference cannot be built on this image, so its C restatement (oracle/)
+    stands in."""
     if rank != 0:
         return 0
     from oracle import oracle as O
@@ -193,24 +199,21 @@ def run_reference(args, ws, rank):
     threads = os.cpu_count() or 1
     o = O.lbvh(s["verts"], threads=threads)
     ph = o.phr(*PHR)
-    sw, sh = 480, 270
     for i in range(args.warmup):
-        ph.render(s, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=1000 + i, threads=threads)
+        ph.render(s, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH, seed=1000 + i, threads=threads)
     rays, el = 0, 0.0
     for i in range(args.steps):
         t = time.perf_counter()
-        ph.render(s, width=sw, height=sh, spp=SPP, max_depth=MAX_DEPTH, seed=1 + i, threads=threads)
+        ph.render(s, width=W, height=H, spp=SPP, max_depth=MAX_DEPTH, seed=1 + i, threads=threads)
         el += time.perf_counter() - t
         rays += ph.last_rays
     val = rays / el / 1e6
     line = {"impl": "reference", "metric": "Mrays/s", "value": val, "unit": "Mrays/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
-                       "max_depth": MAX_DEPTH, "bvh": "phr(alpha=0.5,delta=6,bf=2)",
-                       "step_sample": "%dx%d frame of the same view per step" % (sw, sh)},
+            "config": dict(CONFIG),
             "cpu_baseline": {"value": val, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": "%dx%d frame per step, %d steps, %d rays" % (sw, sh, args.steps, rays)},
+                             "sample": "one full %dx%d frame per step, %d steps, %d rays" % (W, H, args.steps, rays)},
             "e2e": {"value": val, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "C restatement of pkg/pt (oracle/); the Go reference cannot be built on this image"}
     print(json.dumps(line), flush=True)
@@ -218,6 +221,11 @@ def run_reference(args, ws, rank):
 
 
 def run_batch_workload(args):
+    print(json.dumps(measure_batch(args, rebuilds=True)), flush=True)
+    return 0
+
+
+def measure_batch(args, rebuilds=True):
     """64 scenes of log-uniform size in [1k, 2M] triangles (seed 3), each a soup or
     an fBm terrain patch, 512x512, 16 spp, depth 4: the per-scene wavefront loop
     (gbt_render_async per scene) against the batched frame over all scenes (the
@@ -279,6 +287,26 @@ def run_batch_workload(args):
     b.make_graph(rebuild=False, cfg=cfg)
     ms_graph, rays_graph = timed("graph", steps)
     b.close_graph()
+    diff = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, batched))
+    rmse = float(np.sqrt(np.mean([np.mean((x - y) ** 2) for x, y in zip(plain, batched)])))
+    line = {"metric": "Mrays/s (64-scene batch)", "unit": "Mrays/s", "workload": "batch%d_512x512_spp16_depth4" % count,
+            "triangles_total": tris, "scenes": count, "steps": steps,
+            "plain": {"value": rays_plain / ms_plain / 1e3, "ms_per_frame": ms_plain, "rays": rays_plain},
+            "batched": {"value": rays_batch / ms_batch / 1e3, "ms_per_frame": ms_batch, "rays": rays_batch,
+                        "config": {"mode": ["megakernel", "wavefront"][cfg.mode], "block": cfg.block,
+                                   "fetch_min": cfg.fetch_min, "stack": cfg.stack, "packets": cfg.packets},
+                        "autotune_best_ms": tune_ms},
+            "forms": forms,
+            "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},
+            "speedup_batched_vs_plain": (rays_batch / ms_batch) / (rays_plain / ms_plain),
+            "speedup_graph_vs_plain": (rays_graph / ms_graph) / (rays_plain / ms_plain),
+            "images": {"max_abs_diff_batched_vs_plain": diff, "rmse_batched_vs_plain": rmse,
+                       "note": "the same paths and random numbers: equal RMSE against any reference image"},
+            "scene_generation_s": gen_s}
+    if not rebuilds:
+        b.close()
+        ctx.close()
+        return line
     # frames that rebuild every LBVH first
     choices = [g.packets() for g in bvhs]
 
@@ -297,31 +325,22 @@ def run_batch_workload(args):
     ms_graph_rb, _ = timed("graph", steps)
     rebuilt = [b.read(i) for i in range(b.n)]
     diff_rb = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, rebuilt))
-    diff = max(float(np.max(np.abs(x - y))) for x, y in zip(plain, batched))
-    rmse = float(np.sqrt(np.mean([np.mean((x - y) ** 2) for x, y in zip(plain, batched)])))
-    line = {"metric": "Mrays/s (64-scene batch)", "unit": "Mrays/s", "workload": "batch%d_512x512_spp16_depth4" % count,
-            "triangles_total": tris, "scenes": count,
-            "plain": {"value": rays_plain / ms_plain / 1e3, "ms_per_frame": ms_plain, "rays": rays_plain},
-            "batched": {"value": rays_batch / ms_batch / 1e3, "ms_per_frame": ms_batch, "rays": rays_batch,
-                        "config": {"mode": ["megakernel", "wavefront"][cfg.mode], "block": cfg.block,
-                                   "fetch_min": cfg.fetch_min, "stack": cfg.stack, "packets": cfg.packets},
-                        "autotune_best_ms": tune_ms},
-            "forms": forms,
-            "graph": {"value": rays_graph / ms_graph / 1e3, "ms_per_frame": ms_graph},
-            "with_lbvh_rebuilds": {
-                "plain_ms_per_frame": ms_plain_rb, "graph_ms_per_frame": ms_graph_rb,
-                "plain_value": rays_plain / ms_plain_rb / 1e3, "graph_value": rays_plain / ms_graph_rb / 1e3,
-                "speedup_graph_vs_plain": ms_plain_rb / ms_graph_rb,
-                "max_abs_diff_graph_vs_plain": diff_rb},
-            "speedup_batched_vs_plain": (rays_batch / ms_batch) / (rays_plain / ms_plain),
-            "images": {"max_abs_diff_batched_vs_plain": diff, "rmse_batched_vs_plain": rmse},
-            "scene_generation_s": gen_s}
-    print(json.dumps(line), flush=True)
+    line["with_lbvh_rebuilds"] = {
+        "plain_ms_per_frame": ms_plain_rb, "graph_ms_per_frame": ms_graph_rb,
+        "plain_value": rays_plain / ms_plain_rb / 1e3, "graph_value": rays_plain / ms_graph_rb / 1e3,
+        "speedup_graph_vs_plain": ms_plain_rb / ms_graph_rb,
+        "max_abs_diff_graph_vs_plain": diff_rb}
     b.close()
-    return 0
+    ctx.close()
+    return line
 
 
 def run_adjoint_workload(args):
+    print(json.dumps(measure_adjoint(args)), flush=True)
+    return 0
+
+
+def measure_adjoint(args):
     """Cornell-box scene with a 256x128 sphere (65,036 triangles), per-triangle albedo and
     emission U[0.2, 0.8] (seed 4), target rendered from seed-5 parameters, 512x512,
     64 spp, depth 5: milliseconds per forward + L2 loss + backward iteration."""
@@ -365,10 +384,11 @@ def run_adjoint_workload(args):
     ms = e_0.elapsed_time(e_1) / steps
     line = {"metric": "adjoint ms/iter", "value": ms, "unit": "ms", "higher_is_better": False,
             "workload": "cornell_sphere256x128_512x512_spp64_depth5", "triangles": n,
-            "parameters": n * 4, "paths_per_pass": 512 * 512 * 64, "steps": steps}
-    print(json.dumps(line), flush=True)
+            "parameters": n * 4, "paths_per_pass": 512 * 512 * 64, "steps": steps,
+            "timed": "forward + L2 loss + backward, CUDA events on the library's stream"}
     f.close()
-    return 0
+    ctx.close()
+    return line
 
 
 def run_terrain_workload(args):
@@ -446,6 +466,44 @@ def run_terrain_workload(args):
             "scene_generation_s": gen_s}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def measure_terrain_lbvh(args):
+    """LBVH build throughput on the 2048x2048 fBm terrain (8,380,418 triangles plus its
+    sun sphere): W warm-up rebuilds, then K timed rebuilds (CUDA events on the library's
+    stream).  The scene (2.3 GB on the device) is far larger than L2, so nothing is
+    flushed.  Roofline: LBVH_BYTES_PER_TRI algorithmic bytes against the measured HBM
+    copy bandwidth; traffic is the DRAM bytes of one build from an ncu capture."""
+    import torch
+
+    from trace_gb300 import pt, scenes
+
+    ctx = pt.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    hbm, peak_kind = peaks()
+    s = scenes.terrain(2048)
+    ds = pt.DeviceScene.from_dict(ctx, s)
+    n = ds.n_prim
+    aux = pt.DefaultLBVH(ds)
+    for _ in range(max(1, args.warmup)):
+        ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
+    ctx.sync()
+    steps = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / steps
+    bw = n * LBVH_BYTES_PER_TRI / (ms * 1e-3) / 1e9
+    ctx.close()
+    return {"workload": "terrain2048_lbvh", "triangles": n, "ms": ms, "mtri_s": n / ms / 1e3, "steps": steps,
+            "roofline": {"bound": "hbm", "achieved": bw, "peak": hbm, "unit": "GB/s", "frac": bw / hbm,
+                         "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind,
+                         "traffic": LBVH_TRAFFIC_PER_TRI["terrain2048"] * n,
+                         "traffic_scope": "DRAM bytes of one build (18 launches), ncu cold-cache capture",
+                         "kernel": "whole build (18 launches)"}}
 
 
 def run_lbvh_workload(args):
@@ -538,6 +596,8 @@ def main():
     ap.add_argument("--layout", type=int, default=4, choices=[2, 4],
                     help="traversal layout: the 4-wide view collapsed from the binary tree, or the binary nodes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave out the batch, adjoint and terrain LBVH measurements of the default line")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--profile", choices=["render", "lbvh", "phr"], default=None,
                     help="run a small fixed case for an ncu capture and exit: 3 frames (render), 3 LBVH builds "
@@ -699,18 +759,19 @@ def main():
         phr_build["lbvh_plus_phr_mtri_s"] = N_TRI / (lb_ms + phr_build["ms"]) / 1e3
     lbvh = {"mtri_s": N_TRI / lb_ms / 1e3 * ws, "ms": lb_ms,
             "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
-                         "bytes_per_tri": LBVH_BYTES_PER_TRI, "traffic": None, "kernel": "whole build (15 launches)"}}
+                         "bytes_per_tri": LBVH_BYTES_PER_TRI,
+                         "traffic": LBVH_TRAFFIC_PER_TRI["soup1M"] * N_TRI if LBVH_TRAFFIC_PER_TRI["soup1M"] else None,
+                         "traffic_scope": "DRAM bytes of one build (18 launches), ncu cold-cache capture",
+                         "kernel": "whole build (18 launches)"}}
 
     line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles": N_TRI, "width": W, "height": H, "spp": SPP,
-                       "max_depth": MAX_DEPTH, "miss": "white", "bvh": bvh_name,
-                       "traversal_layout": "%d-wide" % args.layout,
-                       "camera_rays": "8x4 pixel tiles per warp", "past_max_depth": "any-hit query",
-                       "rays_per_step": timed["rays_traced"] / args.steps,
-                       "l2": "flushed before every timed step (256 MiB write)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": dict(CONFIG, bvh=bvh_name) if bvh_name != CONFIG["bvh"] else dict(CONFIG),
+            "execution": {"traversal_layout": "%d-wide" % args.layout,
+                          "camera_rays": "8x4 pixel tiles per warp", "past_max_depth": "any-hit query",
+                          "rays_per_step": timed["rays_traced"] / args.steps,
+                          "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof,
             "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s",
                     "h2d_bytes_per_step": C.sizeof(cam) + C.sizeof(rp), "d2h_bytes_per_step": W * H * 3 * 4,
@@ -719,14 +780,27 @@ def main():
             "clocks": clk,
             "lbvh": lbvh,
             "phr_build": phr_build}
+    ctx.free(d_img)
+    if ws == 1 and not args.no_extras:
+        # the metric's other parts, each on its own context after the headline's timed region:
+        # the 64-scene batch (batched vs the per-scene loop at equal RMSE), the adjoint's
+        # ms/iter and the terrain LBVH's Mtri/s
+        ctx.close()
+        line["batch"] = measure_batch(args, rebuilds=False)
+        line["adjoint"] = measure_adjoint(args)
+        line["terrain_lbvh"] = measure_terrain_lbvh(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, seconds=args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.free(d_img)
     dist.close()
     return 0
 
+
+# DRAM bytes per triangle of one LBVH build (dram__bytes_read.sum + dram__bytes_write.sum summed
+# over the build's 18 launches, one ncu capture of the second of three builds each):
+# terrain2048 3816.5 MB / 8,380,419 primitives; soup1M from its own capture.
+LBVH_TRAFFIC_PER_TRI = {"terrain2048": 3816.5e6 / 8380419, "soup1M": None}
 
 # DRAM bytes of one headline frame's two traversal launches on the PHR tree
 # (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full capture each:

@@ -102,8 +102,10 @@ int gbt_ctx_sync(gbt_ctx *ctx);
  * launch (ms_traverse); 2 also counts inner nodes and primitive tests (a
  * slower counting traversal).  No counterpart in the reference. */
 int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
-/* Execution options of later calls on this context.  None of them changes a
- * result: hits, images and gradients are identical under every setting.
+/* Execution options of later calls on this context.  None of options 0-6
+ * changes a result: hits, images and gradients are identical under every
+ * setting (a spin limit too low for the work fails the call instead).  The
+ * testing aids 7 and 8 make calls fail on purpose, with no fault.
  *   GBT_OPT_TRAVERSAL      0 persistent with dynamic ray fetch (default),
  *                          1 one thread per ray, 2 persistent without refills
  *   GBT_OPT_ANYHIT_LAST    1 (default): rays of the level past MaxDepth, whose
@@ -125,6 +127,19 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
  *                          at most this many nodes run with one-warp blocks in
  *                          batches of launches; a launch that meets a larger
  *                          cut is repeated with wider blocks
+ *   GBT_OPT_SPIN_LIMIT     1..4194304 (default 4194304): polls before a bounded
+ *                          device-side wait (the LBVH sort's look-back) gives
+ *                          up; the call then returns GBT_ETIMEOUT, the kernels
+ *                          after the wait do nothing, and the context stays
+ *                          usable
+ *   GBT_OPT_TEST_WITHHOLD_TILE  testing aid, -1 (default) off: the LBVH sort's
+ *                          tile of this index never publishes its digit counts
+ *                          in the first pass, so the tiles after it wait for a
+ *                          status nothing sets until GBT_OPT_SPIN_LIMIT runs out
+ *   GBT_OPT_TEST_COLLAPSE_CAP   testing aid, 0 (default) off: the work list of
+ *                          the 4-wide collapse holds at most this many nodes;
+ *                          children past it are dropped, never written, and
+ *                          the call returns GBT_EDEVICE ("work list full")
  * The environment variables GBT_TRAVERSAL (persistent|simple|ww),
  * GBT_ANYHIT_LAST, GBT_PRIMARY_TILES (0|1) and GBT_PRIMARY_PACKETS (0|1|2) set
  * the initial values.
@@ -135,6 +150,9 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
 #define GBT_OPT_PRIMARY_PACKETS 3
 #define GBT_OPT_KEEP_WORKSPACE 4
 #define GBT_OPT_PHR_SMALL_CUT 5
+#define GBT_OPT_SPIN_LIMIT 6
+#define GBT_OPT_TEST_WITHHOLD_TILE 7
+#define GBT_OPT_TEST_COLLAPSE_CAP 8
 int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */

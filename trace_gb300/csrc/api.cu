@@ -188,6 +188,19 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
             gbt_phr_release(ctx);
         }
         return GBT_OK;
+    case GBT_OPT_SPIN_LIMIT:
+        if (value < 1 || (uint32_t)value > GBT_SPIN_LIMIT)
+            return gbt_fail(ctx, GBT_EINVAL, "set_option: spin limit must be 1..4194304");
+        ctx->spin_limit = (uint32_t)value;
+        return GBT_OK;
+    case GBT_OPT_TEST_WITHHOLD_TILE:
+        if (value < -1) return gbt_fail(ctx, GBT_EINVAL, "set_option: tile must be >= -1");
+        ctx->withhold_tile = value < 0 ? 0xffffffffu : (uint32_t)value;
+        return GBT_OK;
+    case GBT_OPT_TEST_COLLAPSE_CAP:
+        if (value < 0) return gbt_fail(ctx, GBT_EINVAL, "set_option: capacity must be >= 0");
+        ctx->collapse_cap = (uint32_t)value;
+        return GBT_OK;
     default:
         return gbt_fail(ctx, GBT_EINVAL, "set_option: unknown option " + std::to_string(option));
     }

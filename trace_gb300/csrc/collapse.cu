@@ -196,6 +196,9 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
     const uint32_t cap = h.n_nodes + 1;  // a 4-wide tree never has more nodes than the binary one
     int rc0 = reserve4(ctx, bvh, cap);
     if (rc0) return rc0;
+    // the work-list capacity the kernels check against (a testing aid can lower it below what
+    // was allocated; children past it are dropped and reported, never written)
+    const uint32_t kcap = ctx->collapse_cap && ctx->collapse_cap < cap ? ctx->collapse_cap : cap;
     // queues (two halves), counters
     size_t qbytes = queue_bytes(cap);
     void *scr = nullptr;
@@ -211,7 +214,7 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
     for (;;) {
         for (int b = 0; b < COLLAPSE_BATCH; b++) {
             k_collapse_level_gs<<<(unsigned)ctx->num_sms * 4, 128, 0, st>>>(bvh->d_nodes, q0, q1, ctr, bvh->d_nodes4,
-                                                                            cap, ctx->d_error);
+                                                                            kcap, ctx->d_error);
             k_collapse_step<<<1, 1, 0, st>>>(ctr, ctx->d_error);
         }
         GBT_CUDA(ctx, cudaGetLastError());

@@ -71,6 +71,11 @@ struct gbt_ctx {
     // largest cut of a PHR level run with one-warp blocks (GBT_OPT_PHR_SMALL_CUT, 1..GBT_PHR_SMALL_CUT)
     int phr_small_cut = GBT_PHR_SMALL_CUT;
     void *h_pin = nullptr;  // small pinned host buffer for counter readbacks (gbt_pinned)
+    // bounded device waits (GBT_OPT_SPIN_LIMIT) and the testing aids that make them and the
+    // work-list checks trip (GBT_OPT_TEST_WITHHOLD_TILE, GBT_OPT_TEST_COLLAPSE_CAP)
+    uint32_t spin_limit = GBT_SPIN_LIMIT;
+    uint32_t withhold_tile = 0xffffffffu;
+    uint32_t collapse_cap = 0;
 };
 
 // A pinned host buffer of GBT_PINNED_BYTES owned by the context (allocated on first use).

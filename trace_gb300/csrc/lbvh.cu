@@ -371,11 +371,11 @@ __global__ void __launch_bounds__(256) k_sort_plan(SortPlan *plan, const uint32_
     }
 }
 
-__device__ __forceinline__ uint32_t lookback_wait(const uint32_t *p, unsigned int *err) {
+__device__ __forceinline__ uint32_t lookback_wait(const uint32_t *p, unsigned int *err, uint32_t limit) {
     for (uint32_t it = 0;; ++it) {
         uint32_t s = ld_relaxed(p);
         if (s & ST_FLAGS) return s;
-        if (it >= GBT_SPIN_LIMIT) {
+        if (it >= limit) {
             atomicOr(err, GBT_DEVERR_SPIN);
             return ST_PREFIX;  // give up: the result is wrong but the kernel ends; the host sees the flag
         }
@@ -383,13 +383,25 @@ __device__ __forceinline__ uint32_t lookback_wait(const uint32_t *p, unsigned in
     }
 }
 
+// True once a bounded wait of the sort has run out: the sorted order is then
+// unusable, and every later kernel of the build returns at once instead of
+// reading it.  The flag is only set by k_onesweep, so inside any later kernel
+// every thread reads the same value.
+__device__ __forceinline__ bool sort_failed(const unsigned int *err) {
+    return (*reinterpret_cast<const volatile unsigned int *>(err) & GBT_DEVERR_SPIN) != 0u;
+}
+
 // One pass: rank each key within its warp by digit (match_any + ballot
 // counts into warp-private shared histograms), publish the tile's digit
 // counts, look back over earlier tiles for the global offsets, stage the tile
-// in shared memory in digit order and write it out in runs.
+// in shared memory in digit order and write it out in runs.  Look-back waits
+// give up after spin_limit polls.  withhold_tile (a testing aid, 0xffffffff
+// when off) names a tile that never publishes its counts, so that the tiles
+// after it wait for a status nothing sets and the limit is reached.
 __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                               uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
-                                                              unsigned int *err) {
+                                                              unsigned int *err, uint32_t spin_limit,
+                                                              uint32_t withhold_tile) {
     if (!plan->active[pass]) return;
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *s_wh = reinterpret_cast<uint32_t *>(smem);  // [8][256]
@@ -400,10 +412,15 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + SORT_TILE);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_misc[16] = atomicAdd(&tile_ctr[pass], 1u);
+    if (tid == 0) {
+        s_misc[17] = sort_failed(err) ? 1u : 0u;  // an earlier pass or tile gave up: the input is unusable
+        s_misc[16] = atomicAdd(&tile_ctr[pass], 1u);
+    }
     for (int i = tid; i < 8 * 256; i += SORT_THREADS) s_wh[i] = 0;
     __syncthreads();
+    if (s_misc[17]) return;
     const uint32_t tile = s_misc[16];
+    const bool publish = tile != withhold_tile;
     const uint32_t shift = 8u * pass;
     const uint64_t *__restrict__ kin = plan->in_k[pass];
     const uint32_t *__restrict__ vin = plan->in_v[pass];
@@ -452,16 +469,16 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
             sum += c;
         }
         uint32_t *st = status + (size_t)tile * 256;
-        st_relaxed(&st[t], (tile == 0 ? ST_PREFIX : ST_AGG) | sum);
+        if (publish) st_relaxed(&st[t], (tile == 0 ? ST_PREFIX : ST_AGG) | sum);
         s_tstart[t] = block_excl_scan256(sum, s_misc, nullptr);
         uint32_t prefix = 0;
         if (tile > 0) {
             for (int j = (int)tile - 1; j >= 0; --j) {
-                uint32_t s = lookback_wait(&status[(size_t)j * 256 + t], err);
+                uint32_t s = lookback_wait(&status[(size_t)j * 256 + t], err, spin_limit);
                 prefix += s & ST_VALUE;
                 if ((s & ST_FLAGS) == ST_PREFIX) break;
             }
-            st_relaxed(&st[t], ST_PREFIX | (prefix + sum));
+            if (publish) st_relaxed(&st[t], ST_PREFIX | (prefix + sum));
         }
         s_gbase[t] = plan->digit_base[pass][t] + prefix;
     }
@@ -500,7 +517,8 @@ __device__ __forceinline__ bool run_start_at(const uint64_t *__restrict__ k, uin
 }
 
 __global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__restrict__ plan, uint32_t n,
-                                                           uint32_t *__restrict__ tile_cnt) {
+                                                           uint32_t *__restrict__ tile_cnt, const unsigned int *err) {
+    if (sort_failed(err)) return;
     const uint64_t *k = plan->final_k;
     uint32_t base = blockIdx.x * RLE_TILE, c = 0;
 #pragma unroll
@@ -516,7 +534,9 @@ __global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__res
     }
 }
 
-__global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t n_tiles, BvhHeader *hdr) {
+__global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t n_tiles, BvhHeader *hdr,
+                                                   const unsigned int *err) {
+    if (sort_failed(err)) return;
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
     if (threadIdx.x == 0) s_carry = 0;
@@ -550,7 +570,9 @@ __global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t 
 
 __global__ void __launch_bounds__(RLE_THREADS) k_rle_write(const SortPlan *__restrict__ plan, uint32_t n,
                                                            const uint32_t *__restrict__ tile_off,
-                                                           uint32_t *__restrict__ run, uint64_t *__restrict__ ukey) {
+                                                           uint32_t *__restrict__ run, uint64_t *__restrict__ ukey,
+                                                           const unsigned int *err) {
+    if (sort_failed(err)) return;
     const uint64_t *k = plan->final_k;
     __shared__ uint32_t s_w[8];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -584,7 +606,8 @@ __global__ void __launch_bounds__(RLE_THREADS) k_rle_write(const SortPlan *__res
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_gather(const SortPlan *__restrict__ plan, const float *__restrict__ verts,
                                                 const float4 *__restrict__ sph, uint32_t n_tri, uint32_t n,
-                                                float4 *__restrict__ recs) {
+                                                float4 *__restrict__ recs, const unsigned int *err) {
+    if (sort_failed(err)) return;
     const uint32_t *idx = plan->final_v;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         uint32_t o = idx[s];
@@ -687,6 +710,7 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
                                                        uint32_t *subtree, int32_t *parent_of, uint2 *range,
                                                        uint32_t n, EmitState *top, uint32_t *top_n, uint32_t top_cap,
                                                        unsigned int *err) {
+    if (sort_failed(err)) return;
     constexpr int B = EMIT_THREADS, NW = B / 32;
     // s_d[i]: common prefix length at the split k0-1+i | k0+i (i = 0..B), -1 past
     // either end of the codes.  s_loc[t]: inner node k0+t has its whole range in
@@ -824,7 +848,8 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
 __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t *__restrict__ ukey, float4 *nodes,
                                                   int32_t *other, uint32_t *subtree, int32_t *parent_of,
                                                   uint2 *range, const EmitState *__restrict__ top,
-                                                  const uint32_t *top_n, uint32_t top_cap) {
+                                                  const uint32_t *top_n, uint32_t top_cap, const unsigned int *err) {
+    if (sort_failed(err)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= min(*top_n, top_cap)) return;
     const uint32_t U = hdr->n_unique;
@@ -900,7 +925,8 @@ static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &s
     GBT_CUDA(ctx, cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     for (int p = 0; p < 8; p++)
         k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr,
-                                                            ctx->d_error);
+                                                            ctx->d_error, ctx->spin_limit,
+                                                            p == 0 ? ctx->withhold_tile : 0xffffffffu);
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }
@@ -931,10 +957,10 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     const SortPlan *plan = reinterpret_cast<const SortPlan *>(sb + ss.plan);
     uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
     uint32_t *tcnt = reinterpret_cast<uint32_t *>(sb + rle_off);
-    k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt);
-    k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr);
-    k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey);
-    k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims);
+    k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, ctx->d_error);
+    k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr, ctx->d_error);
+    k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey, ctx->d_error);
+    k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims, ctx->d_error);
     uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
     EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
     const uint32_t eb = emit_blocks(n);
@@ -944,7 +970,7 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
                                         bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n, top, top_n, eb,
                                         ctx->d_error);
     k_emit_top<<<(eb + 127) / 128, 128, 0, st>>>(bvh->d_hdr, bvh->d_ukey, bvh->d_nodes, bvh->d_other, bvh->d_size,
-                                                 bvh->d_parent, bvh->d_range, top, top_n, eb);
+                                                 bvh->d_parent, bvh->d_range, top, top_n, eb, ctx->d_error);
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }
@@ -1008,6 +1034,7 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
     if (cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return GBT_ECUDA;
     for (int p = 0; p < 8; p++)
-        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr, err);
+        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr, err,
+                                                            GBT_SPIN_LIMIT, 0xffffffffu);
     return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_ECUDA;
 }
