@@ -33,10 +33,12 @@ __device__ __forceinline__ float area(const Child &c) {
 }
 
 // A queued binary node becomes the 4-wide node already assigned to it; its
-// inner children are queued for the next level.
+// inner children are queued for the next level.  A queue slot whose child was
+// dropped for lack of capacity holds (-1, -1) and is skipped.
 __device__ void collapse_one(const float4 *__restrict__ bin, int2 e, int2 *__restrict__ q_out, uint32_t *n_out,
                              uint32_t *n_nodes4, float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
     // e = (binary node, 4-wide node)
+    if (e.x < 0 || e.y < 0 || (uint32_t)e.y >= cap) return;
     Child c[4];
     load_slots(bin, e.x, c[0], c[1]);
     int nc = 0;
@@ -74,6 +76,7 @@ __device__ void collapse_one(const float4 *__restrict__ bin, int2 e, int2 *__res
                 uint32_t q = atomicAdd(n_out, 1u);
                 if (idx >= cap || q >= cap) {
                     atomicOr(err, GBT_DEVERR_CAPACITY);
+                    if (q < cap) q_out[q] = make_int2(-1, -1);
                     cnt[k] = -1;
                     continue;
                 }
@@ -106,7 +109,7 @@ constexpr int COLLAPSE_BATCH = 8;      // levels launched per readback (gbt_coll
 __global__ void k_collapse_level_gs(const float4 *__restrict__ bin, int2 *q0, int2 *q1, uint32_t *ctr,
                                     float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
     const uint32_t par = ctr[3];
-    const uint32_t n = ctr[par];
+    const uint32_t n = min(ctr[par], cap);  // a full queue counted past its capacity (reported)
     const int2 *q_in = par ? q1 : q0;
     int2 *q_out = par ? q0 : q1;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
