@@ -1,17 +1,44 @@
 """Comparison helpers shared by the parity tests."""
 import numpy as np
 
+EPS32 = 2.0 ** -24  # unit roundoff of float32
+COND_C = 4.0        # rounding steps allowed in the bound of a float32 barycentric coordinate
 
-def classify_disagreements(orc_bvh, rays, gpu_prim, gpu_t, orc_prim, orc_t, rel_tie=1e-5, edge=1e-4):
+
+def mt_float32_margin_bound(verts, prim, ray):
+    """Bound on the float32 rounding error of Moeller-Trumbore's u and v (primitive.go:172-208)
+    for one triangle and ray, from float64: u = (tv . pv) / det and v = (d . qv) / det lose
+    about EPS32 * (|tv| |pv|) / |det| and EPS32 * (|d| |qv|) / |det|, which is large when the
+    ray grazes the triangle's plane (|det| near the reference's 1e-7 cut-off)."""
+    v = np.asarray(verts[prim], np.float64).reshape(3, 3)
+    o = np.asarray(ray[0:3], np.float64)
+    d = np.asarray(ray[4:7], np.float64)
+    e1, e2 = v[1] - v[0], v[2] - v[0]
+    pv = np.cross(d, e2)
+    det = float(np.dot(e1, pv))
+    if det == 0.0:
+        return np.inf
+    tv = o - v[0]
+    qv = np.cross(tv, e1)
+    cu = np.linalg.norm(tv) * np.linalg.norm(pv) / abs(det)
+    cv = np.linalg.norm(d) * np.linalg.norm(qv) / abs(det)
+    return COND_C * EPS32 * max(cu, cv, 1.0)
+
+
+def classify_disagreements(orc_bvh, rays, gpu_prim, gpu_t, orc_prim, orc_t, rel_tie=1e-5, edge=1e-4, verts=None):
     """Split hit-ID disagreements into near-ties and hard mismatches.
 
     near-tie: both primitives are hit in float64 at distances within rel_tie
     (an equal-distance tie whose winner depends on traversal order), or the
     primitive one side reports lies within `edge` of a barycentric or
-    distance boundary in float64 (float32 rounding decides it).
+    distance boundary in float64 (float32 rounding decides it).  With `verts`
+    (the scene's triangles), the barycentric margin is also compared with the
+    float32 rounding bound of that triangle and ray (mt_float32_margin_bound),
+    which covers grazing rays whose float32 u, v are off by more than `edge`.
     """
     bad = np.nonzero(gpu_prim != orc_prim)[0]
     near, hard = [], []
+    n_tri = None if verts is None else len(verts)
     for i in bad:
         r = rays[i]
         gp, op = int(gpu_prim[i]), int(orc_prim[i])
@@ -26,6 +53,8 @@ def classify_disagreements(orc_bvh, rays, gpu_prim, gpu_t, orc_prim, orc_t, rel_
             ok, t, u, v, det = orc_bvh.prim_intersect(p, r)
             margin = min(abs(u), abs(1 - u), abs(v), abs(1 - u - v))
             if margin <= edge or abs(abs(det) - 1e-7) <= 1e-7 * 0.5 or abs(t - r[3]) <= edge * max(1.0, abs(t)):
+                tie = True
+            elif n_tri is not None and p < n_tri and margin <= mt_float32_margin_bound(verts, p, r):
                 tie = True
             if p == gp and op >= 0 and not ok:
                 # the GPU's primitive is not hit in float64 but the closest is: compare distances

@@ -92,11 +92,15 @@ def test_terrain_full_grid_choice_equals_oracle(terrain_full):
     ph.close()
 
 
-def _check_hits(g, o, rays, label):
+def _check_hits(g, o, rays, label, verts):
+    """Closest hits against the float64 oracle.  Disagreements are near-ties when float32
+    rounding decides them: equal distances, or a barycentric margin within the float32
+    rounding bound of Moeller-Trumbore for that triangle and ray (grazing rays, whose
+    determinant is near the reference's absolute 1e-7 cut-off, lose the most)."""
     gp, gt, _, _ = g.trace(rays)
     op, ot, _, _ = o.trace(rays)
     agree = (gp == op).mean()
-    near, hard = classify_disagreements(o, rays, gp, gt, op, ot)
+    near, hard = classify_disagreements(o, rays, gp, gt, op, ot, verts=verts)
     both = (gp == op) & (op >= 0)
     rel = np.abs(gt[both] - ot[both]) / np.maximum(np.abs(ot[both]), 1e-30)
     print("%s: rays=%d hit=%.4f agree=%.6f near_ties=%d (%.2e of rays) hard=%d t_rel_max=%.2e" % (
@@ -104,6 +108,7 @@ def _check_hits(g, o, rays, label):
         rel.max() if rel.size else 0.0))
     assert len(hard) == 0, "hard hit-ID mismatches at rays %s" % hard[:10]
     assert agree >= 0.9999
+    assert len(near) <= 1e-4 * len(rays)
     assert (rel <= T_REL).mean() >= 0.9999
     return gp, gt
 
@@ -115,9 +120,9 @@ def test_soup_full_frame_hit_ids_on_phr(ctx):
     o = O.lbvh(s["verts"]).phr(0.5, 6.0, 2)
     rays = scenes.camera_rays(s["camera"], 1920, 1080, jitter_seed=6)
     assert rays.shape[0] == 1920 * 1080
-    gp, gt = _check_hits(g, o, rays, "soup1M PHR camera 1920x1080")
+    gp, gt = _check_hits(g, o, rays, "soup1M PHR camera 1920x1080", s["verts"])
     b = bounce_rays(s["verts"], rays, gp, gt, seed=10)
-    _check_hits(g, o, b, "soup1M PHR bounce")
+    _check_hits(g, o, b, "soup1M PHR bounce", s["verts"])
 
 
 def test_cornell_full_render(ctx):

@@ -129,6 +129,7 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->rstate) cudaFree(ctx->rstate);
+    if (ctx->sort_arena) cudaFree(ctx->sort_arena);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_out) cudaFree(ctx->d_out);
@@ -196,6 +197,10 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
     case GBT_OPT_TEST_WITHHOLD_TILE:
         if (value < -1) return gbt_fail(ctx, GBT_EINVAL, "set_option: tile must be >= -1");
         ctx->withhold_tile = value < 0 ? 0xffffffffu : (uint32_t)value;
+        return GBT_OK;
+    case GBT_OPT_SORT_BOUNCE:
+        if (value < 0 || value > 7) return gbt_fail(ctx, GBT_EINVAL, "set_option: Morton bits per axis must be 0..7");
+        ctx->sort_bounce = value;
         return GBT_OK;
     case GBT_OPT_TEST_COLLAPSE_CAP:
         if (value < 0) return gbt_fail(ctx, GBT_EINVAL, "set_option: capacity must be >= 0");

@@ -1038,3 +1038,25 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
                                                             GBT_SPIN_LIMIT, 0xffffffffu);
     return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_ECUDA;
 }
+
+// ---------------------------------------------------------------------------
+// (key, position) sort for other parts of the library (the renderer's ray order)
+// ---------------------------------------------------------------------------
+size_t gbt_key_sort_bytes(uint32_t max_n) {
+    SortScratch ss = sort_layout(max_n, 0);
+    return gbt_align(ss.total + (size_t)max_n * (sizeof(uint32_t) + sizeof(uint64_t) + sizeof(uint32_t)) + 256);
+}
+
+int gbt_key_sort_enqueue(gbt_ctx *ctx, void *arena, uint32_t max_n, uint64_t *keys, uint32_t n,
+                         uint32_t *const **sorted) {
+    if (n > max_n) return gbt_fail(ctx, GBT_EINVAL, "key sort: more keys than the arena holds");
+    unsigned char *sb = static_cast<unsigned char *>(arena);
+    SortScratch ss = sort_layout(n, 0), smax = sort_layout(max_n, 0);
+    uint32_t *vA = reinterpret_cast<uint32_t *>(sb + smax.total);
+    uint64_t *kB = reinterpret_cast<uint64_t *>(sb + gbt_align(smax.total + (size_t)max_n * sizeof(uint32_t)));
+    uint32_t *vB = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(kB) + (size_t)max_n * sizeof(uint64_t));
+    int rc = sort_enqueue(ctx, sb, ss, keys, vA, kB, vB, n, 1, nullptr);
+    if (rc) return rc;
+    *sorted = &reinterpret_cast<SortPlan *>(sb + ss.plan)->final_v;
+    return GBT_OK;
+}
