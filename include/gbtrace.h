@@ -153,7 +153,6 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
 #define GBT_OPT_SPIN_LIMIT 6
 #define GBT_OPT_TEST_WITHHOLD_TILE 7
 #define GBT_OPT_TEST_COLLAPSE_CAP 8
-#define GBT_OPT_SORT_BOUNCE 9
 int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- scene (pkg/pt/scene.go:7-150 Scene/Mesh collected into flat arrays) */

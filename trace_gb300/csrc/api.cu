@@ -119,6 +119,7 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
     if (const char *t = std::getenv("GBT_ANYHIT_LAST")) c->anyhit_last = std::strcmp(t, "0") != 0;
     if (const char *t = std::getenv("GBT_PRIMARY_TILES")) c->primary_tiles = std::strcmp(t, "0") != 0;
     if (const char *t = std::getenv("GBT_PRIMARY_PACKETS")) c->primary_packets = std::atoi(t) < 0 ? 0 : std::atoi(t) > 2 ? 2 : std::atoi(t);
+    if (const char *t = std::getenv("GBT_SORT_THREADS")) c->sort_threads = std::atoi(t) == 512 ? 512 : 256;
     *out = c;
     return GBT_OK;
 }
@@ -129,7 +130,6 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->rstate) cudaFree(ctx->rstate);
-    if (ctx->sort_arena) cudaFree(ctx->sort_arena);
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_out) cudaFree(ctx->d_out);
@@ -197,10 +197,6 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
     case GBT_OPT_TEST_WITHHOLD_TILE:
         if (value < -1) return gbt_fail(ctx, GBT_EINVAL, "set_option: tile must be >= -1");
         ctx->withhold_tile = value < 0 ? 0xffffffffu : (uint32_t)value;
-        return GBT_OK;
-    case GBT_OPT_SORT_BOUNCE:
-        if (value < 0 || value > 7) return gbt_fail(ctx, GBT_EINVAL, "set_option: Morton bits per axis must be 0..7");
-        ctx->sort_bounce = value;
         return GBT_OK;
     case GBT_OPT_TEST_COLLAPSE_CAP:
         if (value < 0) return gbt_fail(ctx, GBT_EINVAL, "set_option: capacity must be >= 0");

@@ -74,10 +74,8 @@ struct gbt_ctx {
     // bounded device waits (GBT_OPT_SPIN_LIMIT) and the testing aids that make them and the
     // work-list checks trip (GBT_OPT_TEST_WITHHOLD_TILE, GBT_OPT_TEST_COLLAPSE_CAP)
     uint32_t spin_limit = GBT_SPIN_LIMIT;
-    // rays after a bounce traced in (octant, origin Morton cell) order: Morton bits per axis, 0 off
-    int sort_bounce = 0;
-    void *sort_arena = nullptr;
-    size_t sort_arena_bytes = 0;
+    // threads per tile of the LBVH sort's passes: 256 (16 keys each) or 512 (8 keys each)
+    int sort_threads = 256;
     uint32_t withhold_tile = 0xffffffffu;
     uint32_t collapse_cap = 0;
 };
@@ -180,21 +178,12 @@ static inline size_t gbt_align(size_t x, size_t a = 256) { return (x + a - 1) / 
 // lbvh.cu
 int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh);
 size_t gbt_lbvh_scratch_bytes(uint32_t n);
-// Stable ascending sort of n 64-bit keys with their positions 0..n-1 as values, in an arena of
-// gbt_key_sort_bytes(max_n) bytes; the keys array is overwritten.  *sorted receives the device
-// address where the sort leaves the pointer to the sorted positions (which of two buffers holds
-// them is decided on the device, by the passes whose digit is not the same for every key).
-size_t gbt_key_sort_bytes(uint32_t max_n);
-int gbt_key_sort_enqueue(gbt_ctx *ctx, void *arena, uint32_t max_n, uint64_t *keys, uint32_t n,
-                         uint32_t *const **sorted);
+
 // traverse.cu
 int gbt_trace_enqueue(gbt_ctx *ctx, const gbt_bvh *bvh, const gbt_ray *d_rays, uint32_t n, gbt_hit *d_hits);
-// order_pp (optional): the device address of a pointer to positions 0..n-1 in the order the
-// rays are to be traced (see gbt_key_sort_enqueue); hits still land at each ray's position.
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n,
                          const uint32_t *d_count, int out_mode, unsigned int *d_error, cudaStream_t s,
-                         unsigned long long *d_counters = nullptr, bool any = false,
-                         const uint32_t *const *order_pp = nullptr);
+                         unsigned long long *d_counters = nullptr, bool any = false);
 // One tree of a batched frame as the multi-tree traversal reads it: a ray's
 // tree is the index in .w of its second path record (aux[2 i + 1].w).
 struct TreeRef {

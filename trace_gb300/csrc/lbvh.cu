@@ -17,14 +17,9 @@
 
 namespace {
 
-constexpr int SORT_THREADS = 256;
-// Keys per thread of a sort tile; the register budget allows 2 * 16 / SORT_ITEMS
-// resident blocks per SM.
-#ifndef GBT_SORT_ITEMS
-#define GBT_SORT_ITEMS 16
-#endif
-constexpr int SORT_ITEMS = GBT_SORT_ITEMS;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+// Keys per sort tile: 256 threads of 16 keys or 512 threads of 8 (the context's
+// sort_threads); tiles of 2048 and 1024 keys were measured slower.
+constexpr int SORT_TILE = 4096;
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_PREFIX = 2u << 30;
 constexpr uint32_t ST_FLAGS = 3u << 30;
@@ -305,6 +300,7 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys,
 }
 
 // Exclusive scan of 256 values held one per thread (blockDim == 256).
+// Threads past the first 256 of a larger block take part in the barriers only.
 __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_tmp /*8*/, uint32_t *total) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t x = v;
@@ -313,7 +309,7 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_t
         uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) s_tmp[w] = x;
+    if (lane == 31 && w < 8) s_tmp[w] = x;
     __syncthreads();
     uint32_t off = 0, tot = 0;
 #pragma unroll
@@ -398,14 +394,18 @@ __device__ __forceinline__ bool sort_failed(const unsigned int *err) {
 // give up after spin_limit polls.  withhold_tile (a testing aid, 0xffffffff
 // when off) names a tile that never publishes its counts, so that the tiles
 // after it wait for a status nothing sets and the limit is reached.
-__global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
-                                                              uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
-                                                              unsigned int *err, uint32_t spin_limit,
-                                                              uint32_t withhold_tile) {
+// T threads of I keys each (T * I = SORT_TILE); the register budget is sized for two
+// resident blocks per SM.  Digit-wise steps take one thread per digit (the first 256).
+template <int T, int I>
+__global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
+                                                 uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
+                                                 unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
+    static_assert(T * I == SORT_TILE && T >= 256 && T % 32 == 0, "tile shape");
+    constexpr int NW = T / 32;
     if (!plan->active[pass]) return;
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *s_wh = reinterpret_cast<uint32_t *>(smem);  // [8][256]
-    uint32_t *s_tstart = s_wh + 8 * 256;                    // [256]
+    uint32_t *s_wh = reinterpret_cast<uint32_t *>(smem);  // [NW][256]
+    uint32_t *s_tstart = s_wh + NW * 256;                   // [256]
     uint32_t *s_gbase = s_tstart + 256;                      // [256]
     uint32_t *s_misc = s_gbase + 256;                        // [32]
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(s_misc + 32);
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
         s_misc[17] = sort_failed(err) ? 1u : 0u;  // an earlier pass or tile gave up: the input is unusable
         s_misc[16] = atomicAdd(&tile_ctr[pass], 1u);
     }
-    for (int i = tid; i < 8 * 256; i += SORT_THREADS) s_wh[i] = 0;
+    for (int i = tid; i < NW * 256; i += T) s_wh[i] = 0;
     __syncthreads();
     if (s_misc[17]) return;
     const uint32_t tile = s_misc[16];
@@ -425,13 +425,13 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     const uint64_t *__restrict__ kin = plan->in_k[pass];
     const uint32_t *__restrict__ vin = plan->in_v[pass];
     const bool ident = plan->identity[pass] != 0;
-    const uint32_t wbase = tile * SORT_TILE + warp * 32 * SORT_ITEMS;
+    const uint32_t wbase = tile * SORT_TILE + warp * 32 * I;
 
-    uint64_t k[SORT_ITEMS];
-    uint32_t v[SORT_ITEMS];
-    uint32_t rk[SORT_ITEMS];
+    uint64_t k[I];
+    uint32_t v[I];
+    uint32_t rk[I];
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; i++) {
+    for (int i = 0; i < I; i++) {
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
         k[i] = ok ? __ldcs(kin + idx) : 0ull;
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     uint32_t *wh = s_wh + warp * 256;
     const uint32_t lt = lanemask_lt();
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; i++) {
+    for (int i = 0; i < I; i++) {
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
         uint32_t d = ok ? (uint32_t)((k[i] >> shift) & 255u) : 256u;
@@ -459,18 +459,21 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     }
     __syncthreads();
 
-    {
-        const uint32_t t = tid;  // one thread per digit
-        uint32_t sum = 0;
+    const uint32_t t = (uint32_t)tid;  // one thread per digit (t < 256)
+    uint32_t sum = 0;
+    uint32_t *st = status + (size_t)tile * 256;
+    if (t < 256) {
 #pragma unroll
-        for (int w = 0; w < 8; w++) {
+        for (int w = 0; w < NW; w++) {
             uint32_t c = s_wh[w * 256 + t];
             s_wh[w * 256 + t] = sum;
             sum += c;
         }
-        uint32_t *st = status + (size_t)tile * 256;
         if (publish) st_relaxed(&st[t], (tile == 0 ? ST_PREFIX : ST_AGG) | sum);
-        s_tstart[t] = block_excl_scan256(sum, s_misc, nullptr);
+    }
+    const uint32_t tstart = block_excl_scan256(sum, s_misc, nullptr);  // every thread takes part
+    if (t < 256) {
+        s_tstart[t] = tstart;
         uint32_t prefix = 0;
         if (tile > 0) {
             for (int j = (int)tile - 1; j >= 0; --j) {
@@ -484,7 +487,7 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; i++) {
+    for (int i = 0; i < I; i++) {
         uint32_t idx = wbase + i * 32 + lane;
         if (idx < n) {
             uint32_t d = (uint32_t)((k[i] >> shift) & 255u);
@@ -498,13 +501,37 @@ __global__ void __launch_bounds__(SORT_THREADS, 32 / SORT_ITEMS) k_onesweep(cons
     uint32_t *__restrict__ vout = plan->out_v[pass];
     const uint32_t tile0 = tile * SORT_TILE;
     const uint32_t valid = (n - tile0) < (uint32_t)SORT_TILE ? (n - tile0) : (uint32_t)SORT_TILE;
-    for (uint32_t j = tid; j < valid; j += SORT_THREADS) {
+    for (uint32_t j = tid; j < valid; j += T) {
         uint64_t kk = s_keys[j];
         uint32_t d = (uint32_t)((kk >> shift) & 255u);
         uint32_t g = s_gbase[d] + (j - s_tstart[d]);
         kout[g] = kk;
         vout[g] = s_vals[j];
     }
+}
+
+// Launches the eight passes (a pass whose plan entry is inactive returns at once).
+static cudaError_t onesweep_passes(int threads, const SortPlan *plan, uint32_t n, uint32_t n_tiles, uint32_t *status,
+                                   uint32_t *ctr, unsigned int *err, uint32_t spin_limit, uint32_t withhold0,
+                                   cudaStream_t st) {
+    const int nw = threads / 32;
+    const size_t smem = (size_t)(nw * 256 + 256 + 256 + 32) * sizeof(uint32_t) +
+                        (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+    cudaError_t e;
+    if (threads == 512) e = cudaFuncSetAttribute(k_onesweep<512, SORT_TILE / 512>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    else e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem);
+    if (e != cudaSuccess) return e;
+    for (int p = 0; p < 8; p++) {
+        uint32_t *sp = status + (size_t)p * n_tiles * 256;
+        const uint32_t wh = p == 0 ? withhold0 : 0xffffffffu;
+        if (threads == 512)
+            k_onesweep<512, SORT_TILE / 512><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+        else
+            k_onesweep<256, SORT_TILE / 256><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+    }
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -921,13 +948,8 @@ static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &s
     int hb = ctx->num_sms * 2;
     k_hist<<<hb, 256, 0, st>>>(kA, n, hist);
     k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
-    size_t smem = (8 * 256 + 256 + 256 + 32) * sizeof(uint32_t) + (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
-    GBT_CUDA(ctx, cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    for (int p = 0; p < 8; p++)
-        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr,
-                                                            ctx->d_error, ctx->spin_limit,
-                                                            p == 0 ? ctx->withhold_tile : 0xffffffffu);
-    GBT_CUDA(ctx, cudaGetLastError());
+    GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
+                                  ctx->withhold_tile, st));
     return GBT_OK;
 }
 
@@ -1030,33 +1052,7 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
     if (cudaMemsetAsync(err, 0, sizeof(unsigned int), st) != cudaSuccess) return GBT_ECUDA;
     k_hist<<<num_sms * 2, 256, 0, st>>>(codes_in, n, hist);
     k_sort_plan_all<<<1, 256, 0, st>>>(plan, hist, codes_in, codes_out, idx_out, kB, vB);
-    size_t smem = (8 * 256 + 256 + 256 + 32) * sizeof(uint32_t) + (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
-    if (cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return GBT_ECUDA;
-    for (int p = 0; p < 8; p++)
-        k_onesweep<<<ss.n_tiles, SORT_THREADS, smem, st>>>(plan, p, n, status + (size_t)p * ss.n_tiles * 256, ctr, err,
-                                                            GBT_SPIN_LIMIT, 0xffffffffu);
-    return cudaGetLastError() == cudaSuccess ? GBT_OK : GBT_ECUDA;
-}
-
-// ---------------------------------------------------------------------------
-// (key, position) sort for other parts of the library (the renderer's ray order)
-// ---------------------------------------------------------------------------
-size_t gbt_key_sort_bytes(uint32_t max_n) {
-    SortScratch ss = sort_layout(max_n, 0);
-    return gbt_align(ss.total + (size_t)max_n * (sizeof(uint32_t) + sizeof(uint64_t) + sizeof(uint32_t)) + 256);
-}
-
-int gbt_key_sort_enqueue(gbt_ctx *ctx, void *arena, uint32_t max_n, uint64_t *keys, uint32_t n,
-                         uint32_t *const **sorted) {
-    if (n > max_n) return gbt_fail(ctx, GBT_EINVAL, "key sort: more keys than the arena holds");
-    unsigned char *sb = static_cast<unsigned char *>(arena);
-    SortScratch ss = sort_layout(n, 0), smax = sort_layout(max_n, 0);
-    uint32_t *vA = reinterpret_cast<uint32_t *>(sb + smax.total);
-    uint64_t *kB = reinterpret_cast<uint64_t *>(sb + gbt_align(smax.total + (size_t)max_n * sizeof(uint32_t)));
-    uint32_t *vB = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(kB) + (size_t)max_n * sizeof(uint64_t));
-    int rc = sort_enqueue(ctx, sb, ss, keys, vA, kB, vB, n, 1, nullptr);
-    if (rc) return rc;
-    *sorted = &reinterpret_cast<SortPlan *>(sb + ss.plan)->final_v;
-    return GBT_OK;
+    return onesweep_passes(256, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
+               ? GBT_OK
+               : GBT_ECUDA;
 }

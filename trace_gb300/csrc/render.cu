@@ -86,39 +86,6 @@ __global__ void __launch_bounds__(256) k_shade(ShadeParams sp, int level, const 
     }
 }
 
-// Sort key of each ray of a level for a coherent trace order: the direction's
-// octant above the Morton code of the origin quantised to `bits` per axis in the
-// root box.  Slots [count, n) hold no ray and get the largest key, so they sort
-// last and the first `count` sorted positions are the level's rays.
-__global__ void __launch_bounds__(256) k_ray_keys(const float4 *__restrict__ rays, const uint32_t *__restrict__ d_count,
-                                                  uint32_t n, const BvhHeader *__restrict__ hdr, int bits,
-                                                  uint64_t *__restrict__ keys) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t count = *d_count;
-    const uint32_t kb = 3u + 3u * (uint32_t)bits;
-    if (i >= count) {
-        keys[i] = 1ull << kb;
-        return;
-    }
-    const float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
-    const float cells = (float)(1u << bits);
-    uint32_t q[3];
-    const float oc[3] = {o.x, o.y, o.z};
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const float ext = hdr->root_hi[a] - hdr->root_lo[a];
-        float f = ext > 0.f ? (oc[a] - hdr->root_lo[a]) / ext * cells : 0.f;
-        f = fminf(fmaxf(f, 0.f), cells - 1.f);
-        q[a] = (uint32_t)f;
-    }
-    uint64_t m = 0;
-    for (int b = bits - 1; b >= 0; b--)
-        m = (m << 3) | (uint64_t)((((q[2] >> b) & 1u) << 2) | (((q[1] >> b) & 1u) << 1) | ((q[0] >> b) & 1u));
-    const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
-    keys[i] = ((uint64_t)oct << (3u * (uint32_t)bits)) | m;
-}
-
 __global__ void k_resolve(const float *__restrict__ acc, float *__restrict__ out, uint32_t n, float inv_spp) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = acc[i] * inv_spp;
@@ -244,25 +211,6 @@ int gbt_render_buffers(gbt_ctx *ctx, size_t total, size_t npix, RenderState *rs)
 
 int gbt_render_check(gbt_ctx *ctx, const gbt_render_params *p);
 
-// The context's arena for ray-order sorts of up to n rays: keys, then the sort's own scratch
-// (grow-only; a growth synchronises the stream).
-static int sort_arena(gbt_ctx *ctx, uint32_t n) {
-    const size_t need = gbt_align((size_t)n * 8) + gbt_key_sort_bytes(n);
-    if (ctx->sort_arena_bytes >= need) return GBT_OK;
-    if (ctx->sort_arena) {
-        cudaStreamSynchronize(ctx->stream);
-        cudaFree(ctx->sort_arena);
-    }
-    ctx->sort_arena = nullptr;
-    ctx->sort_arena_bytes = 0;
-    if (cudaMalloc(&ctx->sort_arena, need) != cudaSuccess) {
-        cudaGetLastError();
-        return gbt_fail(ctx, GBT_ENOMEM, "render: ray-order sort arena");
-    }
-    ctx->sort_arena_bytes = need;
-    return GBT_OK;
-}
-
 // Times the packet and the one-ray-per-lane kernels on the same camera rays (both leave the same
 // hits) and keeps the faster for this tree.  Synchronises the stream.
 static void measure_packets(gbt_ctx *ctx, gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t count,
@@ -353,21 +301,8 @@ int gbt_render_enqueue(gbt_ctx *ctx, gbt_bvh *bvh, const gbt_camera *cam, const 
                 packets = ctx->primary_packets == 1 || bvh->packet_choice == 1;
             }
             if (!done) {
-                // rays after a bounce: traced in (octant, origin cell) order when the option asks for it
-                uint32_t *const *order = nullptr;
-                if (lv > 0 && ctx->sort_bounce > 0 && count >= (1u << 16)) {
-                    GBT_TRY_R(sort_arena(ctx, count));
-                    uint64_t *keys = reinterpret_cast<uint64_t *>(ctx->sort_arena);
-                    void *arena = static_cast<unsigned char *>(ctx->sort_arena) + gbt_align((size_t)count * 8);
-                    k_ray_keys<<<(count + 255) / 256, 256, 0, st>>>(rs.rays[a], rs.counts + lv, count,
-                                                                    (bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr),
-                                                                    ctx->sort_bounce, keys);
-                    GBT_TRY_R(gbt_key_sort_enqueue(ctx, arena, count, keys, count, &order));
-                    launches += 2 + 8;
-                }
                 if (packets) gbt_launch_traverse_packets(bvh, rs.rays[a], rs.hits, count, 1, ctx->d_error, st, ctr);
-                else gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any,
-                                         order);
+                else gbt_launch_traverse(bvh, rs.rays[a], rs.hits, count, rs.counts + lv, 1, ctx->d_error, st, ctr, any);
             }
             gbt_prof_end(ctx);
             k_shade<<<blocks, 256, 0, st>>>(sp, lv, rs.rays[a], rs.aux[a], rs.hits, rs.counts + lv, rs.rays[a ^ 1],

@@ -332,18 +332,13 @@ __device__ __forceinline__ uint32_t lane_lt() {
 #endif
 
 // ANY: stop at the first hit found (for rays whose shading only needs hit or miss)
-// ORD: the rays are taken in the order *order_pp lists them (positions into rays and
-// hits), e.g. sorted for coherence; hits are still stored at each ray's own position.
-template <int W, bool COUNT, int DYN, bool ANY, bool ORD = false>
+template <int W, bool COUNT, int DYN, bool ANY>
 __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                   const float4 *__restrict__ recs, const float4 *__restrict__ rays,
                                                   float4 *__restrict__ hits, uint32_t n,
                                                   const uint32_t *__restrict__ d_count, int out_mode, unsigned int *err,
-                                                  unsigned long long *counters, uint32_t *fetch,
-                                                  const uint32_t *const *order_pp) {
+                                                  unsigned long long *counters, uint32_t *fetch) {
     constexpr int STACK = W == 2 ? 64 : 96;
-    const uint32_t *order = nullptr;
-    if constexpr (ORD) order = *order_pp;
     constexpr int SH = GBT_PT_SH;
     const uint32_t total = d_count ? *d_count : n;
     const uint32_t lane = threadIdx.x & 31;
@@ -383,9 +378,8 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
             if (want) {
                 const uint32_t id = base + __popc(need & lane_lt());
                 if (id < total) {
-                    const uint32_t slot = ORD ? __ldg(order + id) : id;
-                    rid = slot;
-                    r = gbt_dev::load_ray(rays, slot);
+                    rid = id;
+                    r = gbt_dev::load_ray(rays, id);
                     h.t = r.tmax;
                     h.u = h.v = 0.f;
                     h.rec = -1;
@@ -542,13 +536,13 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_multi(const TreeRef 
     }
 }
 
-template <int W, bool COUNT, int DYN, bool ANY, bool ORD>
+template <int W, bool COUNT, int DYN, bool ANY>
 void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
-               cudaStream_t s, const uint32_t *const *order_pp) {
+               cudaStream_t s) {
     static int per_sm = 0;  // resident blocks per SM of this instantiation
     if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN, ANY, ORD>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN, ANY>, 128, 0);
         if (per_sm <= 0) per_sm = 1;
     }
     uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
@@ -556,51 +550,42 @@ void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const fl
     uint32_t grid = (uint32_t)(ctx->num_sms * per_sm);
     uint32_t need = (n + 127) / 128;
     if (need < grid) grid = need;
-    k_trace_pt<W, COUNT, DYN, ANY, ORD><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode,
-                                                             ctx->d_error, counters, fetch, order_pp);
+    k_trace_pt<W, COUNT, DYN, ANY><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
+                                                  counters, fetch);
 }
 
-template <int W, bool ANY, bool ORD>
-void launch_pt_c(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
-                 float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
-                 cudaStream_t s, bool dyn, const uint32_t *const *order_pp) {
-    if (dyn) {
-        if (counters) launch_pt<W, true, GBT_PT_DYN, ANY, ORD>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, order_pp);
-        else launch_pt<W, false, GBT_PT_DYN, ANY, ORD>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s, order_pp);
-    } else {
-        if (counters) launch_pt<W, true, 0, ANY, ORD>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, order_pp);
-        else launch_pt<W, false, 0, ANY, ORD>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s, order_pp);
-    }
-}
-
-template <int W>
+template <int W, int DYN>
 void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                    float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
-                   cudaStream_t s, bool dyn, bool any, const uint32_t *const *order_pp) {
-    if (order_pp) {
-        if (any) launch_pt_c<W, true, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, dyn, order_pp);
-        else launch_pt_c<W, false, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, dyn, order_pp);
+                   cudaStream_t s, bool any) {
+    if (any) {
+        if (counters) launch_pt<W, true, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     } else {
-        if (any) launch_pt_c<W, true, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, dyn, nullptr);
-        else launch_pt_c<W, false, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s, dyn, nullptr);
+        if (counters) launch_pt<W, true, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     }
 }
 
 }  // namespace
 
 void gbt_launch_traverse(const gbt_bvh *bvh, const float4 *rays, float4 *hits, uint32_t n, const uint32_t *d_count,
-                         int out_mode, unsigned int *d_error, cudaStream_t s, unsigned long long *counters, bool any,
-                         const uint32_t *const *order_pp) {
+                         int out_mode, unsigned int *d_error, cudaStream_t s, unsigned long long *counters, bool any) {
     if (n == 0) return;
     uint32_t blocks = (n + 127) / 128;
     gbt_ctx *ctx = bvh->ctx;
-    if (ctx && (ctx->traversal != 1 || order_pp)) {  // persistent kernels (the only ones that take a ray order)
+    if (ctx && ctx->traversal != 1) {  // persistent kernels
         const bool four = bvh->has_nodes4 || bvh->arity == 4;
         const BvhHeader *hd = bvh->has_nodes4 ? bvh->d_hdr4 : bvh->d_hdr;
         const float4 *nd = bvh->has_nodes4 ? bvh->d_nodes4 : bvh->d_nodes;
-        const bool dyn = ctx->traversal != 2;
-        if (four) launch_pt_any<4>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, dyn, any, order_pp);
-        else launch_pt_any<2>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, dyn, any, order_pp);
+        const bool dyn = ctx->traversal == 0;
+        if (four) {
+            if (dyn) launch_pt_any<4, GBT_PT_DYN>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            else launch_pt_any<4, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+        } else {
+            if (dyn) launch_pt_any<2, GBT_PT_DYN>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+            else launch_pt_any<2, 0>(ctx, hd, nd, bvh->d_prims, rays, hits, n, d_count, out_mode, counters, s, any);
+        }
         return;
     }
     (void)d_error;

@@ -73,7 +73,7 @@ class Context:
         self.check(self.L.gbt_ctx_sync(self.h), "sync")
 
     OPTIONS = {"traversal": 0, "anyhit_last": 1, "primary_tiles": 2, "primary_packets": 3, "keep_workspace": 4,
-               "phr_small_cut": 5, "spin_limit": 6, "test_withhold_tile": 7, "test_collapse_cap": 8, "sort_bounce": 9}
+               "phr_small_cut": 5, "spin_limit": 6, "test_withhold_tile": 7, "test_collapse_cap": 8}
 
     def set_option(self, name, value):
         """Execution option of later calls (gbt_ctx_set_option); results do not depend on it."""
