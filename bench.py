@@ -548,6 +548,8 @@ def run_profile_case(args):
     `phr`: 3 PHR refinements of the scene's LBVH."""
     from trace_gb300 import _lib, pt, scenes
 
+    if args.profile == "batch":
+        return run_profile_batch(args)
     ctx = pt.Context(0)
     if args.profile_scene == "terrain":
         s = scenes.terrain(2048)
@@ -586,6 +588,42 @@ def run_profile_case(args):
     return 0
 
 
+def run_profile_batch(args):
+    """The 64-scene batch without timing, for a launch-list capture: one warm frame of each
+    form, then 2 frames of the per-scene loop (gbt_render_batch_plain_async) and 2 of the
+    batched wavefront, each frame's device time printed from CUDA events so that the
+    launch list's kernel durations can be set against it (the difference is idle time
+    between launches)."""
+    import torch
+
+    from trace_gb300 import _lib, pt, scenes
+
+    ctx = pt.Context(0)
+    ss = scenes.batch(count=args.batch_scenes, seed=3, width=512, height=512, spp=16, max_depth=4)
+    bvhs, cams, params = [], [], []
+    for k, s in enumerate(ss):
+        bvhs.append(pt.DefaultLBVH(pt.DeviceScene.from_dict(ctx, s)))
+        cams.append(s["camera"])
+        p = dict(s["render"])
+        p["seed"] = 1000 + k
+        params.append(p)
+    b = pt.Batch(ctx, bvhs, cams, params)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    cfg = _lib.BatchConfig(128, 16, 0, _lib.BATCH_WAVEFRONT, 1)
+    b.render("plain")
+    b.render("batched", cfg)
+    ctx.sync()
+    for mode in ("plain", "plain", "batched", "batched"):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.render(mode, cfg if mode == "batched" else None)
+        e1.record(stream)
+        ctx.sync()
+        print("profile case batch: %s frame %.3f ms" % (mode, e0.elapsed_time(e1)), flush=True)
+    b.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -599,9 +637,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="leave out the batch, adjoint and terrain LBVH measurements of the default line")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
-    ap.add_argument("--profile", choices=["render", "lbvh", "phr"], default=None,
-                    help="run a small fixed case for an ncu capture and exit: 3 frames (render), 3 LBVH builds "
-                         "or 3 PHR refinements of the LBVH")
+    ap.add_argument("--profile", choices=["render", "lbvh", "phr", "batch"], default=None,
+                    help="run a small fixed case for an ncu capture and exit: 3 frames (render), 3 LBVH builds, "
+                         "3 PHR refinements of the LBVH, or warm then 2+2 frames of the 64-scene batch (batch)")
     ap.add_argument("--phr-bf", type=int, default=PHR[2], choices=[2, 3, 4],
                     help="branching factor of --profile phr")
     ap.add_argument("--profile-scene", choices=["soup", "terrain"], default="soup",

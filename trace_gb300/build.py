@@ -45,11 +45,18 @@ def _stale(out, inputs):
     return any(os.path.getmtime(i) > t for i in inputs)
 
 
+def _extra():
+    """Extra nvcc arguments from GBT_NVCC_EXTRA (e.g. "-DGBT_PT_DYN=12"), for measuring build
+    variants; a change of them rebuilds every object."""
+    return os.environ.get("GBT_NVCC_EXTRA", "").split()
+
+
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
-    if not _stale(obj, _deps(src)):
+    stamp = os.path.join(BUILD, "extra_flags")
+    if not _stale(obj, _deps(src) + ([stamp] if os.path.exists(stamp) else [])):
         return obj, ""
-    cmd = [nvcc(), *ARCH, *FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *FLAGS, *_extra(), "-c", src, "-o", obj]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -60,6 +67,11 @@ def _compile(src, verbose_ptxas=False):
 
 def build(force=False, verbose_ptxas=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "extra_flags")
+    extra = " ".join(_extra())
+    if (open(stamp).read() if os.path.exists(stamp) else "") != extra:
+        with open(stamp, "w") as f:  # newer than every object: all are rebuilt with the new flags
+            f.write(extra)
     if force:
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))

@@ -1783,8 +1783,11 @@ struct LevelSmem<BS, 2> {
 // LMODE (one-warp blocks): 1 the lane path for bf = 2, 2 the lane path for
 // bf > 2 in rounds, 0 none (a one-warp block then holds less state and more
 // of them are resident).
+#ifndef GBT_PHR_LANE_MINB
+#define GBT_PHR_LANE_MINB 20  // resident one-warp blocks per SM the lane path's registers are sized for
+#endif
 template <int BS, int LMODE = (BS == 32 ? 1 : 0)>
-__global__ void __launch_bounds__(BS, BS == 32 ? (LMODE ? 20 : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
+__global__ void __launch_bounds__(BS, BS == 32 ? (LMODE ? GBT_PHR_LANE_MINB : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {
     constexpr bool LANES = LMODE != 0;
     __shared__ LevelSmem<BS, LMODE> smem;
     BlockShared<BS> &sh = smem.block;

@@ -331,8 +331,10 @@ __device__ __forceinline__ uint32_t lane_lt() {
 #define GBT_PT_SH 12
 #endif
 
-// ANY: stop at the first hit found (for rays whose shading only needs hit or miss)
-template <int W, bool COUNT, int DYN, bool ANY>
+// AM 0: closest hit.  AM 1 and 2: stop at the first hit found (for rays whose shading
+// only needs hit or miss); with AM 2 a lane that reaches a leaf waits for the warp's leaf
+// phase instead of descending further, since that leaf may end its query.
+template <int W, bool COUNT, int DYN, int AM>
 __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                   const float4 *__restrict__ recs, const float4 *__restrict__ rays,
                                                   float4 *__restrict__ hits, uint32_t n,
@@ -340,6 +342,8 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                                                   unsigned long long *counters, uint32_t *fetch) {
     constexpr int STACK = W == 2 ? 64 : 96;
     constexpr int SH = GBT_PT_SH;
+    constexpr bool ANY = AM > 0;
+    constexpr int PAUSED = -2;  // node.y of a lane waiting (AM 2) with its leaf for the leaf phase
     const uint32_t total = d_count ? *d_count : n;
     const uint32_t lane = threadIdx.x & 31;
     using StackT = typename std::conditional<(SH > 0), gbt_dev::SharedTopStack<STACK, (SH > 0 ? SH : 1)>,
@@ -406,9 +410,9 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                 if (COUNT) w.nodes++;
                 node = W == 2 ? gbt_dev::step2(nodes, node, st, sp, r, h.t, err)
                               : gbt_dev::step4(nodes, node, st, sp, r, h.t, err);
-                if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf, keep descending
+                if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf
                     leaf = node;
-                    node = st.pop(sp, h.t);
+                    node = AM == 2 ? make_int2(0, PAUSED) : st.pop(sp, h.t);  // wait, or keep descending
                 }
                 if (!__any_sync(__activemask(), leaf.y <= 0)) break;  // every lane here holds a leaf
             }
@@ -426,6 +430,7 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                     leaf = make_int2(0, 0);
                 }
             }
+            if (AM == 2 && node.y == PAUSED) node = st.pop(sp, h.t);  // no hit in the leaf: descend on
             if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
         }
     }
@@ -536,13 +541,13 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_multi(const TreeRef 
     }
 }
 
-template <int W, bool COUNT, int DYN, bool ANY>
+template <int W, bool COUNT, int DYN, int AM>
 void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
                cudaStream_t s) {
     static int per_sm = 0;  // resident blocks per SM of this instantiation
     if (per_sm == 0) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN, ANY>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_pt<W, COUNT, DYN, AM>, 128, 0);
         if (per_sm <= 0) per_sm = 1;
     }
     uint32_t *fetch = reinterpret_cast<uint32_t *>(ctx->d_counters + 3);
@@ -550,20 +555,23 @@ void launch_pt(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const fl
     uint32_t grid = (uint32_t)(ctx->num_sms * per_sm);
     uint32_t need = (n + 127) / 128;
     if (need < grid) grid = need;
-    k_trace_pt<W, COUNT, DYN, ANY><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
-                                                  counters, fetch);
+    k_trace_pt<W, COUNT, DYN, AM><<<grid, 128, 0, s>>>(hdr, nodes, recs, rays, hits, n, d_count, out_mode, ctx->d_error,
+                                                     counters, fetch);
 }
 
 template <int W, int DYN>
 void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                    float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
                    cudaStream_t s, bool any) {
-    if (any) {
-        if (counters) launch_pt<W, true, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
-        else launch_pt<W, false, DYN, true>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+    if (any && ctx->any_pause) {
+        if (counters) launch_pt<W, true, DYN, 2>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, 2>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+    } else if (any) {
+        if (counters) launch_pt<W, true, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     } else {
-        if (counters) launch_pt<W, true, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
-        else launch_pt<W, false, DYN, false>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+        if (counters) launch_pt<W, true, DYN, 0>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN, 0>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     }
 }
 
