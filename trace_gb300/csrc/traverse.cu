@@ -330,6 +330,12 @@ __device__ __forceinline__ uint32_t lane_lt() {
 #ifndef GBT_PT_SH
 #define GBT_PT_SH 12
 #endif
+// 4-wide nodes with an index below TOPN (the collapse numbers them level by level, so these
+// are the top of the tree, which every ray passes through) copied into each block's shared
+// memory at launch; 0: none.
+#ifndef GBT_PT_TOPN
+#define GBT_PT_TOPN 0
+#endif
 
 // AM 0: closest hit.  AM 1 and 2: stop at the first hit found (for rays whose shading
 // only needs hit or miss); with AM 2 a lane that reaches a leaf waits for the warp's leaf
@@ -355,6 +361,17 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
         st.se = s_se + threadIdx.x;
         st.st = s_st + threadIdx.x;
         st.stride = 128;
+    }
+    const float4 *top = nullptr;
+    int ntop = 0;
+    if constexpr (W == 4 && GBT_PT_TOPN > 0) {
+        __shared__ float4 s_top[8 * (GBT_PT_TOPN > 0 ? GBT_PT_TOPN : 1)];
+        // n_nodes (inner nodes of the tree the view was collapsed from, or of a 4-wide PHR
+        // tree) bounds the nodes the array holds; copies past the ones in use are never read
+        ntop = hdr->root_cnt == 0 ? (int)min((uint32_t)GBT_PT_TOPN, hdr->n_nodes) : 0;
+        for (int i = threadIdx.x; i < 8 * ntop; i += blockDim.x) s_top[i] = __ldg(nodes + i);
+        __syncthreads();
+        top = s_top;
     }
     int sp = 0;
     int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
@@ -409,7 +426,7 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
             while (node.y == 0) {
                 if (COUNT) w.nodes++;
                 node = W == 2 ? gbt_dev::step2(nodes, node, st, sp, r, h.t, err)
-                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err);
+                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err, top, ntop);
                 if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf
                     leaf = node;
                     node = AM == 2 ? make_int2(0, PAUSED) : st.pop(sp, h.t);  // wait, or keep descending
