@@ -74,11 +74,8 @@ struct gbt_ctx {
     // bounded device waits (GBT_OPT_SPIN_LIMIT) and the testing aids that make them and the
     // work-list checks trip (GBT_OPT_TEST_WITHHOLD_TILE, GBT_OPT_TEST_COLLAPSE_CAP)
     uint32_t spin_limit = GBT_SPIN_LIMIT;
-    // the LBVH sort's pass kernel: 0 256 threads of 16 keys ranked by ballots, 1 512 threads of
-    // 8 keys, 2 256 threads ranked by __match_any_sync
-    int sort_variant = 0;
-    // 1: the LBVH emission makes the primitive records itself (no separate gather launch)
-    int lbvh_fuse = 0;
+    // threads per tile of the LBVH sort's passes: 256 (16 keys each) or 512 (8 keys each)
+    int sort_threads = 256;
     // any-hit queries: 1, a lane that reaches a leaf waits for the warp's leaf phase
     int any_pause = 0;
     uint32_t withhold_tile = 0xffffffffu;

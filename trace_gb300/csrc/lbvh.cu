@@ -7,9 +7,9 @@
 //   k_hist, k_sort_plan, k_onesweep x8
 //                stable LSD radix sort of (code, index)   (lbvh.go:216-301 bucket sort)
 //   k_rle_*      runs of equal codes -> leaves            (lbvh.go:134-145, 179-181)
-//   k_gather     primitive records in leaf order
-//   k_emit       binary radix tree over the distinct codes with the
-//                bottom-up box refit fused in             (lbvh.go:76-203, bvh.go:104-126,201-222)
+//   k_emit       primitive records in leaf order, and the binary radix tree
+//                over the distinct codes with the bottom-up box refit fused
+//                in                                       (lbvh.go:76-203, bvh.go:104-126,201-222)
 #include <cuda_runtime.h>
 
 #include "gbt_internal.cuh"
@@ -396,8 +396,7 @@ __device__ __forceinline__ bool sort_failed(const unsigned int *err) {
 // after it wait for a status nothing sets and the limit is reached.
 // T threads of I keys each (T * I = SORT_TILE); the register budget is sized for two
 // resident blocks per SM.  Digit-wise steps take one thread per digit (the first 256).
-// MATCH: the lanes sharing a digit from __match_any_sync instead of one ballot per digit bit.
-template <int T, int I, bool MATCH>
+template <int T, int I>
 __global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                  uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
                                                  unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
@@ -445,17 +444,13 @@ __global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ 
         uint32_t idx = wbase + i * 32 + lane;
         bool ok = idx < n;
         uint32_t d = ok ? (uint32_t)((k[i] >> shift) & 255u) : 256u;
-        // lanes with the same digit (lanes past the end share digit 256 and are not counted)
-        uint32_t peers;
-        if constexpr (MATCH) {
-            peers = __match_any_sync(0xffffffffu, d);
-        } else {  // one vote per digit bit, valid lanes only
-            peers = __ballot_sync(0xffffffffu, ok);
+        // lanes with the same digit, from one vote per digit bit (valid lanes only; ranking by
+        // __match_any_sync measured slower)
+        uint32_t peers = __ballot_sync(0xffffffffu, ok);
 #pragma unroll
-            for (int b = 0; b < 8; b++) {
-                const uint32_t vb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-                peers &= ((d >> b) & 1u) ? vb : ~vb;
-            }
+        for (int b = 0; b < 8; b++) {
+            const uint32_t vb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? vb : ~vb;
         }
         uint32_t base = ok ? wh[d] : 0u;
         __syncwarp();
@@ -517,32 +512,27 @@ __global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ 
 }
 
 // Launches the eight passes (a pass whose plan entry is inactive returns at once).
-// Launches the eight passes (a pass whose plan entry is inactive returns at once).  variant:
-// 0 256 threads with ballot ranking, 1 512 threads, 2 256 threads with __match_any_sync ranking.
-static cudaError_t onesweep_passes(int variant, const SortPlan *plan, uint32_t n, uint32_t n_tiles, uint32_t *status,
+// Launches the eight passes (a pass whose plan entry is inactive returns at once) with tiles
+// of 256 threads x 16 keys (threads 256) or 512 x 8 (threads 512, measured no faster).
+static cudaError_t onesweep_passes(int threads, const SortPlan *plan, uint32_t n, uint32_t n_tiles, uint32_t *status,
                                    uint32_t *ctr, unsigned int *err, uint32_t spin_limit, uint32_t withhold0,
                                    cudaStream_t st) {
-    const int threads = variant == 1 ? 512 : 256;
     const int nw = threads / 32;
     const size_t smem = (size_t)(nw * 256 + 256 + 256 + 32) * sizeof(uint32_t) +
                         (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
     cudaError_t e;
-    if (variant == 1) e = cudaFuncSetAttribute(k_onesweep<512, SORT_TILE / 512, false>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    else if (variant == 2) e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, true>,
-                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    else e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (threads == 512) e = cudaFuncSetAttribute(k_onesweep<512, SORT_TILE / 512>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    else e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem);
     if (e != cudaSuccess) return e;
     for (int p = 0; p < 8; p++) {
         uint32_t *sp = status + (size_t)p * n_tiles * 256;
         const uint32_t wh = p == 0 ? withhold0 : 0xffffffffu;
-        if (variant == 1)
-            k_onesweep<512, SORT_TILE / 512, false><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
-        else if (variant == 2)
-            k_onesweep<256, SORT_TILE / 256, true><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+        if (threads == 512)
+            k_onesweep<512, SORT_TILE / 512><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
         else
-            k_onesweep<256, SORT_TILE / 256, false><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+            k_onesweep<256, SORT_TILE / 256><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
     }
     return cudaGetLastError();
 }
@@ -660,20 +650,6 @@ __device__ __forceinline__ void make_record(const float *__restrict__ verts, con
     }
 }
 
-__global__ void __launch_bounds__(256) k_gather(const SortPlan *__restrict__ plan, const float *__restrict__ verts,
-                                                const float4 *__restrict__ sph, uint32_t n_tri, uint32_t n,
-                                                float4 *__restrict__ recs, const unsigned int *err) {
-    if (sort_failed(err)) return;
-    const uint32_t *idx = plan->final_v;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-        float4 r0, r1, r2;
-        make_record(verts, sph, n_tri, idx[s], r0, r1, r2);
-        recs[3 * (size_t)s + 0] = r0;
-        recs[3 * (size_t)s + 1] = r1;
-        recs[3 * (size_t)s + 2] = r2;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // hierarchy emission + refit
 // ---------------------------------------------------------------------------
@@ -682,21 +658,6 @@ __global__ void __launch_bounds__(256) k_gather(const SortPlan *__restrict__ pla
 __device__ __forceinline__ void box_of_record(const float4 &r0, const float4 &r1, const float4 &r2, float3 &lo,
                                               float3 &hi) {
     if (__float_as_int(r1.w) == 0) {
-        lo = make_float3(fminf(fminf(r0.x, r1.x), r2.x), fminf(fminf(r0.y, r1.y), r2.y), fminf(fminf(r0.z, r1.z), r2.z));
-        hi = make_float3(fmaxf(fmaxf(r0.x, r1.x), r2.x), fmaxf(fmaxf(r0.y, r1.y), r2.y), fmaxf(fmaxf(r0.z, r1.z), r2.z));
-    } else {
-        double r = r1.x;
-        lo = make_float3(__double2float_rd((double)r0.x - r), __double2float_rd((double)r0.y - r),
-                         __double2float_rd((double)r0.z - r));
-        hi = make_float3(__double2float_ru((double)r0.x + r), __double2float_ru((double)r0.y + r),
-                         __double2float_ru((double)r0.z + r));
-    }
-}
-
-__device__ __forceinline__ void record_box(const float4 *__restrict__ recs, uint32_t s, float3 &lo, float3 &hi) {
-    float4 r0 = recs[3 * (size_t)s], r1 = recs[3 * (size_t)s + 1];
-    if (__float_as_int(r1.w) == 0) {
-        float4 r2 = recs[3 * (size_t)s + 2];
         lo = make_float3(fminf(fminf(r0.x, r1.x), r2.x), fminf(fminf(r0.y, r1.y), r2.y), fminf(fminf(r0.z, r1.z), r2.z));
         hi = make_float3(fmaxf(fmaxf(r0.x, r1.x), r2.x), fmaxf(fmaxf(r0.y, r1.y), r2.y), fmaxf(fmaxf(r0.z, r1.z), r2.z));
     } else {
@@ -762,9 +723,9 @@ __device__ __forceinline__ float4 lds_f4(const float4 *p) {
 // Number of nodes (leaves included) under a node of distinct-code range [l, r].
 __device__ __forceinline__ uint32_t range_size(uint32_t l, uint32_t r) { return 2u * (r - l) + 1u; }
 
-// FUSE: the leaves' primitive records are made here from the sorted indices and the
-// vertices (the work of k_gather), and their boxes taken from the values in registers.
-template <bool FUSE>
+// Each leaf's primitive records are made here, from the sorted indices and the vertices,
+// and its box is taken from the values in registers (one pass over the records instead of
+// a gather launch that writes them and an emission that reads them back).
 __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
                                                        const uint32_t *__restrict__ run,
                                                        const uint64_t *__restrict__ ukey,
@@ -827,29 +788,19 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
     if (u >= U || u >= n) return;
     uint32_t first = run[u], last = run[u + 1];
     float3 lo, hi;
-    if constexpr (FUSE) {
-        const uint32_t *__restrict__ idx = plan->final_v;
-        for (uint32_t s = first; s < last; s++) {
-            float4 r0, r1, r2;
-            make_record(verts, sph, n_tri, idx[s], r0, r1, r2);
-            recs[3 * (size_t)s + 0] = r0;
-            recs[3 * (size_t)s + 1] = r1;
-            recs[3 * (size_t)s + 2] = r2;
-            float3 a, b;
-            box_of_record(r0, r1, r2, a, b);
-            if (s == first) {
-                lo = a;
-                hi = b;
-            } else {
-                lo = make_float3(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z));
-                hi = make_float3(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z));
-            }
-        }
-    } else {
-        record_box(recs, first, lo, hi);
-        for (uint32_t s = first + 1; s < last; s++) {
-            float3 a, b;
-            record_box(recs, s, a, b);
+    const uint32_t *__restrict__ idx = plan->final_v;
+    for (uint32_t s = first; s < last; s++) {
+        float4 r0, r1, r2;
+        make_record(verts, sph, n_tri, idx[s], r0, r1, r2);
+        recs[3 * (size_t)s + 0] = r0;
+        recs[3 * (size_t)s + 1] = r1;
+        recs[3 * (size_t)s + 2] = r2;
+        float3 a, b;
+        box_of_record(r0, r1, r2, a, b);
+        if (s == first) {
+            lo = a;
+            hi = b;
+        } else {
             lo = make_float3(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z));
             hi = make_float3(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z));
         }
@@ -1005,7 +956,7 @@ static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &s
     int hb = ctx->num_sms * 2;
     k_hist<<<hb, 256, 0, st>>>(kA, n, hist);
     k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
-    GBT_CUDA(ctx, onesweep_passes(ctx->sort_variant, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
+    GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
                                   ctx->withhold_tile, st));
     return GBT_OK;
 }
@@ -1039,21 +990,14 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, ctx->d_error);
     k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr, ctx->d_error);
     k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey, ctx->d_error);
-    if (!ctx->lbvh_fuse)
-        k_gather<<<grid, 256, 0, st>>>(plan, sc->d_verts, sc->d_sph, n_tri, n, bvh->d_prims, ctx->d_error);
     uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
     EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
     const uint32_t eb = emit_blocks(n);
     GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
     GBT_CUDA(ctx, cudaMemsetAsync(top_n, 0, sizeof(uint32_t), st));
-    if (ctx->lbvh_fuse)
-        k_emit<true><<<eb, EMIT_THREADS, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims,
-                                                  bvh->d_nodes, bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range,
-                                                  n, top, top_n, eb, ctx->d_error, plan, sc->d_verts, sc->d_sph, n_tri);
-    else
-        k_emit<false><<<eb, EMIT_THREADS, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims,
-                                                   bvh->d_nodes, bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range,
-                                                   n, top, top_n, eb, ctx->d_error, plan, sc->d_verts, sc->d_sph, n_tri);
+    k_emit<<<eb, EMIT_THREADS, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
+                                        bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n, top, top_n, eb,
+                                        ctx->d_error, plan, sc->d_verts, sc->d_sph, n_tri);
     k_emit_top<<<(eb + 127) / 128, 128, 0, st>>>(bvh->d_hdr, bvh->d_ukey, bvh->d_nodes, bvh->d_other, bvh->d_size,
                                                  bvh->d_parent, bvh->d_range, top, top_n, eb, ctx->d_error);
     GBT_CUDA(ctx, cudaGetLastError());
@@ -1115,7 +1059,7 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
     if (cudaMemsetAsync(err, 0, sizeof(unsigned int), st) != cudaSuccess) return GBT_ECUDA;
     k_hist<<<num_sms * 2, 256, 0, st>>>(codes_in, n, hist);
     k_sort_plan_all<<<1, 256, 0, st>>>(plan, hist, codes_in, codes_out, idx_out, kB, vB);
-    return onesweep_passes(0, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
+    return onesweep_passes(256, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
                ? GBT_OK
                : GBT_ECUDA;
 }

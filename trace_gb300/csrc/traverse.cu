@@ -447,7 +447,13 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                     leaf = make_int2(0, 0);
                 }
             }
-            if (AM == 2 && node.y == PAUSED) node = st.pop(sp, h.t);  // no hit in the leaf: descend on
+            if (AM == 2 && node.y == PAUSED) {  // no hit in the leaf: go on with the next stack entry
+                node = st.pop(sp, h.t);
+                if (node.y > 0) {  // itself a leaf: hold it and wait for the next leaf phase
+                    leaf = node;
+                    node = make_int2(0, PAUSED);
+                }
+            }
             if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
         }
     }
