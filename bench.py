@@ -502,7 +502,7 @@ def measure_terrain_lbvh(args):
             "roofline": {"bound": "hbm", "achieved": bw, "peak": hbm, "unit": "GB/s", "frac": bw / hbm,
                          "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind,
                          "traffic": LBVH_TRAFFIC_PER_TRI["terrain2048"] * n,
-                         "traffic_scope": "DRAM bytes of one build, ncu cold-cache capture (before the gather was fused into the emission)",
+                         "traffic_scope": "DRAM bytes of one build (17 launches), ncu cold-cache capture",
                          "kernel": "whole build (17 launches)"}}
 
 
@@ -799,7 +799,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
                          "bytes_per_tri": LBVH_BYTES_PER_TRI,
                          "traffic": LBVH_TRAFFIC_PER_TRI["soup1M"] * N_TRI if LBVH_TRAFFIC_PER_TRI["soup1M"] else None,
-                         "traffic_scope": "DRAM bytes of one build, ncu cold-cache capture (before the gather was fused into the emission)",
+                         "traffic_scope": "DRAM bytes of one build (17 launches), ncu cold-cache capture",
                          "kernel": "whole build (17 launches)"}}
 
     line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -836,10 +836,10 @@ def main():
 
 
 # DRAM bytes per triangle of one LBVH build (dram__bytes_read.sum + dram__bytes_write.sum summed
-# over the build's 18 launches, one ncu capture of the second of three builds each):
-# terrain2048 3816.5 MB / 8,380,419 primitives; soup1M 333.3 MB / 1,000,000 (its keys and
-# records largely stay in the 129 MB L2, so the capture counts fewer bytes than the algorithm).
-LBVH_TRAFFIC_PER_TRI = {"terrain2048": 3816.5e6 / 8380419, "soup1M": 333.25e6 / 1e6}
+# over the build's 17 launches, one ncu capture of the second of four builds each):
+# terrain2048 3510.6 MB / 8,380,419 primitives; soup1M 366.3 MB / 1,000,000 (its keys largely
+# stay in the 129 MB L2, so the capture counts fewer bytes than the algorithm moves).
+LBVH_TRAFFIC_PER_TRI = {"terrain2048": 3510.6e6 / 8380419, "soup1M": 366.3e6 / 1e6}
 
 # DRAM bytes of one headline frame's two traversal launches on the PHR tree
 # (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full capture each:

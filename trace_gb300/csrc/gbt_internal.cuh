@@ -76,8 +76,6 @@ struct gbt_ctx {
     uint32_t spin_limit = GBT_SPIN_LIMIT;
     // threads per tile of the LBVH sort's passes: 256 (16 keys each) or 512 (8 keys each)
     int sort_threads = 256;
-    // any-hit queries: 1, a lane that reaches a leaf waits for the warp's leaf phase
-    int any_pause = 0;
     uint32_t withhold_tile = 0xffffffffu;
     uint32_t collapse_cap = 0;
 };

@@ -1785,6 +1785,7 @@ struct LevelSmem<BS, 2> {
 // of them are resident).
 #ifndef GBT_PHR_LANE_MINB
 #define GBT_PHR_LANE_MINB 20  // resident one-warp blocks per SM the lane path's registers are sized for
+                              // (24 and 32, with spills, measured slower)
 #endif
 template <int BS, int LMODE = (BS == 32 ? 1 : 0)>
 __global__ void __launch_bounds__(BS, BS == 32 ? (LMODE ? GBT_PHR_LANE_MINB : 32) : (BS == PT ? 2 : 1)) k_phr_level(LevelArgs A) {

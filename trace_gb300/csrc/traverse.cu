@@ -330,16 +330,10 @@ __device__ __forceinline__ uint32_t lane_lt() {
 #ifndef GBT_PT_SH
 #define GBT_PT_SH 12
 #endif
-// 4-wide nodes with an index below TOPN (the collapse numbers them level by level, so these
-// are the top of the tree, which every ray passes through) copied into each block's shared
-// memory at launch; 0: none.
-#ifndef GBT_PT_TOPN
-#define GBT_PT_TOPN 0
-#endif
 
-// AM 0: closest hit.  AM 1 and 2: stop at the first hit found (for rays whose shading
-// only needs hit or miss); with AM 2 a lane that reaches a leaf waits for the warp's leaf
-// phase instead of descending further, since that leaf may end its query.
+
+// AM 0: closest hit.  AM 1: stop at the first hit found (for rays whose shading only
+// needs hit or miss).
 template <int W, bool COUNT, int DYN, int AM>
 __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                                   const float4 *__restrict__ recs, const float4 *__restrict__ rays,
@@ -349,7 +343,6 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
     constexpr int STACK = W == 2 ? 64 : 96;
     constexpr int SH = GBT_PT_SH;
     constexpr bool ANY = AM > 0;
-    constexpr int PAUSED = -2;  // node.y of a lane waiting (AM 2) with its leaf for the leaf phase
     const uint32_t total = d_count ? *d_count : n;
     const uint32_t lane = threadIdx.x & 31;
     using StackT = typename std::conditional<(SH > 0), gbt_dev::SharedTopStack<STACK, (SH > 0 ? SH : 1)>,
@@ -361,17 +354,6 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
         st.se = s_se + threadIdx.x;
         st.st = s_st + threadIdx.x;
         st.stride = 128;
-    }
-    const float4 *top = nullptr;
-    int ntop = 0;
-    if constexpr (W == 4 && GBT_PT_TOPN > 0) {
-        __shared__ float4 s_top[8 * (GBT_PT_TOPN > 0 ? GBT_PT_TOPN : 1)];
-        // n_nodes (inner nodes of the tree the view was collapsed from, or of a 4-wide PHR
-        // tree) bounds the nodes the array holds; copies past the ones in use are never read
-        ntop = hdr->root_cnt == 0 ? (int)min((uint32_t)GBT_PT_TOPN, hdr->n_nodes) : 0;
-        for (int i = threadIdx.x; i < 8 * ntop; i += blockDim.x) s_top[i] = __ldg(nodes + i);
-        __syncthreads();
-        top = s_top;
     }
     int sp = 0;
     int2 node = make_int2(0, -1), leaf = make_int2(0, 0);
@@ -426,10 +408,10 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
             while (node.y == 0) {
                 if (COUNT) w.nodes++;
                 node = W == 2 ? gbt_dev::step2(nodes, node, st, sp, r, h.t, err)
-                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err, top, ntop);
-                if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf
+                              : gbt_dev::step4(nodes, node, st, sp, r, h.t, err);
+                if (node.y > 0 && leaf.y <= 0) {  // postpone the leaf, keep descending
                     leaf = node;
-                    node = AM == 2 ? make_int2(0, PAUSED) : st.pop(sp, h.t);  // wait, or keep descending
+                    node = st.pop(sp, h.t);
                 }
                 if (!__any_sync(__activemask(), leaf.y <= 0)) break;  // every lane here holds a leaf
             }
@@ -445,13 +427,6 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                     node = st.pop(sp, h.t);
                 } else {
                     leaf = make_int2(0, 0);
-                }
-            }
-            if (AM == 2 && node.y == PAUSED) {  // no hit in the leaf: go on with the next stack entry
-                node = st.pop(sp, h.t);
-                if (node.y > 0) {  // itself a leaf: hold it and wait for the next leaf phase
-                    leaf = node;
-                    node = make_int2(0, PAUSED);
                 }
             }
             if (DYN > 0 && !pool_empty && __popc(__activemask()) < DYN) break;
@@ -586,10 +561,7 @@ template <int W, int DYN>
 void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                    float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
                    cudaStream_t s, bool any) {
-    if (any && ctx->any_pause) {
-        if (counters) launch_pt<W, true, DYN, 2>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
-        else launch_pt<W, false, DYN, 2>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
-    } else if (any) {
+    if (any) {
         if (counters) launch_pt<W, true, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
         else launch_pt<W, false, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     } else {

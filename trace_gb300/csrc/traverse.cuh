@@ -306,21 +306,15 @@ __device__ __forceinline__ void cx(Cand &a, Cand &b) {  // compare-exchange, asc
 
 // One inner-node step on a 4-wide node: children sorted near to far by a
 // register sorting network, the nearest taken, the others pushed far first.
-// With top != nullptr the nodes below index ntop are read from that shared-memory copy.
 template <class StackT>
 __device__ __forceinline__ int2 step4(const float4 *__restrict__ nodes, int2 node, StackT &st, int &sp, const Ray &r,
-                                      float tmax, unsigned int *err, const float4 *top = nullptr, int ntop = 0) {
+                                      float tmax, unsigned int *err) {
+    const float4 *nd = nodes + 8 * (size_t)node.x;
     float4 lx, hx, ly, hy, lz, hz, rff, cnf;
-    if (top && node.x < ntop) {
-        const float4 *sd = top + 8 * node.x;
-        lx = sd[0]; hx = sd[1]; ly = sd[2]; hy = sd[3]; lz = sd[4]; hz = sd[5]; rff = sd[6]; cnf = sd[7];
-    } else {
-        const float4 *nd = nodes + 8 * (size_t)node.x;
-        ldg256(nd, lx, hx);
-        ldg256(nd + 2, ly, hy);
-        ldg256(nd + 4, lz, hz);
-        ldg256(nd + 6, rff, cnf);
-    }
+    ldg256(nd, lx, hx);
+    ldg256(nd + 2, ly, hy);
+    ldg256(nd + 4, lz, hz);
+    ldg256(nd + 6, rff, cnf);
     const int4 rf = make_int4(__float_as_int(rff.x), __float_as_int(rff.y), __float_as_int(rff.z), __float_as_int(rff.w));
     const int4 cn = make_int4(__float_as_int(cnf.x), __float_as_int(cnf.y), __float_as_int(cnf.z), __float_as_int(cnf.w));
     const float MISS = __int_as_float(0x7f800000);
