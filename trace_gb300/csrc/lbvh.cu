@@ -12,6 +12,8 @@
 //                in                                       (lbvh.go:76-203, bvh.go:104-126,201-222)
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "gbt_internal.cuh"
 #include "morton_exact.cuh"
 
@@ -79,6 +81,9 @@ __device__ __forceinline__ void prim_box_f64(const float *__restrict__ verts, co
 // ---------------------------------------------------------------------------
 // scene bounds
 // ---------------------------------------------------------------------------
+#ifndef GBT_BOUNDS_BLOCKS_PER_SM
+#define GBT_BOUNDS_BLOCKS_PER_SM 8
+#endif
 // Triangle boxes are float32 values, so their fold is done in float32 (exact)
 // over the vertex array read as float4 triples: 12 floats hold 4 vertices with
 // the axis pattern x y z x | y z x y | z x y z.  Sphere boxes (c -+ r in
@@ -396,8 +401,11 @@ __device__ __forceinline__ bool sort_failed(const unsigned int *err) {
 // after it wait for a status nothing sets and the limit is reached.
 // T threads of I keys each (T * I = SORT_TILE); the register budget is sized for two
 // resident blocks per SM.  Digit-wise steps take one thread per digit (the first 256).
+#ifndef GBT_SORT_MINB
+#define GBT_SORT_MINB 2  // resident 256-thread sort blocks per SM the registers are sized for
+#endif
 template <int T, int I>
-__global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
+__global__ void __launch_bounds__(T, T == 256 ? GBT_SORT_MINB : 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                  uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
                                                  unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
     static_assert(T * I == SORT_TILE && T >= 256 && T % 32 == 0, "tile shape");
@@ -433,9 +441,7 @@ __global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ 
 #pragma unroll
     for (int i = 0; i < I; i++) {
         uint32_t idx = wbase + i * 32 + lane;
-        bool ok = idx < n;
-        k[i] = ok ? __ldcs(kin + idx) : 0ull;
-        v[i] = ident ? idx : (ok ? __ldcs(vin + idx) : 0u);
+        k[i] = idx < n ? __ldcs(kin + idx) : 0ull;
     }
     uint32_t *wh = s_wh + warp * 256;
     const uint32_t lt = lanemask_lt();
@@ -457,6 +463,13 @@ __global__ void __launch_bounds__(T, 2) k_onesweep(const SortPlan *__restrict__ 
         if (ok && lane == (uint32_t)(__ffs(peers) - 1)) wh[d] = base + __popc(peers);
         __syncwarp();
         rk[i] = base + __popc(peers & lt);
+    }
+    // the values are needed only for the scatter: loaded now, they arrive during the
+    // per-digit steps and the look-back, and take no registers during the ranking
+#pragma unroll
+    for (int i = 0; i < I; i++) {
+        uint32_t idx = wbase + i * 32 + lane;
+        v[i] = ident ? idx : (idx < n ? __ldcs(vin + idx) : 0u);
     }
     __syncthreads();
 
@@ -980,7 +993,9 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     int grid = ctx->num_sms * 8;
     int g2 = (int)((n + 255) / 256);
     if (g2 < grid) grid = g2;
-    k_bounds<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc);
+    // the scene box: each block ends with six atomics on the same six words
+    const int gb = std::min(grid, ctx->num_sms * GBT_BOUNDS_BLOCKS_PER_SM);
+    k_bounds<<<gb, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc);
     k_morton<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes);
     rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr);
     if (rc) return rc;
