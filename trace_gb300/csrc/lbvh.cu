@@ -81,8 +81,11 @@ __device__ __forceinline__ void prim_box_f64(const float *__restrict__ verts, co
 // ---------------------------------------------------------------------------
 // scene bounds
 // ---------------------------------------------------------------------------
+// Blocks per SM of the scene-box fold: each block ends with atomics on the same six words,
+// which serialise (8 blocks per SM: 31 us for the 1M soup's 36 MB, 2: 0.367 against 0.381 ms
+// for the whole build)
 #ifndef GBT_BOUNDS_BLOCKS_PER_SM
-#define GBT_BOUNDS_BLOCKS_PER_SM 8
+#define GBT_BOUNDS_BLOCKS_PER_SM 2
 #endif
 // Triangle boxes are float32 values, so their fold is done in float32 (exact)
 // over the vertex array read as float4 triples: 12 floats hold 4 vertices with
@@ -401,11 +404,11 @@ __device__ __forceinline__ bool sort_failed(const unsigned int *err) {
 // after it wait for a status nothing sets and the limit is reached.
 // T threads of I keys each (T * I = SORT_TILE); the register budget is sized for two
 // resident blocks per SM.  Digit-wise steps take one thread per digit (the first 256).
-#ifndef GBT_SORT_MINB
-#define GBT_SORT_MINB 2  // resident 256-thread sort blocks per SM the registers are sized for
-#endif
-template <int T, int I>
-__global__ void __launch_bounds__(T, T == 256 ? GBT_SORT_MINB : 2) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
+// MINB: resident blocks per SM the registers are sized for.  3 (80 registers) is faster for
+// sorts of many tiles (the 8.4M terrain: 1.622 against 1.642 ms a build) and slower for
+// sorts of about one wave (the 1M soup: 0.376 against 0.367 ms).
+template <int T, int I, int MINB = 2>
+__global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                  uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
                                                  unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
     static_assert(T * I == SORT_TILE && T >= 256 && T % 32 == 0, "tile shape");
@@ -527,15 +530,20 @@ __global__ void __launch_bounds__(T, T == 256 ? GBT_SORT_MINB : 2) k_onesweep(co
 // Launches the eight passes (a pass whose plan entry is inactive returns at once).
 // Launches the eight passes (a pass whose plan entry is inactive returns at once) with tiles
 // of 256 threads x 16 keys (threads 256) or 512 x 8 (threads 512, measured no faster).
-static cudaError_t onesweep_passes(int threads, const SortPlan *plan, uint32_t n, uint32_t n_tiles, uint32_t *status,
-                                   uint32_t *ctr, unsigned int *err, uint32_t spin_limit, uint32_t withhold0,
-                                   cudaStream_t st) {
+// 256-thread tiles take the 3-blocks-per-SM register budget once there are more than four
+// resident blocks' worth of tiles.
+static cudaError_t onesweep_passes(int threads, int num_sms, const SortPlan *plan, uint32_t n, uint32_t n_tiles,
+                                   uint32_t *status, uint32_t *ctr, unsigned int *err, uint32_t spin_limit,
+                                   uint32_t withhold0, cudaStream_t st) {
     const int nw = threads / 32;
     const size_t smem = (size_t)(nw * 256 + 256 + 256 + 32) * sizeof(uint32_t) +
                         (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t));
+    const bool many = threads == 256 && n_tiles > (uint32_t)num_sms * 8u;
     cudaError_t e;
     if (threads == 512) e = cudaFuncSetAttribute(k_onesweep<512, SORT_TILE / 512>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    else if (many) e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, 3>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     else e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem);
     if (e != cudaSuccess) return e;
@@ -544,6 +552,8 @@ static cudaError_t onesweep_passes(int threads, const SortPlan *plan, uint32_t n
         const uint32_t wh = p == 0 ? withhold0 : 0xffffffffu;
         if (threads == 512)
             k_onesweep<512, SORT_TILE / 512><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+        else if (many)
+            k_onesweep<256, SORT_TILE / 256, 3><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
         else
             k_onesweep<256, SORT_TILE / 256><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
     }
@@ -969,7 +979,7 @@ static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &s
     int hb = ctx->num_sms * 2;
     k_hist<<<hb, 256, 0, st>>>(kA, n, hist);
     k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
-    GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
+    GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, ctx->num_sms, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
                                   ctx->withhold_tile, st));
     return GBT_OK;
 }
@@ -1074,7 +1084,7 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
     if (cudaMemsetAsync(err, 0, sizeof(unsigned int), st) != cudaSuccess) return GBT_ECUDA;
     k_hist<<<num_sms * 2, 256, 0, st>>>(codes_in, n, hist);
     k_sort_plan_all<<<1, 256, 0, st>>>(plan, hist, codes_in, codes_out, idx_out, kB, vB);
-    return onesweep_passes(256, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
+    return onesweep_passes(256, num_sms, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
                ? GBT_OK
                : GBT_ECUDA;
 }
