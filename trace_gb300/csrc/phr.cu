@@ -38,7 +38,7 @@ constexpr int WIDE = 512;                // threads per job block on levels of a
 constexpr uint32_t SORT_SMEM_MAX = 8192; // largest padded cut sorted in shared memory (96 KB)
 constexpr int SPEC_LEVELS = 8;           // small-cut levels launched per readback
 #ifndef GBT_PHR_SPEC_BIG
-#define GBT_PHR_SPEC_BIG 1                // levels of larger cuts launched per readback
+#define GBT_PHR_SPEC_BIG 3                // levels of larger cuts launched per readback (branching 2)
 #endif
 constexpr int DEPTH_TABLE = 4096;
 // Cuts of at most this many nodes are swept by a single lane (bf = 2): most
@@ -2107,7 +2107,9 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         // large cuts (the first ones), PT-thread blocks otherwise
         const uint32_t small_cut = (uint32_t)ctx->phr_small_cut;
         const int variant = nmax <= small_cut ? 0 : (n_jobs * 4 <= (uint32_t)ctx->num_sms ? 2 : 1);
-        const int batch = variant == 0 ? SPEC_LEVELS : GBT_PHR_SPEC_BIG;
+        // (with branching 2: 4.57 against 4.67 ms per refinement of the 1M soup; branching 4
+        // measured no faster)
+        const int batch = variant == 0 ? SPEC_LEVELS : (bf == 2 ? GBT_PHR_SPEC_BIG : 1);
         // splits after the first one of a job (bf > 2) sort refined cuts: each refinement at
         // most doubles a cut (binary auxiliary nodes), so bf - 2 of them bound the size
         if (nmax > (1u << 28)) {
@@ -2116,9 +2118,11 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         }
         // levels of larger cuts launched ahead of their readback get twice the largest cut
         // known now (refinement can grow a cut from one level to the next; a level whose
-        // cuts still do not fit flags a stall and is relaunched here)
-        const uint32_t big = batch > 1 && pow2_at_least(2 * nmax) <= SORT_SMEM_MAX ? 2 * nmax : nmax;
-        const uint32_t cap = (variant == 0 ? small_cut : big) << (bf > 2 ? bf - 2 : 0);
+        // cuts still do not fit flags a stall and is relaunched here), unless the headroom
+        // would push the cut's sort out of shared memory
+        const uint32_t shift = bf > 2 ? (uint32_t)(bf - 2) : 0u;
+        const uint32_t big = batch > 1 && pow2_at_least((2 * nmax) << shift) <= SORT_SMEM_MAX ? 2 * nmax : nmax;
+        const uint32_t cap = (variant == 0 ? small_cut : big) << shift;
         const uint32_t sort_p = pow2_at_least(cap > 0 ? cap : 1);
         const size_t dyn = variant != 0 && sort_p <= SORT_SMEM_MAX ? (size_t)sort_p * 12 : 0;
         // grid: at most the blocks that are resident at once
