@@ -18,8 +18,17 @@ Reported:
                48 B per primitive record tested, 32 B ray + 16 B hit per ray)
                per second against the measured HBM copy bandwidth
   cpu_baseline the C restatement of the reference (oracle/) on the host cores,
-               on a bounded sample of the same frame
+               on a bounded sample of the same workload (full frames)
   lbvh         LBVH build Mtri/s on the same scene, with its own roofline
+  phr_build    wall clock of the PHR(0.5, 6, 2) refinement of that LBVH
+  batch        the 64-scene batch (log-uniform 1k-2M triangles, 512x512, 16 spp,
+               depth 4): the per-scene loop, the batched frame in each form and
+               from a CUDA graph, and speedup_batched_vs_plain (same paths, so
+               equal RMSE)
+  adjoint      ms per forward + L2 loss + backward iteration on the 65k-triangle
+               Cornell scene at 512x512, 64 spp
+  terrain      the 8.4M-triangle terrain: LBVH Mtri/s with its roofline, the
+               grid optimiser's PHR parameters, and Mrays/s of the 64 spp render
 
 --impl reference times the reference's CPU path (the C restatement in
 oracle/, since the Go reference cannot be built here) on the same workload.
@@ -392,6 +401,11 @@ def measure_adjoint(args):
 
 
 def run_terrain_workload(args):
+    print(json.dumps(measure_terrain(args)), flush=True)
+    return 0
+
+
+def measure_terrain(args):
     """The 2048x2048 fBm terrain (8,380,418 triangles plus a sun sphere): LBVH build
     Mtri/s with its HBM roofline, the PHR grid optimiser and build, and Mrays/s of the
     1920x1080, 64 spp, MaxDepth 4 render (constant sky 0.5) on the chosen PHR tree.
@@ -457,53 +471,18 @@ def run_terrain_workload(args):
     line = {"metric": "Mrays/s (terrain)", "value": st.rays_traced / frames / ms / 1e3, "unit": "Mrays/s",
             "workload": "terrain2048_1920x1080_spp64_depth4", "triangles": n, "ms_per_frame": ms,
             "rays_per_frame": st.rays_traced / frames, "image_mean": float(img.mean()),
-            "lbvh": {"mtri_s": n / lb_ms / 1e3, "ms": lb_ms,
+            "lbvh": {"mtri_s": n / lb_ms / 1e3, "ms": lb_ms, "steps": steps,
                      "roofline": {"bound": "hbm", "achieved": lb_bw, "peak": hbm, "unit": "GB/s", "frac": lb_bw / hbm,
-                                  "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind}},
+                                  "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind,
+                                  "traffic": LBVH_TRAFFIC_PER_TRI["terrain2048"] * n,
+                                  "traffic_scope": "DRAM bytes of one build (17 launches), ncu cold-cache capture",
+                                  "kernel": "whole build (17 launches)"}},
             "phr": {"alpha": alpha, "delta": delta, "sah_cost": bvh.Cost(), "lbvh_sah_cost": aux.Cost(),
                     "build_s_wall": phr_s, "optimizer_s_wall": opt_s,
                     "grid": [{"alpha": a, "delta": d, "sah": c, "build_cost": b} for a, d, c, b in opt.evaluations]},
             "scene_generation_s": gen_s}
-    print(json.dumps(line), flush=True)
-    return 0
-
-
-def measure_terrain_lbvh(args):
-    """LBVH build throughput on the 2048x2048 fBm terrain (8,380,418 triangles plus its
-    sun sphere): W warm-up rebuilds, then K timed rebuilds (CUDA events on the library's
-    stream).  The scene (2.3 GB on the device) is far larger than L2, so nothing is
-    flushed.  Roofline: LBVH_BYTES_PER_TRI algorithmic bytes against the measured HBM
-    copy bandwidth; traffic is the DRAM bytes of one build from an ncu capture."""
-    import torch
-
-    from trace_gb300 import pt, scenes
-
-    ctx = pt.Context(0)
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    hbm, peak_kind = peaks()
-    s = scenes.terrain(2048)
-    ds = pt.DeviceScene.from_dict(ctx, s)
-    n = ds.n_prim
-    aux = pt.DefaultLBVH(ds)
-    for _ in range(max(1, args.warmup)):
-        ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
-    ctx.sync()
-    steps = max(3, args.steps)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(steps):
-        ctx.check(ctx.L.gbt_lbvh_rebuild_async(ctx.h, aux.h), "rebuild")
-    e1.record(stream)
-    ctx.sync()
-    ms = e0.elapsed_time(e1) / steps
-    bw = n * LBVH_BYTES_PER_TRI / (ms * 1e-3) / 1e9
     ctx.close()
-    return {"workload": "terrain2048_lbvh", "triangles": n, "ms": ms, "mtri_s": n / ms / 1e3, "steps": steps,
-            "roofline": {"bound": "hbm", "achieved": bw, "peak": hbm, "unit": "GB/s", "frac": bw / hbm,
-                         "bytes_per_tri": LBVH_BYTES_PER_TRI, "peak_source": peak_kind,
-                         "traffic": LBVH_TRAFFIC_PER_TRI["terrain2048"] * n,
-                         "traffic_scope": "DRAM bytes of one build (17 launches), ncu cold-cache capture",
-                         "kernel": "whole build (17 launches)"}}
+    return line
 
 
 def run_lbvh_workload(args):
@@ -822,11 +801,11 @@ def main():
     if ws == 1 and not args.no_extras:
         # the metric's other parts, each on its own context after the headline's timed region:
         # the 64-scene batch (batched vs the per-scene loop at equal RMSE), the adjoint's
-        # ms/iter and the terrain LBVH's Mtri/s
+        # ms/iter, and the terrain's LBVH Mtri/s, PHR grid choice and 64 spp render
         ctx.close()
         line["batch"] = measure_batch(args, rebuilds=False)
         line["adjoint"] = measure_adjoint(args)
-        line["terrain_lbvh"] = measure_terrain_lbvh(args)
+        line["terrain"] = measure_terrain(args)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, seconds=args.cpu_seconds)
     if rank == 0:
