@@ -124,3 +124,18 @@ def test_scene_generators_sizes_and_determinism():
     assert scenes.terrain_tris(9).shape == (2 * 8 * 8, 9)
     sz = scenes.batch_sizes()
     assert len(sz) == 64 and sz.min() >= 1000 and sz.max() <= 2_000_000
+
+
+def test_header_compiles_as_c99(tmp_path):
+    """include/gbtrace.h is what a cgo binding includes: it must be plain C."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "hdr.c"
+    src.write_text('#include "gbtrace.h"\nint main(void) { gbt_ctx *c = 0; (void)c; return GBT_OK; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        "-c", str(src), "-o", str(tmp_path / "hdr.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
