@@ -6,7 +6,7 @@
 //   k_morton     fp64 quantisation + bit interleave       (lbvh.go:64-73, morton.go:6-20)
 //   k_hist, k_sort_plan, k_onesweep x8
 //                stable LSD radix sort of (code, index)   (lbvh.go:216-301 bucket sort)
-//   k_rle        runs of equal codes -> leaves            (lbvh.go:134-145, 179-181)
+//   k_rle_*      runs of equal codes -> leaves            (lbvh.go:134-145, 179-181)
 //   k_emit       primitive records in leaf order, and the binary radix tree
 //                over the distinct codes with the bottom-up box refit fused
 //                in                                       (lbvh.go:76-203, bvh.go:104-126,201-222)
@@ -569,75 +569,88 @@ __device__ __forceinline__ bool run_start_at(const uint64_t *__restrict__ k, uin
     return i < n && (i == 0 || k[i] != k[i - 1]);
 }
 
-// Runs of equal codes in one pass over the sorted keys.  Each tile of RLE_TILE
-// keys, taken in order from a counter, counts its run starts, publishes the
-// count, looks back over the earlier tiles for its offset (bounded waits, as in
-// the sort) and writes the first position and the code of each of its runs.
-// The tile holding the last key also writes the end marker run[U] = n and the
-// header's distinct-code count U.
-__global__ void __launch_bounds__(RLE_THREADS) k_rle(const SortPlan *__restrict__ plan, uint32_t n,
-                                                     uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
-                                                     uint32_t *__restrict__ run, uint64_t *__restrict__ ukey,
-                                                     BvhHeader *hdr, unsigned int *err, uint32_t spin_limit) {
-    constexpr int NW = RLE_THREADS / 32;
-    __shared__ uint32_t s_off[RLE_ITEMS][NW];  // run starts before (round, warp), within the tile
-    __shared__ uint32_t s_tile, s_fail, s_total, s_prefix;
-    if (threadIdx.x == 0) {
-        s_fail = sort_failed(err) ? 1u : 0u;
-        s_tile = atomicAdd(tile_ctr, 1u);
-    }
+__global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__restrict__ plan, uint32_t n,
+                                                           uint32_t *__restrict__ tile_cnt, const unsigned int *err) {
+    if (sort_failed(err)) return;
+    const uint64_t *k = plan->final_k;
+    uint32_t base = blockIdx.x * RLE_TILE, c = 0;
+#pragma unroll
+    for (int i = 0; i < RLE_ITEMS; i++) c += run_start_at(k, base + i * RLE_THREADS + threadIdx.x, n);
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ uint32_t s[8];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = c;
     __syncthreads();
-    if (s_fail) return;
-    const uint32_t tile = s_tile, base = tile * RLE_TILE;
-    const uint64_t *__restrict__ k = plan->final_k;
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int j = 0; j < 8; j++) t += s[j];
+        tile_cnt[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t n_tiles, BvhHeader *hdr,
+                                                   const unsigned int *err) {
+    if (sort_failed(err)) return;
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t ball[RLE_ITEMS];
+    for (uint32_t b = 0; b < n_tiles; b += 1024) {
+        uint32_t i = b + threadIdx.x;
+        uint32_t v = i < n_tiles ? tile_cnt[i] : 0u, x = v;
 #pragma unroll
-    for (int i = 0; i < RLE_ITEMS; i++) {
-        ball[i] = __ballot_sync(0xffffffffu, run_start_at(k, base + i * RLE_THREADS + threadIdx.x, n));
-        if (lane == 0) s_off[i][w] = __popc(ball[i]);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int i = 0; i < RLE_ITEMS; i++)
-            for (int v = 0; v < NW; v++) {
-                const uint32_t c = s_off[i][v];
-                s_off[i][v] = acc;
-                acc += c;
-            }
-        s_total = acc;
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            st_relaxed(&status[0], ST_PREFIX | acc);
-        } else {
-            st_relaxed(&status[tile], ST_AGG | acc);
-            for (int j = (int)tile - 1; j >= 0; --j) {
-                const uint32_t sj = lookback_wait(&status[j], err, spin_limit);
-                prefix += sj & ST_VALUE;
-                if ((sj & ST_FLAGS) == ST_PREFIX) break;
-            }
-            st_relaxed(&status[tile], ST_PREFIX | (prefix + acc));
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        s_prefix = prefix;
+        if (lane == 31) s_w[w] = x;
+        __syncthreads();
+        uint32_t off = s_carry, tot = 0;
+        for (int j = 0; j < 32; j++) {
+            off += (j < w) ? s_w[j] : 0u;
+            tot += s_w[j];
+        }
+        if (i < n_tiles) tile_cnt[i] = off + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
     }
-    __syncthreads();
+    if (threadIdx.x == 0) {
+        hdr->n_unique = s_carry;
+        hdr->n_nodes = s_carry > 0 ? s_carry - 1 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(RLE_THREADS) k_rle_write(const SortPlan *__restrict__ plan, uint32_t n,
+                                                           const uint32_t *__restrict__ tile_off,
+                                                           uint32_t *__restrict__ run, uint64_t *__restrict__ ukey,
+                                                           const unsigned int *err) {
+    if (sort_failed(err)) return;
+    const uint64_t *k = plan->final_k;
+    __shared__ uint32_t s_w[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
-#pragma unroll
+    uint32_t base = blockIdx.x * RLE_TILE, carry = tile_off[blockIdx.x];
     for (int i = 0; i < RLE_ITEMS; i++) {
-        const uint32_t idx = base + i * RLE_THREADS + threadIdx.x;
-        const uint32_t f = (ball[i] >> lane) & 1u;
-        const uint32_t u = s_prefix + s_off[i][w] + __popc(ball[i] & lt);
+        uint32_t idx = base + i * RLE_THREADS + threadIdx.x;
+        bool f = run_start_at(k, idx, n);
+        uint32_t b = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_w[w] = __popc(b);
+        __syncthreads();
+        uint32_t off = carry, tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            off += (j < w) ? s_w[j] : 0u;
+            tot += s_w[j];
+        }
         if (f) {
+            uint32_t u = off + __popc(b & lt);
             run[u] = idx;
             ukey[u] = k[idx];
         }
-        if (idx == n - 1) {  // the last key: U distinct codes in all
-            const uint32_t U = u + f;
-            run[U] = n;
-            hdr->n_unique = U;
-            hdr->n_nodes = U > 0 ? U - 1 : 0;
-        }
+        if (idx == n - 1) run[off + __popc(b & lt) + (f ? 1u : 0u)] = n;
+        carry += tot;
+        __syncthreads();
     }
 }
 
@@ -998,10 +1011,10 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     if (rc) return rc;
     const SortPlan *plan = reinterpret_cast<const SortPlan *>(sb + ss.plan);
     uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
-    uint32_t *rstat = reinterpret_cast<uint32_t *>(sb + rle_off);  // rt look-back words, then the tile counter
-    GBT_CUDA(ctx, cudaMemsetAsync(rstat, 0, (size_t)(rt + 1) * sizeof(uint32_t), st));
-    k_rle<<<rt, RLE_THREADS, 0, st>>>(plan, n, rstat, rstat + rt, bvh->d_run, bvh->d_ukey, bvh->d_hdr, ctx->d_error,
-                                      ctx->spin_limit);
+    uint32_t *tcnt = reinterpret_cast<uint32_t *>(sb + rle_off);
+    k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, ctx->d_error);
+    k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr, ctx->d_error);
+    k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey, ctx->d_error);
     uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
     EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
     const uint32_t eb = emit_blocks(n);
