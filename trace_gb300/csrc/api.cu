@@ -120,8 +120,6 @@ extern "C" int gbt_ctx_create(int device, gbt_ctx **out) {
     if (const char *t = std::getenv("GBT_PRIMARY_TILES")) c->primary_tiles = std::strcmp(t, "0") != 0;
     if (const char *t = std::getenv("GBT_PRIMARY_PACKETS")) c->primary_packets = std::atoi(t) < 0 ? 0 : std::atoi(t) > 2 ? 2 : std::atoi(t);
     if (const char *t = std::getenv("GBT_SORT_THREADS")) c->sort_threads = std::atoi(t) == 512 ? 512 : 256;
-    if (const char *t = std::getenv("GBT_SORT_ORMASK")) c->sort_ormask = std::strcmp(t, "0") != 0;
-    if (const char *t = std::getenv("GBT_MORTON_HIST")) c->morton_hist = std::strcmp(t, "0") != 0;
     *out = c;
     return GBT_OK;
 }

@@ -76,8 +76,6 @@ struct gbt_ctx {
     uint32_t spin_limit = GBT_SPIN_LIMIT;
     // threads per tile of the LBVH sort's passes: 256 (16 keys each) or 512 (8 keys each)
     int sort_threads = 256;
-    int sort_ormask = 0;
-    int morton_hist = 0;  // 1: the Morton kernel also builds the sort's digit histograms (GBT_MORTON_HIST)  // 1: the sort ranks keys with shared-memory lane masks (GBT_SORT_ORMASK)
     uint32_t withhold_tile = 0xffffffffu;
     uint32_t collapse_cap = 0;
 };

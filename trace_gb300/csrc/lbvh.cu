@@ -206,17 +206,11 @@ __device__ __forceinline__ uint64_t quantise(double dx, double step, double rste
     return (uint64_t)__double2ull_rz(q);
 }
 
-// HIST: also the digit histograms of the sort's eight passes (the work of k_hist, from
-// the codes in registers), in shared memory per block and then added to ghist.
-template <bool HIST = false>
 __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts, const float4 *__restrict__ sph,
                                                 uint32_t n_tri, uint32_t n, const unsigned long long *__restrict__ acc,
-                                                uint64_t *__restrict__ codes, uint32_t *__restrict__ ghist = nullptr) {
+                                                uint64_t *__restrict__ codes) {
     __shared__ double s_e[9];  // lo.xyz, step.xyz, 1/step.xyz
     __shared__ float s_f[15];  // lo.xyz and 1/step.xyz as float pairs, margin.xyz
-    __shared__ uint32_t s_h[HIST ? 8 * 256 : 1];
-    if constexpr (HIST)
-        for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) s_h[i] = 0;
     if (threadIdx.x < 3) {
         int k = threadIdx.x;
         double lo = ord_to_dbl(acc[k]), hi = ord_to_dbl(acc[3 + k]);
@@ -261,17 +255,7 @@ __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts,
                 q[k] = quantise(dx, s_e[3 + k], s_e[6 + k]);
             }
         }
-        const uint64_t code = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
-        codes[i] = code;
-        if constexpr (HIST) {
-#pragma unroll
-            for (int p = 0; p < 8; p++) atomicAdd(&s_h[p * 256 + (uint32_t)((code >> (8 * p)) & 255u)], 1u);
-        }
-    }
-    if constexpr (HIST) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
-            if (s_h[i]) atomicAdd(&ghist[i], s_h[i]);
+        codes[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
     }
 }
 
@@ -423,9 +407,7 @@ __device__ __forceinline__ bool sort_failed(const unsigned int *err) {
 // MINB: resident blocks per SM the registers are sized for.  3 (80 registers) is faster for
 // sorts of many tiles (the 8.4M terrain: 1.622 against 1.642 ms a build) and slower for
 // sorts of about one wave (the 1M soup: 0.376 against 0.367 ms).
-// ORMASK: the lanes sharing a digit from a shared-memory word per digit that every lane
-// ORs its bit into, instead of one ballot per digit bit.
-template <int T, int I, int MINB = 2, bool ORMASK = false>
+template <int T, int I, int MINB = 2>
 __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict__ plan, int pass, uint32_t n,
                                                  uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr,
                                                  unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
@@ -439,7 +421,7 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
     uint32_t *s_misc = s_gbase + 256;                        // [32]
     uint64_t *s_keys = reinterpret_cast<uint64_t *>(s_misc + 32);
     uint32_t *s_vals = reinterpret_cast<uint32_t *>(s_keys + SORT_TILE);
-    uint32_t *s_mask = s_vals + SORT_TILE;  // ORMASK: [NW][257] lane masks per digit (257: past the end)
+    uint32_t *s_mask = s_vals + SORT_TILE;  // [NW][257] lane masks per digit (digit 256: past the end)
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
@@ -447,8 +429,7 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
         s_misc[16] = atomicAdd(&tile_ctr[pass], 1u);
     }
     for (int i = tid; i < NW * 256; i += T) s_wh[i] = 0;
-    if constexpr (ORMASK)
-        for (int i = tid; i < NW * 257; i += T) s_mask[i] = 0;
+    for (int i = tid; i < NW * 257; i += T) s_mask[i] = 0;
     __syncthreads();
     if (s_misc[17]) return;
     const uint32_t tile = s_misc[16];
@@ -476,26 +457,18 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
         uint32_t d = ok ? (uint32_t)((k[i] >> shift) & 255u) : 256u;
         // lanes with the same digit, from one vote per digit bit (valid lanes only; ranking by
         // __match_any_sync measured slower)
-        uint32_t peers;
-        if constexpr (ORMASK) {
-            uint32_t *mk = s_mask + warp * 257;
-            atomicOr(&mk[d], 1u << lane);
-            __syncwarp();
-            peers = mk[d];
-        } else {
-            peers = __ballot_sync(0xffffffffu, ok);
-#pragma unroll
-            for (int b = 0; b < 8; b++) {
-                const uint32_t vb = __ballot_sync(0xffffffffu, (d >> b) & 1u);
-                peers &= ((d >> b) & 1u) ? vb : ~vb;
-            }
-        }
+        // the lanes with the same digit: each lane ORs its bit into its digit's word of the
+        // warp's masks and reads the word back (one ballot per digit bit measured 4% slower
+        // for the whole build); the group's leader clears the word for the next round
+        uint32_t *mk = s_mask + warp * 257;
+        atomicOr(&mk[d], 1u << lane);
+        __syncwarp();
+        const uint32_t peers = mk[d];
         uint32_t base = ok ? wh[d] : 0u;
         __syncwarp();
         const bool leader = lane == (uint32_t)(__ffs(peers) - 1);
         if (ok && leader) wh[d] = base + __popc(peers);
-        if constexpr (ORMASK)
-            if (leader) s_mask[warp * 257 + d] = 0;  // every lane of the group has read it
+        if (leader) mk[d] = 0;  // every lane of the group has read it
         __syncwarp();
         rk[i] = base + __popc(peers & lt);
     }
@@ -566,19 +539,14 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
 // resident blocks' worth of tiles.
 static cudaError_t onesweep_passes(int threads, int num_sms, const SortPlan *plan, uint32_t n, uint32_t n_tiles,
                                    uint32_t *status, uint32_t *ctr, unsigned int *err, uint32_t spin_limit,
-                                   uint32_t withhold0, cudaStream_t st, bool ormask = false) {
+                                   uint32_t withhold0, cudaStream_t st) {
     const int nw = threads / 32;
     const size_t smem = (size_t)(nw * 256 + 256 + 256 + 32) * sizeof(uint32_t) +
-                        (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t)) +
-                        (ormask ? (size_t)nw * 257 * sizeof(uint32_t) : 0);
+                        (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)nw * 257 * sizeof(uint32_t);
     const bool many = threads == 256 && n_tiles > (uint32_t)num_sms * 8u;
     cudaError_t e;
     if (threads == 512) e = cudaFuncSetAttribute(k_onesweep<512, SORT_TILE / 512>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    else if (ormask && many) e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, 3, true>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    else if (ormask) e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, 2, true>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     else if (many) e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256, 3>,
                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     else e = cudaFuncSetAttribute(k_onesweep<256, SORT_TILE / 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -589,10 +557,6 @@ static cudaError_t onesweep_passes(int threads, int num_sms, const SortPlan *pla
         const uint32_t wh = p == 0 ? withhold0 : 0xffffffffu;
         if (threads == 512)
             k_onesweep<512, SORT_TILE / 512><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
-        else if (ormask && many)
-            k_onesweep<256, SORT_TILE / 256, 3, true><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
-        else if (ormask)
-            k_onesweep<256, SORT_TILE / 256, 2, true><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
         else if (many)
             k_onesweep<256, SORT_TILE / 256, 3><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
         else
@@ -1009,24 +973,18 @@ size_t gbt_lbvh_scratch_bytes(uint32_t n) {
     return lbvh_scratch_layout(n, &a, &s, &r);
 }
 
-// hist_ready: the digit histograms are already in the scratch (k_morton<true> made them).
 static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &ss, uint64_t *kA, uint32_t *vA,
-                        uint64_t *kB, uint32_t *vB, uint32_t n, int identity_vals, BvhHeader *hdr,
-                        bool hist_ready = false) {
+                        uint64_t *kB, uint32_t *vB, uint32_t n, int identity_vals, BvhHeader *hdr) {
     cudaStream_t st = ctx->stream;
     SortPlan *plan = reinterpret_cast<SortPlan *>(sbase + ss.plan);
     uint32_t *hist = reinterpret_cast<uint32_t *>(sbase + ss.hist);
     uint32_t *ctr = reinterpret_cast<uint32_t *>(sbase + ss.ctr);
     uint32_t *status = reinterpret_cast<uint32_t *>(sbase + ss.status);
-    if (hist_ready) {
-        GBT_CUDA(ctx, cudaMemsetAsync(sbase + ss.ctr, 0, ss.total - ss.ctr, st));
-    } else {
-        GBT_CUDA(ctx, cudaMemsetAsync(sbase + ss.hist, 0, ss.total - ss.hist, st));
-        k_hist<<<ctx->num_sms * 2, 256, 0, st>>>(kA, n, hist);
-    }
+    GBT_CUDA(ctx, cudaMemsetAsync(sbase + ss.hist, 0, ss.total - ss.hist, st));
+    k_hist<<<ctx->num_sms * 2, 256, 0, st>>>(kA, n, hist);
     k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
     GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, ctx->num_sms, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
-                                  ctx->withhold_tile, st, ctx->sort_ormask != 0));
+                                  ctx->withhold_tile, st));
     return GBT_OK;
 }
 
@@ -1052,15 +1010,8 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     // the scene box: each block ends with six atomics on the same six words
     const int gb = std::min(grid, ctx->num_sms * GBT_BOUNDS_BLOCKS_PER_SM);
     k_bounds<<<gb, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc);
-    if (ctx->morton_hist) {  // the histograms from the codes in k_morton's registers (no k_hist pass)
-        GBT_CUDA(ctx, cudaMemsetAsync(sb + ss.hist, 0, 8 * 256 * sizeof(uint32_t), st));
-        k_morton<true><<<std::min(grid, ctx->num_sms * 2), 256, 0, st>>>(
-            sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes, reinterpret_cast<uint32_t *>(sb + ss.hist));
-    } else {
-        k_morton<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes);
-    }
-    rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr,
-                      ctx->morton_hist != 0);
+    k_morton<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes);
+    rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr);
     if (rc) return rc;
     const SortPlan *plan = reinterpret_cast<const SortPlan *>(sb + ss.plan);
     uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
