@@ -736,7 +736,15 @@ def main():
             "nodes_per_ray": count_stats["nodes_visited"] / rays_per_frame,
             "prims_per_ray": count_stats["prims_tested"] / rays_per_frame,
             "note": "bytes counted at the node/record level; most are L1/L2 hits, so frac can exceed 1; "
-                    "camera rays run as 32-ray packets whose node and record fetches count once per warp"}
+                    "camera rays run as 32-ray packets whose node and record fetches count once per warp",
+            # Static figures from one ncu --set full capture of the two traversal
+            # kernels on the PHR(0.5,6,2) tree of the 1M soup (not measured by this run).
+            "cache_profile": {
+                "source": "profiles/traversal_kernels_soup1M_phr.md (ncu --set full)",
+                "l2_throughput_pct": {"camera_packets": 1.5, "anyhit_bounce": 16.4},
+                "l1_hit_pct": {"camera_packets": 54.0, "anyhit_bounce": 17.1},
+                "l2_hit_pct": {"camera_packets": 51.1, "anyhit_bounce": 93.5},
+                "warp_efficiency": {"camera_packets": 0.93, "anyhit_bounce": 0.28}}}
     ctx.check(L.gbt_ctx_set_profiling(h, 0))
 
     # e2e: the C-ABI call with a pinned host image, device->host copy inside the timed region
