@@ -73,54 +73,27 @@ __global__ void __launch_bounds__(128) k_trace4(const BvhHeader *__restrict__ hd
     flush_work<COUNT>(w, counters);
 }
 
-// Packet traversal of a 4-wide tree for coherent rays (camera rays of one 8x4
-// pixel tile per warp): the warp walks one node sequence with a stack in shared
-// memory; each lane tests every child box against its own ray and closest hit,
-// the children that any lane hits are taken nearest first by the warp's
-// smallest entry distance, and a popped entry is skipped when no lane can
-// still reach it.  Control flow is uniform across the warp.  Each lane keeps
-// its own closest hit, so the hits equal the single-ray kernels' (exact ties
-// go to the lower record whatever the order).  Counters (profiling level 2)
-// count the warp's node fetches and leaf visits.
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restrict__ hdr,
-                                                       const float4 *__restrict__ nodes, const float4 *__restrict__ recs,
-                                                       const float4 *__restrict__ rays, float4 *__restrict__ hits,
-                                                       uint32_t n, int out_mode, unsigned int *err,
-                                                       unsigned long long *counters) {
+// 1: packet warps whose rays share an octant run the loop instantiated for it.
+#ifndef GBT_PACKET_OCT
+#define GBT_PACKET_OCT 1
+#endif
+
+// The node loop of k_trace_packet4 from `node` on: the warp's stack is se/st in
+// shared memory.  OCT in 0..7 when every ray of the warp lies in that octant
+// (the slab tests then pick planes by sign), -1 otherwise.
+template <bool COUNT, int OCT>
+__device__ __forceinline__ void packet4_loop(int2 node, const float4 *__restrict__ nodes,
+                                             const float4 *__restrict__ recs, const gbt_dev::Ray &r, gbt_dev::Hit &h,
+                                             int2 *se, float *st, int lane, unsigned int *err, gbt_dev::Work &w) {
     constexpr int PSTACK = 96;
     constexpr uint32_t FULL = 0xffffffffu;
-    __shared__ int2 s_e[4][PSTACK];
-    __shared__ float s_t[4][PSTACK];
-    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t id = blockIdx.x * 128 + threadIdx.x;
-    const bool live = id < n;
-    gbt_dev::Work w;
-    gbt_dev::Ray r;
-    if (live) {
-        r = gbt_dev::load_ray(rays, id);
-    } else {  // a ray that hits nothing keeps the lane in step
-        r.o = make_float3(0.f, 0.f, 0.f);
-        r.d = make_float3(1.f, 1.f, 1.f);
-        r.tmin = 1.f;
-        r.tmax = 0.f;
-        gbt_dev::finish_ray(r);
-    }
-    gbt_dev::Hit h;
-    h.t = r.tmax;
-    h.u = h.v = 0.f;
-    h.rec = -1;
     const float MISS = __int_as_float(0x7f800000);
-    float te;
-    const bool root_hit = gbt_dev::slab(hdr->root_lo[0], hdr->root_lo[1], hdr->root_lo[2], hdr->root_hi[0],
-                                        hdr->root_hi[1], hdr->root_hi[2], r, h.t, te);
-    int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
     int sp = 0;
     auto pop = [&]() -> int2 {
         while (sp > 0) {
             --sp;
-            const float t = s_t[wp][sp];
-            const int2 e = s_e[wp][sp];
+            const float t = st[sp];
+            const int2 e = se[sp];
             if (__any_sync(FULL, t <= h.t * 1.0000005f)) return e;
         }
         return make_int2(0, -1);
@@ -136,10 +109,10 @@ __global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restri
             gbt_dev::ldg256(nd + 6, rff, cnf);
             float t;
             // per lane entry distance (+0 for -0, so that unsigned min orders them), MISS if missed
-            const float t0 = (__float_as_int(cnf.x) >= 0 && gbt_dev::slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) ? t + 0.f : MISS;
-            const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
-            const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
-            const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
+            const float t0 = (__float_as_int(cnf.x) >= 0 && gbt_dev::slab_sel<OCT>(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) ? t + 0.f : MISS;
+            const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab_sel<OCT>(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
+            const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab_sel<OCT>(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
+            const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab_sel<OCT>(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
             gbt_dev::Cand c0, c1, c2, c3;
             c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
             c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
@@ -164,9 +137,9 @@ __global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restri
             } else {
                 if (lane == 0) {
                     int q = sp;
-                    if (c3.t != MISS) { s_e[wp][q] = c3.e; s_t[wp][q] = c3.t; ++q; }
-                    if (c2.t != MISS) { s_e[wp][q] = c2.e; s_t[wp][q] = c2.t; ++q; }
-                    if (c1.t != MISS) { s_e[wp][q] = c1.e; s_t[wp][q] = c1.t; ++q; }
+                    if (c3.t != MISS) { se[q] = c3.e; st[q] = c3.t; ++q; }
+                    if (c2.t != MISS) { se[q] = c2.e; st[q] = c2.t; ++q; }
+                    if (c1.t != MISS) { se[q] = c1.e; st[q] = c1.t; ++q; }
                 }
                 sp += np;
                 __syncwarp();
@@ -179,6 +152,66 @@ __global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restri
         } else {
             break;
         }
+    }
+}
+
+// Packet traversal of a 4-wide tree for coherent rays (camera rays of one 8x4
+// pixel tile per warp): the warp walks one node sequence with a stack in shared
+// memory; each lane tests every child box against its own ray and closest hit,
+// the children that any lane hits are taken nearest first by the warp's
+// smallest entry distance, and a popped entry is skipped when no lane can
+// still reach it.  Control flow is uniform across the warp.  Each lane keeps
+// its own closest hit, so the hits equal the single-ray kernels' (exact ties
+// go to the lower record whatever the order).  A warp whose rays share one
+// octant (almost every tile of a pinhole camera) runs the loop instantiated
+// for that octant.  Counters (profiling level 2) count the warp's node
+// fetches and leaf visits.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restrict__ hdr,
+                                                       const float4 *__restrict__ nodes, const float4 *__restrict__ recs,
+                                                       const float4 *__restrict__ rays, float4 *__restrict__ hits,
+                                                       uint32_t n, int out_mode, unsigned int *err,
+                                                       unsigned long long *counters) {
+    constexpr int PSTACK = 96;
+    constexpr uint32_t FULL = 0xffffffffu;
+    __shared__ int2 s_e[4][PSTACK];
+    __shared__ float s_t[4][PSTACK];
+    const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t id = blockIdx.x * 128 + threadIdx.x;
+    const bool live = id < n;
+    gbt_dev::Work w;
+    gbt_dev::Ray r;
+    if (live) {
+        r = gbt_dev::load_ray(rays, id);
+    } else {  // a ray that hits nothing keeps the lane in step (tmin > tmax: every slab test fails)
+        r.o = make_float3(0.f, 0.f, 0.f);
+        r.d = make_float3(1.f, 1.f, 1.f);
+        r.tmin = 1.f;
+        r.tmax = 0.f;
+        gbt_dev::finish_ray(r);
+    }
+    gbt_dev::Hit h;
+    h.t = r.tmax;
+    h.u = h.v = 0.f;
+    h.rec = -1;
+    float te;
+    const bool root_hit = gbt_dev::slab(hdr->root_lo[0], hdr->root_lo[1], hdr->root_lo[2], hdr->root_hi[0],
+                                        hdr->root_hi[1], hdr->root_hi[2], r, h.t, te);
+    const int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
+    const uint32_t octs = __reduce_or_sync(FULL, live ? 1u << gbt_dev::octant(r) : 0u);
+    const int oct = GBT_PACKET_OCT && __popc(octs) == 1 ? __ffs(octs) - 1 : -1;
+    int2 *se = s_e[wp];
+    float *st = s_t[wp];
+    switch (oct) {
+        case 0: packet4_loop<COUNT, 0>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 1: packet4_loop<COUNT, 1>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 2: packet4_loop<COUNT, 2>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 3: packet4_loop<COUNT, 3>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 4: packet4_loop<COUNT, 4>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 5: packet4_loop<COUNT, 5>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 6: packet4_loop<COUNT, 6>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        case 7: packet4_loop<COUNT, 7>(node, nodes, recs, r, h, se, st, lane, err, w); break;
+        default: packet4_loop<COUNT, -1>(node, nodes, recs, r, h, se, st, lane, err, w); break;
     }
     if (live) gbt_dev::store_hit(hits, id, h, recs, out_mode);
     flush_work<COUNT>(w, counters);

@@ -72,6 +72,39 @@ __device__ __forceinline__ bool slab(float lx, float ly, float lz, float hx, flo
     return tn <= tf * 1.0000005f;
 }
 
+// The direction signs of a ray as three bits (bit a set: negative along axis a),
+// read from the reciprocal, whose sign finish_ray fixes also for zero components.
+__device__ __forceinline__ uint32_t octant(const Ray &r) {
+    return (__float_as_uint(r.inv.x) >> 31) | ((__float_as_uint(r.inv.y) >> 31) << 1) |
+           ((__float_as_uint(r.inv.z) >> 31) << 2);
+}
+
+// slab() for a ray whose octant is OCT, known at compile time: on each axis the
+// near and far planes are picked by the sign instead of ordered by min/max.
+// For a box with lo <= hi and finite distances the entry distance and the
+// answer equal slab()'s, since the rounded products keep the order of the planes.
+template <int OCT>
+__device__ __forceinline__ bool slab_oct(float lx, float ly, float lz, float hx, float hy, float hz, const Ray &r,
+                                         float tmax, float &tenter) {
+    const float tnx = fmaf((OCT & 1) ? hx : lx, r.inv.x, -r.oi.x), tfx = fmaf((OCT & 1) ? lx : hx, r.inv.x, -r.oi.x);
+    const float tny = fmaf((OCT & 2) ? hy : ly, r.inv.y, -r.oi.y), tfy = fmaf((OCT & 2) ? ly : hy, r.inv.y, -r.oi.y);
+    const float tnz = fmaf((OCT & 4) ? hz : lz, r.inv.z, -r.oi.z), tfz = fmaf((OCT & 4) ? lz : hz, r.inv.z, -r.oi.z);
+    const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+    const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+    tenter = tn;
+    return tn <= tf * 1.0000005f;
+}
+
+// slab() or, for OCT in 0..7, slab_oct<OCT>().
+template <int OCT>
+__device__ __forceinline__ bool slab_sel(float lx, float ly, float lz, float hx, float hy, float hz, const Ray &r,
+                                         float tmax, float &tenter) {
+    if constexpr (OCT < 0)
+        return slab(lx, ly, lz, hx, hy, hz, r, tmax, tenter);
+    else
+        return slab_oct<OCT>(lx, ly, lz, hx, hy, hz, r, tmax, tenter);
+}
+
 // Moeller-Trumbore (primitive.go:172-208) on record s; narrows h on a hit.
 __device__ __forceinline__ void test_record(const float4 *__restrict__ recs, int s, const Ray &r, Hit &h) {
     const float4 *p = recs + 3 * (size_t)s;
