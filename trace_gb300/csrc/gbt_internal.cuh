@@ -173,6 +173,38 @@ int gbt_scratch(gbt_ctx *ctx, size_t bytes, void **out);
 static inline size_t gbt_align(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch (sm_90 and later).  A kernel launched with
+// gbt_launch_pdl may be scheduled while the kernel before it in the stream is
+// still running: its blocks start once every block of that kernel has started
+// (or called gbt_pdl_trigger), then gbt_pdl_wait() holds them until that
+// kernel has completed and its writes are visible.  Such a kernel calls
+// gbt_pdl_wait() first, on every path, so that its own completion still
+// implies its predecessors' (the next kernel's wait relies on it).  Without
+// the launch attribute the wait returns at once.
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ void gbt_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void gbt_pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// pdl false: an ordinary launch.
+template <typename... KArgs, typename... Args>
+static inline cudaError_t gbt_launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                         cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+#endif
+
+// ---------------------------------------------------------------------------
 // entry points between translation units
 // ---------------------------------------------------------------------------
 // lbvh.cu

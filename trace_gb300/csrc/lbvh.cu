@@ -209,6 +209,8 @@ __device__ __forceinline__ uint64_t quantise(double dx, double step, double rste
 __global__ void __launch_bounds__(256) k_morton(const float *__restrict__ verts, const float4 *__restrict__ sph,
                                                 uint32_t n_tri, uint32_t n, const unsigned long long *__restrict__ acc,
                                                 uint64_t *__restrict__ codes) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     __shared__ double s_e[9];  // lo.xyz, step.xyz, 1/step.xyz
     __shared__ float s_f[15];  // lo.xyz and 1/step.xyz as float pairs, margin.xyz
     if (threadIdx.x < 3) {
@@ -294,6 +296,8 @@ SortScratch sort_layout(uint32_t n, size_t base) {
 
 // One read of the keys builds the digit histograms of all eight passes.
 __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys, uint32_t n, uint32_t *__restrict__ ghist) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     __shared__ uint32_t h[8 * 256];
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
@@ -336,6 +340,8 @@ __device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t *s_t
 __global__ void __launch_bounds__(256) k_sort_plan(SortPlan *plan, const uint32_t *__restrict__ ghist, uint32_t n,
                                                    uint64_t *kA, uint32_t *vA, uint64_t *kB, uint32_t *vB,
                                                    int identity_vals, BvhHeader *hdr) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     __shared__ uint32_t s_tmp[8];
     __shared__ uint32_t s_active[8];
     const int t = threadIdx.x;
@@ -413,6 +419,8 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
                                                  unsigned int *err, uint32_t spin_limit, uint32_t withhold_tile) {
     static_assert(T * I == SORT_TILE && T >= 256 && T % 32 == 0, "tile shape");
     constexpr int NW = T / 32;
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (!plan->active[pass]) return;
     extern __shared__ __align__(16) unsigned char smem[];
     uint32_t *s_wh = reinterpret_cast<uint32_t *>(smem);  // [NW][256]
@@ -539,7 +547,7 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
 // resident blocks' worth of tiles.
 static cudaError_t onesweep_passes(int threads, int num_sms, const SortPlan *plan, uint32_t n, uint32_t n_tiles,
                                    uint32_t *status, uint32_t *ctr, unsigned int *err, uint32_t spin_limit,
-                                   uint32_t withhold0, cudaStream_t st) {
+                                   uint32_t withhold0, cudaStream_t st, bool pdl) {
     const int nw = threads / 32;
     const size_t smem = (size_t)(nw * 256 + 256 + 256 + 32) * sizeof(uint32_t) +
                         (size_t)SORT_TILE * (sizeof(uint64_t) + sizeof(uint32_t)) + (size_t)nw * 257 * sizeof(uint32_t);
@@ -556,11 +564,15 @@ static cudaError_t onesweep_passes(int threads, int num_sms, const SortPlan *pla
         uint32_t *sp = status + (size_t)p * n_tiles * 256;
         const uint32_t wh = p == 0 ? withhold0 : 0xffffffffu;
         if (threads == 512)
-            k_onesweep<512, SORT_TILE / 512><<<n_tiles, 512, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+            e = gbt_launch_pdl(pdl, k_onesweep<512, SORT_TILE / 512>, n_tiles, 512, smem, st, plan, p, n, sp, ctr, err,
+                               spin_limit, wh);
         else if (many)
-            k_onesweep<256, SORT_TILE / 256, 3><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+            e = gbt_launch_pdl(pdl, k_onesweep<256, SORT_TILE / 256, 3>, n_tiles, 256, smem, st, plan, p, n, sp, ctr, err,
+                               spin_limit, wh);
         else
-            k_onesweep<256, SORT_TILE / 256><<<n_tiles, 256, smem, st>>>(plan, p, n, sp, ctr, err, spin_limit, wh);
+            e = gbt_launch_pdl(pdl, k_onesweep<256, SORT_TILE / 256>, n_tiles, 256, smem, st, plan, p, n, sp, ctr, err,
+                               spin_limit, wh);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
@@ -576,6 +588,8 @@ __device__ __forceinline__ bool run_start_at(const uint64_t *__restrict__ k, uin
 
 __global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__restrict__ plan, uint32_t n,
                                                            uint32_t *__restrict__ tile_cnt, const unsigned int *err) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (sort_failed(err)) return;
     const uint64_t *k = plan->final_k;
     uint32_t base = blockIdx.x * RLE_TILE, c = 0;
@@ -594,6 +608,8 @@ __global__ void __launch_bounds__(RLE_THREADS) k_rle_count(const SortPlan *__res
 
 __global__ void __launch_bounds__(1024) k_rle_scan(uint32_t *tile_cnt, uint32_t n_tiles, BvhHeader *hdr,
                                                    const unsigned int *err) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (sort_failed(err)) return;
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
@@ -630,6 +646,8 @@ __global__ void __launch_bounds__(RLE_THREADS) k_rle_write(const SortPlan *__res
                                                            const uint32_t *__restrict__ tile_off,
                                                            uint32_t *__restrict__ run, uint64_t *__restrict__ ukey,
                                                            const unsigned int *err) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (sort_failed(err)) return;
     const uint64_t *k = plan->final_k;
     __shared__ uint32_t s_w[8];
@@ -763,6 +781,8 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
                                                        unsigned int *err, const SortPlan *__restrict__ plan,
                                                        const float *__restrict__ verts, const float4 *__restrict__ sph,
                                                        uint32_t n_tri) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (sort_failed(err)) return;
     constexpr int B = EMIT_THREADS, NW = B / 32;
     // s_d[i]: common prefix length at the split k0-1+i | k0+i (i = 0..B), -1 past
@@ -912,6 +932,8 @@ __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t
                                                   int32_t *other, uint32_t *subtree, int32_t *parent_of,
                                                   uint2 *range, const EmitState *__restrict__ top,
                                                   const uint32_t *top_n, uint32_t top_cap, const unsigned int *err) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
     if (sort_failed(err)) return;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= min(*top_n, top_cap)) return;
@@ -920,6 +942,10 @@ __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t
     float3 lo = make_float3(e.lo[0], e.lo[1], e.lo[2]), hi = make_float3(e.hi[0], e.hi[1], e.hi[2]);
     uint32_t l = e.l, r = e.r;
     int32_t ref = (int32_t)e.ref;
+    // prefix lengths at the splits l-1|l and r|r+1 (-1 past either end of the codes); a
+    // step changes one end, whose new prefix is read together with the sibling's box
+    int dl = l == 0 ? -1 : prefix_len(ukey, l - 1, l);
+    int dr = r == U - 1 ? -1 : prefix_len(ukey, r, r + 1);
     for (;;) {
         if (l == 0 && r == U - 1) {
             hdr->root_ref = ref;
@@ -929,7 +955,7 @@ __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t
             parent_of[ref] = -1;
             return;
         }
-        const bool left = (l == 0) || (r != U - 1 && prefix_len(ukey, r, r + 1) > prefix_len(ukey, l - 1, l));
+        const bool left = dr > dl;  // l == 0 (dl = -1, r < U - 1) goes left, r == U - 1 right
         const uint32_t p = left ? r : l - 1;
         const int slot = left ? 0 : 1;
         float4 *nd = nodes + 4 * (size_t)p;
@@ -937,9 +963,14 @@ __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t
         parent_of[ref] = (int32_t)p;
         const int32_t o = exch_acq_rel(&other[p], (int32_t)(left ? l : r));
         if (o < 0) return;
+        if (left) {
+            r = (uint32_t)o;
+            dr = r == U - 1 ? -1 : prefix_len(ukey, r, r + 1);
+        } else {
+            l = (uint32_t)o;
+            dl = l == 0 ? -1 : prefix_len(ukey, l - 1, l);
+        }
         emit_merge_global(nd, slot, lo, hi);
-        if (left) r = (uint32_t)o;
-        else l = (uint32_t)o;
         subtree[p] = range_size(l, r);
         range[p] = make_uint2(l, r);
         ref = (int32_t)p;
@@ -951,6 +982,16 @@ __global__ void __launch_bounds__(128) k_emit_top(BvhHeader *hdr, const uint64_t
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// Programmatic dependent launches between a build's kernels: 0 never, 1 always, 2 for
+// sorts of at most 8 tiles per SM, whose kernels are short enough for the launch
+// latency between them to count.
+#ifndef GBT_LBVH_PDL
+#define GBT_LBVH_PDL 2
+#endif
+static bool lbvh_pdl(uint32_t n_tiles, int num_sms) {
+    return GBT_LBVH_PDL == 1 || (GBT_LBVH_PDL == 2 && n_tiles <= (uint32_t)num_sms * 8u);
+}
+
 // Emission blocks: one per EMIT_THREADS distinct codes; at most one node per
 // block edge goes to k_emit_top.
 static uint32_t emit_blocks(uint32_t n) { return (n + EMIT_THREADS - 1) / EMIT_THREADS; }
@@ -974,17 +1015,17 @@ size_t gbt_lbvh_scratch_bytes(uint32_t n) {
 }
 
 static int sort_enqueue(gbt_ctx *ctx, unsigned char *sbase, const SortScratch &ss, uint64_t *kA, uint32_t *vA,
-                        uint64_t *kB, uint32_t *vB, uint32_t n, int identity_vals, BvhHeader *hdr) {
+                        uint64_t *kB, uint32_t *vB, uint32_t n, int identity_vals, BvhHeader *hdr, bool pdl) {
     cudaStream_t st = ctx->stream;
     SortPlan *plan = reinterpret_cast<SortPlan *>(sbase + ss.plan);
     uint32_t *hist = reinterpret_cast<uint32_t *>(sbase + ss.hist);
     uint32_t *ctr = reinterpret_cast<uint32_t *>(sbase + ss.ctr);
     uint32_t *status = reinterpret_cast<uint32_t *>(sbase + ss.status);
-    GBT_CUDA(ctx, cudaMemsetAsync(sbase + ss.hist, 0, ss.total - ss.hist, st));
-    k_hist<<<ctx->num_sms * 2, 256, 0, st>>>(kA, n, hist);
-    k_sort_plan<<<1, 256, 0, st>>>(plan, hist, n, kA, vA, kB, vB, identity_vals, hdr);
+    // the histograms, tile counters and look-back words were zeroed before the build's first kernel
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_hist, ctx->num_sms * 2, 256, 0, st, kA, n, hist));
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_sort_plan, 1, 256, 0, st, plan, hist, n, kA, vA, kB, vB, identity_vals, hdr));
     GBT_CUDA(ctx, onesweep_passes(ctx->sort_threads, ctx->num_sms, plan, n, ss.n_tiles, status, ctr, ctx->d_error, ctx->spin_limit,
-                                  ctx->withhold_tile, st));
+                                  ctx->withhold_tile, st, pdl));
     return GBT_OK;
 }
 
@@ -1002,33 +1043,42 @@ int gbt_lbvh_enqueue(gbt_ctx *ctx, gbt_bvh *bvh) {
     unsigned char *sb = static_cast<unsigned char *>(scr);
     cudaStream_t st = ctx->stream;
     unsigned long long *acc = reinterpret_cast<unsigned long long *>(sb + acc_off);
+    uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
+    EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
+    const bool pdl = lbvh_pdl(ss.n_tiles, ctx->num_sms);
+    // Every buffer the build's kernels expect zeroed (or -1) is set before its first
+    // kernel, so that the kernels follow one another as programmatic dependent launches.
     GBT_CUDA(ctx, cudaMemsetAsync(acc, 0xff, 3 * sizeof(unsigned long long), st));
     GBT_CUDA(ctx, cudaMemsetAsync(acc + 3, 0x00, 3 * sizeof(unsigned long long), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(sb + ss.hist, 0, ss.total - ss.hist, st));
+    GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
+    GBT_CUDA(ctx, cudaMemsetAsync(top_n, 0, sizeof(uint32_t), st));
     int grid = ctx->num_sms * 8;
     int g2 = (int)((n + 255) / 256);
     if (g2 < grid) grid = g2;
     // the scene box: each block ends with six atomics on the same six words
     const int gb = std::min(grid, ctx->num_sms * GBT_BOUNDS_BLOCKS_PER_SM);
     k_bounds<<<gb, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc);
-    k_morton<<<grid, 256, 0, st>>>(sc->d_verts, sc->d_sph, n_tri, n, acc, bvh->d_codes);
-    rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr);
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_morton, grid, 256, 0, st, sc->d_verts, sc->d_sph, n_tri, n,
+                                 (const unsigned long long *)acc, bvh->d_codes));
+    rc = sort_enqueue(ctx, sb, ss, bvh->d_codes, bvh->d_idx, bvh->d_codes + n, bvh->d_idx + n, n, 1, bvh->d_hdr, pdl);
     if (rc) return rc;
     const SortPlan *plan = reinterpret_cast<const SortPlan *>(sb + ss.plan);
     uint32_t rt = (n + RLE_TILE - 1) / RLE_TILE;
     uint32_t *tcnt = reinterpret_cast<uint32_t *>(sb + rle_off);
-    k_rle_count<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, ctx->d_error);
-    k_rle_scan<<<1, 1024, 0, st>>>(tcnt, rt, bvh->d_hdr, ctx->d_error);
-    k_rle_write<<<rt, RLE_THREADS, 0, st>>>(plan, n, tcnt, bvh->d_run, bvh->d_ukey, ctx->d_error);
-    uint32_t *top_n = reinterpret_cast<uint32_t *>(sb + top_off);
-    EmitState *top = reinterpret_cast<EmitState *>(sb + top_off + 16);
+    const unsigned int *cerr = ctx->d_error;
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_rle_count, rt, RLE_THREADS, 0, st, plan, n, tcnt, cerr));
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_rle_scan, 1, 1024, 0, st, tcnt, rt, bvh->d_hdr, cerr));
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_rle_write, rt, RLE_THREADS, 0, st, plan, n, (const uint32_t *)tcnt, bvh->d_run,
+                                 bvh->d_ukey, cerr));
     const uint32_t eb = emit_blocks(n);
-    GBT_CUDA(ctx, cudaMemsetAsync(bvh->d_other, 0xff, (size_t)n * sizeof(int32_t), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(top_n, 0, sizeof(uint32_t), st));
-    k_emit<<<eb, EMIT_THREADS, 0, st>>>(bvh->d_hdr, bvh->d_hdr, bvh->d_run, bvh->d_ukey, bvh->d_prims, bvh->d_nodes,
-                                        bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n, top, top_n, eb,
-                                        ctx->d_error, plan, sc->d_verts, sc->d_sph, n_tri);
-    k_emit_top<<<(eb + 127) / 128, 128, 0, st>>>(bvh->d_hdr, bvh->d_ukey, bvh->d_nodes, bvh->d_other, bvh->d_size,
-                                                 bvh->d_parent, bvh->d_range, top, top_n, eb, ctx->d_error);
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_emit, eb, EMIT_THREADS, 0, st, (const BvhHeader *)bvh->d_hdr, bvh->d_hdr,
+                                 (const uint32_t *)bvh->d_run, (const uint64_t *)bvh->d_ukey, bvh->d_prims,
+                                 bvh->d_nodes, bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range, n, top, top_n,
+                                 eb, ctx->d_error, plan, (const float *)sc->d_verts, (const float4 *)sc->d_sph, n_tri));
+    GBT_CUDA(ctx, gbt_launch_pdl(pdl, k_emit_top, (eb + 127) / 128, 128, 0, st, bvh->d_hdr, (const uint64_t *)bvh->d_ukey,
+                                 bvh->d_nodes, bvh->d_other, bvh->d_size, bvh->d_parent, bvh->d_range,
+                                 (const EmitState *)top, (const uint32_t *)top_n, eb, (const unsigned int *)ctx->d_error));
     GBT_CUDA(ctx, cudaGetLastError());
     return GBT_OK;
 }
@@ -1088,7 +1138,8 @@ int gbt_sort_pairs_static(cudaStream_t st, int num_sms, unsigned char *sbase, ui
     if (cudaMemsetAsync(err, 0, sizeof(unsigned int), st) != cudaSuccess) return GBT_ECUDA;
     k_hist<<<num_sms * 2, 256, 0, st>>>(codes_in, n, hist);
     k_sort_plan_all<<<1, 256, 0, st>>>(plan, hist, codes_in, codes_out, idx_out, kB, vB);
-    return onesweep_passes(256, num_sms, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st) == cudaSuccess
+    return onesweep_passes(256, num_sms, plan, n, ss.n_tiles, status, ctr, err, GBT_SPIN_LIMIT, 0xffffffffu, st,
+                           lbvh_pdl(ss.n_tiles, num_sms)) == cudaSuccess
                ? GBT_OK
                : GBT_ECUDA;
 }
