@@ -41,6 +41,61 @@ int gbt_check_device_error(gbt_ctx *ctx, const char *what) {
     return gbt_fail(ctx, (flags & GBT_DEVERR_SPIN) ? GBT_ETIMEOUT : GBT_EDEVICE, m);
 }
 
+cudaError_t gbt_block_get(gbt_ctx *ctx, size_t bytes, void **p, size_t *got) {
+    int best = -1;
+    for (int i = 0; i < GBT_BLOCK_CACHE; i++) {
+        const size_t b = ctx->block_cache_bytes[i];
+        if (ctx->block_cache[i] && b >= bytes && b / 2 <= bytes && (best < 0 || b < ctx->block_cache_bytes[best]))
+            best = i;
+    }
+    if (best >= 0) {
+        *p = ctx->block_cache[best];
+        *got = ctx->block_cache_bytes[best];
+        ctx->block_cache[best] = nullptr;
+        ctx->block_cache_bytes[best] = 0;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {  // room held by the cache may be what is missing
+        cudaGetLastError();
+        gbt_block_release(ctx);
+        e = cudaMalloc(p, bytes);
+    }
+    *got = e == cudaSuccess ? bytes : 0;
+    return e;
+}
+
+void gbt_block_put(gbt_ctx *ctx, void *p, size_t bytes) {
+    if (!p) return;
+    if (!ctx->keep_workspace || bytes == 0) {
+        cudaFree(p);
+        return;
+    }
+    int slot = -1;
+    for (int i = 0; i < GBT_BLOCK_CACHE && slot < 0; i++)
+        if (!ctx->block_cache[i]) slot = i;
+    if (slot < 0) {
+        slot = 0;
+        for (int i = 1; i < GBT_BLOCK_CACHE; i++)
+            if (ctx->block_cache_bytes[i] < ctx->block_cache_bytes[slot]) slot = i;
+        if (ctx->block_cache_bytes[slot] >= bytes) {  // every cached block is larger: keep them
+            cudaFree(p);
+            return;
+        }
+        cudaFree(ctx->block_cache[slot]);
+    }
+    ctx->block_cache[slot] = p;
+    ctx->block_cache_bytes[slot] = bytes;
+}
+
+void gbt_block_release(gbt_ctx *ctx) {
+    for (int i = 0; i < GBT_BLOCK_CACHE; i++) {
+        if (ctx->block_cache[i]) cudaFree(ctx->block_cache[i]);
+        ctx->block_cache[i] = nullptr;
+        ctx->block_cache_bytes[i] = 0;
+    }
+}
+
 void *gbt_pinned(gbt_ctx *ctx) {
     if (!ctx->h_pin && cudaMallocHost(&ctx->h_pin, GBT_PINNED_BYTES) != cudaSuccess) {
         cudaGetLastError();
@@ -135,6 +190,7 @@ extern "C" int gbt_ctx_destroy(gbt_ctx *ctx) {
     if (ctx->d_out) cudaFree(ctx->d_out);
     if (ctx->bstate) cudaFree(ctx->bstate);
     gbt_phr_release(ctx);
+    gbt_block_release(ctx);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     for (auto &e : ctx->prof_ev) cudaEventDestroy(e);
     for (auto &e : ctx->ev)
@@ -187,6 +243,7 @@ extern "C" int gbt_ctx_set_option(gbt_ctx *ctx, int32_t option, int32_t value) {
         if (!value) {
             GBT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             gbt_phr_release(ctx);
+            gbt_block_release(ctx);
         }
         return GBT_OK;
     case GBT_OPT_SPIN_LIMIT:
@@ -316,11 +373,16 @@ extern "C" int gbt_bvh_destroy(gbt_bvh *b) {
     if (!b) return GBT_EINVAL;
     if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
     if (b->d_block) {
-        cudaFree(b->d_block);
+        if (b->ctx) gbt_block_put(b->ctx, b->d_block, b->d_block_bytes);
+        else cudaFree(b->d_block);
         b->d_nodes = nullptr;
         b->d_prims = nullptr;
         b->d_hdr = nullptr;
         b->d_parent = nullptr;
+    }
+    if (b->d_nodes4 && b->ctx) {
+        gbt_block_put(b->ctx, b->d_nodes4, b->nodes4_bytes);
+        b->d_nodes4 = nullptr;
     }
     cudaFree(b->d_nodes);
     cudaFree(b->d_prims);

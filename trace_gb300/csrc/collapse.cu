@@ -100,8 +100,8 @@ __device__ void collapse_one(const float4 *__restrict__ bin, int2 e, int2 *__res
     reinterpret_cast<int4 *>(nd)[7] = make_int4(cnt[0], cnt[1], cnt[2], cnt[3]);
 }
 
-// Counters of the graph form: [0], [1] the two queues' sizes, [2] 4-wide nodes, [3] the input
-// queue of the current level, [4] levels done.
+// Counters: [0], [1] the two queues' sizes, [2] 4-wide nodes, [3] the input queue of the
+// current level, [4] levels done, [5] blocks of the running level done (outside a graph).
 constexpr uint32_t MAX_LEVELS = 4096;  // a tree deeper than this is reported, not walked
 constexpr int COLLAPSE_BATCH = 8;      // levels launched per readback (gbt_collapse4)
 
@@ -147,16 +147,37 @@ __global__ void k_collapse_root_gs(const BvhHeader *__restrict__ hdr, BvhHeader 
     ctr[1] = 0;
     ctr[3] = 0;
     ctr[4] = 0;
+    ctr[5] = 0;
 }
 
-// k_collapse_advance outside a graph: the output queue becomes the input.  After the
-// last level the next ones find an empty queue and do nothing.
-__global__ void k_collapse_step(uint32_t *ctr, unsigned int *err) {
-    const uint32_t par = ctr[3], next = par ^ 1;
-    ctr[par] = 0;
-    ctr[3] = next;
-    const uint32_t levels = ++ctr[4];
-    if (ctr[next] > 0 && levels >= MAX_LEVELS) atomicOr(err, GBT_DEVERR_CAPACITY);
+// One level outside a graph, ending with k_collapse_advance's step taken by the grid's
+// last block to finish (ctr[5] counts finished blocks): the output queue becomes the
+// input.  After the last level the next ones find an empty queue and do nothing.
+__global__ void k_collapse_level_step(const float4 *__restrict__ bin, int2 *q0, int2 *q1, uint32_t *ctr,
+                                      float4 *__restrict__ out, uint32_t cap, unsigned int *err) {
+    __shared__ bool s_last;
+    const uint32_t par = ctr[3];
+    const uint32_t n = min(ctr[par], cap);  // a full queue counted past its capacity (reported)
+    const int2 *q_in = par ? q1 : q0;
+    int2 *q_out = par ? q0 : q1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        collapse_one(bin, q_in[i], q_out, ctr + (par ^ 1), ctr + 2, out, cap, err);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's queue appends before its count
+        s_last = atomicAdd(&ctr[5], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0 || !s_last) return;
+    __threadfence();  // every block's appends before the counters are read
+    const uint32_t next = par ^ 1;
+    volatile uint32_t *vc = ctr;
+    vc[par] = 0;
+    vc[3] = next;
+    vc[5] = 0;
+    const uint32_t levels = vc[4] + 1;
+    vc[4] = levels;
+    if (vc[next] > 0 && levels >= MAX_LEVELS) atomicOr(err, GBT_DEVERR_CAPACITY);
 }
 
 __global__ void k_collapse_root_graph(const BvhHeader *__restrict__ hdr, BvhHeader *hdr4, int2 *q0, uint32_t *ctr,
@@ -172,14 +193,19 @@ __global__ void k_collapse_root_graph(const BvhHeader *__restrict__ hdr, BvhHead
 
 static int reserve4(gbt_ctx *ctx, gbt_bvh *bvh, uint32_t cap) {
     if (bvh->nodes4_cap < cap) {
-        cudaFree(bvh->d_nodes4);
+        gbt_block_put(ctx, bvh->d_nodes4, bvh->nodes4_bytes);
         bvh->d_nodes4 = nullptr;
         bvh->nodes4_cap = 0;
-        if (cudaMalloc(&bvh->d_nodes4, (size_t)cap * 8 * sizeof(float4)) != cudaSuccess) {
+        bvh->nodes4_bytes = 0;
+        void *p = nullptr;
+        size_t got = 0;
+        if (gbt_block_get(ctx, (size_t)cap * 8 * sizeof(float4), &p, &got) != cudaSuccess) {
             cudaGetLastError();
             return gbt_fail(ctx, GBT_ENOMEM, "collapse: node allocation");
         }
-        bvh->nodes4_cap = cap;
+        bvh->d_nodes4 = static_cast<float4 *>(p);
+        bvh->nodes4_bytes = got;
+        bvh->nodes4_cap = (uint32_t)(got / (8 * sizeof(float4)));
     }
     if (!bvh->d_hdr4 && cudaMalloc(&bvh->d_hdr4, sizeof(BvhHeader)) != cudaSuccess) {
         cudaGetLastError();
@@ -215,11 +241,9 @@ int gbt_collapse4(gbt_ctx *ctx, gbt_bvh *bvh) {
     k_collapse_root_gs<<<1, 1, 0, st>>>(bvh->d_hdr, bvh->d_hdr4, q0, ctr);
     // levels in batches of COLLAPSE_BATCH launches between readbacks of the counters
     for (;;) {
-        for (int b = 0; b < COLLAPSE_BATCH; b++) {
-            k_collapse_level_gs<<<(unsigned)ctx->num_sms * 4, 128, 0, st>>>(bvh->d_nodes, q0, q1, ctr, bvh->d_nodes4,
-                                                                            kcap, ctx->d_error);
-            k_collapse_step<<<1, 1, 0, st>>>(ctr, ctx->d_error);
-        }
+        for (int b = 0; b < COLLAPSE_BATCH; b++)
+            k_collapse_level_step<<<(unsigned)ctx->num_sms * 4, 128, 0, st>>>(bvh->d_nodes, q0, q1, ctr,
+                                                                              bvh->d_nodes4, kcap, ctx->d_error);
         GBT_CUDA(ctx, cudaGetLastError());
         GBT_CUDA(ctx, cudaMemcpyAsync(hc, ctr, 5 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         GBT_CUDA(ctx, cudaStreamSynchronize(st));

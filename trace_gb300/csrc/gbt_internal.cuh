@@ -22,6 +22,8 @@
 
 #define GBT_PHR_SMALL_CUT 256
 
+#define GBT_BLOCK_CACHE 4
+
 struct gbt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -68,6 +70,12 @@ struct gbt_ctx {
     void *phr_scr = nullptr;
     size_t phr_scr_bytes = 0;
     int keep_workspace = 1;
+    // Device blocks of destroyed trees (a PHR tree's arrays, a 4-wide view), kept for the
+    // next trees built on this context: a cudaMalloc and cudaFree of a tree's few hundred MB
+    // take 0.1-0.5 ms.  Released with the context, when a cudaMalloc of gbt_block_get
+    // fails, and at once under GBT_OPT_KEEP_WORKSPACE 0.
+    void *block_cache[GBT_BLOCK_CACHE] = {};
+    size_t block_cache_bytes[GBT_BLOCK_CACHE] = {};
     // largest cut of a PHR level run with one-warp blocks (GBT_OPT_PHR_SMALL_CUT, 1..GBT_PHR_SMALL_CUT)
     int phr_small_cut = GBT_PHR_SMALL_CUT;
     void *h_pin = nullptr;  // small pinned host buffer for counter readbacks (gbt_pinned)
@@ -141,9 +149,11 @@ struct gbt_bvh {
     float4 *d_nodes4 = nullptr;
     BvhHeader *d_hdr4 = nullptr;
     uint32_t nodes4_cap = 0;
+    size_t nodes4_bytes = 0;        // size of the d_nodes4 block
     int has_nodes4 = 0;
     int packet_choice = 0;          // camera-ray kernel measured for this tree: 0 not yet, 1 packets, 2 single rays
     void *d_block = nullptr;        // when set: d_nodes, d_prims, d_parent and d_hdr are pieces of this allocation
+    size_t d_block_bytes = 0;
 };
 
 // collapse.cu
@@ -163,6 +173,13 @@ int gbt_fail(gbt_ctx *ctx, int code, const std::string &msg);
 int gbt_cuda_fail(gbt_ctx *ctx, cudaError_t e, const char *what);
 int gbt_check_device_error(gbt_ctx *ctx, const char *what);
 int gbt_scratch(gbt_ctx *ctx, size_t bytes, void **out);
+// A device block of at least `bytes` (its size in *got): the smallest cached block that
+// fits and is at most twice as large, else a new allocation.
+cudaError_t gbt_block_get(gbt_ctx *ctx, size_t bytes, void **p, size_t *got);
+// Hands a block of a destroyed tree back to the context's cache (the smallest cached
+// block is freed when the cache is full); frees it under GBT_OPT_KEEP_WORKSPACE 0.
+void gbt_block_put(gbt_ctx *ctx, void *p, size_t bytes);
+void gbt_block_release(gbt_ctx *ctx);
 
 #define GBT_CUDA(ctx, call)                                   \
     do {                                                      \

@@ -2008,12 +2008,15 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
         const size_t b_prims = gbt_align((size_t)N * 3 * sizeof(float4));
         const size_t b_nodes = gbt_align((size_t)pnode_cap * per_node * sizeof(float4));
         const size_t b_parent = gbt_align((size_t)pnode_cap * sizeof(int32_t));
-        char *blk = nullptr;
-        if (cudaMalloc(&blk, b_prims + b_nodes + b_parent + sizeof(BvhHeader)) != cudaSuccess) {
+        void *bp = nullptr;
+        size_t got = 0;
+        if (gbt_block_get(ctx, b_prims + b_nodes + b_parent + sizeof(BvhHeader), &bp, &got) != cudaSuccess) {
             cudaGetLastError();
             return gbt_fail(ctx, GBT_ENOMEM, "phr: output allocation");
         }
+        char *blk = static_cast<char *>(bp);
         out->d_block = blk;
+        out->d_block_bytes = got;
         out->d_prims = reinterpret_cast<float4 *>(blk);
         out->d_nodes = reinterpret_cast<float4 *>(blk + b_prims);
         out->d_parent = reinterpret_cast<int32_t *>(blk + b_prims + b_nodes);
