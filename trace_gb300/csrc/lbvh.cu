@@ -97,15 +97,29 @@ __global__ void __launch_bounds__(256) k_bounds(const float *__restrict__ verts,
     const size_t nf = (size_t)n_tri * 9, nchunk = nf / 12;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
     const float4 *v4 = reinterpret_cast<const float4 *>(verts);
-    for (size_t c = tid; c < nchunk; c += stride) {
-        const float4 a = __ldg(v4 + 3 * c), b = __ldg(v4 + 3 * c + 1), d = __ldg(v4 + 3 * c + 2);
+    auto fold = [&](const float4 &a, const float4 &b, const float4 &d) {
         flo[0] = fminf(fminf(fminf(flo[0], a.x), fminf(a.w, b.z)), d.y);
         fhi[0] = fmaxf(fmaxf(fmaxf(fhi[0], a.x), fmaxf(a.w, b.z)), d.y);
         flo[1] = fminf(fminf(fminf(flo[1], a.y), fminf(b.x, b.w)), d.z);
         fhi[1] = fmaxf(fmaxf(fmaxf(fhi[1], a.y), fmaxf(b.x, b.w)), d.z);
         flo[2] = fminf(fminf(fminf(flo[2], a.z), fminf(b.y, d.x)), d.w);
         fhi[2] = fmaxf(fmaxf(fmaxf(fhi[2], a.z), fmaxf(b.y, d.x)), d.w);
+    };
+    size_t c = tid;
+    // four chunks' loads in flight per thread (the fold is order-free: min and max)
+    for (; c + 3 * stride < nchunk; c += 4 * stride) {
+        float4 a[4], b[4], d[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float4 *q = v4 + 3 * (c + u * stride);
+            a[u] = __ldg(q);
+            b[u] = __ldg(q + 1);
+            d[u] = __ldg(q + 2);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) fold(a[u], b[u], d[u]);
     }
+    for (; c < nchunk; c += stride) fold(__ldg(v4 + 3 * c), __ldg(v4 + 3 * c + 1), __ldg(v4 + 3 * c + 2));
     for (size_t f = nchunk * 12 + tid; f < nf; f += stride) {
         const float x = __ldg(verts + f);
         const int k = (int)(f % 3);
