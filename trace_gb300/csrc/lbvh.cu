@@ -806,71 +806,20 @@ __device__ __forceinline__ float4 lds_f4(const float4 *p) {
 // Number of nodes (leaves included) under a node of distinct-code range [l, r].
 __device__ __forceinline__ uint32_t range_size(uint32_t l, uint32_t r) { return 2u * (r - l) + 1u; }
 
-// Each leaf's primitive records are made here, from the sorted indices and the vertices,
-// and its box is taken from the values in registers (one pass over the records instead of
-// a gather launch that writes them and an emission that reads them back).
-__global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
-                                                       const uint32_t *__restrict__ run,
-                                                       const uint64_t *__restrict__ ukey,
-                                                       float4 *__restrict__ recs, float4 *nodes, int32_t *other,
-                                                       uint32_t *subtree, int32_t *parent_of, uint2 *range,
-                                                       uint32_t n, EmitState *top, uint32_t *top_n, uint32_t top_cap,
-                                                       unsigned int *err, const SortPlan *__restrict__ plan,
-                                                       const float *__restrict__ verts, const float4 *__restrict__ sph,
-                                                       uint32_t n_tri) {
-    gbt_pdl_wait();
-    gbt_pdl_trigger();
-    if (sort_failed(err)) return;
-    constexpr int B = EMIT_THREADS, NW = B / 32;
-    // s_d[i]: common prefix length at the split k0-1+i | k0+i (i = 0..B), -1 past
-    // either end of the codes.  s_loc[t]: inner node k0+t has its whole range in
-    // this block's leaves [k0, k0+B).  A node k covers the widest range around
-    // split k whose splits all share at least its prefix length, so its range
-    // stays inside iff a shorter prefix occurs among the block's splits on both
-    // sides of k (the splits k0-1 and k0+B-1 at the block's edges included).
-    __shared__ int s_d[B + 1];
-    __shared__ int s_suf[B];
-    __shared__ int s_wpre[NW], s_wsuf[NW];
-    __shared__ int32_t s_oth[B];
-    __shared__ float4 s_r0[2][B];  // per inner node, per child slot: lo.xyz, hi.x
-    __shared__ float4 s_r1[2][B];  //                                 hi.yz, ref, count
-    __shared__ uint8_t s_loc[B];
-    const uint32_t U = hdr_in->n_unique;
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const uint32_t k0 = blockIdx.x * B;
-    for (int i = t; i <= B; i += B) {
-        const long long j = (long long)k0 - 1 + i;  // split j | j+1
-        s_d[i] = (j >= 0 && j + 1 < (long long)U) ? prefix_len(ukey, (uint32_t)j, (uint32_t)j + 1) : -1;
-    }
-    s_oth[t] = -1;
-    __syncthreads();
-    // pre = min s_d[0..t]; suf = min s_d[t+1..B-1+1] (inclusive scans, warp shuffles + warp totals)
-    int pre = s_d[t], suf = s_d[t + 1];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int a = __shfl_up_sync(0xffffffffu, pre, o), b = __shfl_down_sync(0xffffffffu, suf, o);
-        if (lane >= o) pre = min(pre, a);
-        if (lane + o < 32) suf = min(suf, b);
-    }
-    if (lane == 31) s_wpre[w] = pre;
-    if (lane == 0) s_wsuf[w] = suf;
-    __syncthreads();
-    for (int k = 0; k < NW; k++) {
-        if (k < w) pre = min(pre, s_wpre[k]);
-        if (k > w) suf = min(suf, s_wsuf[k]);
-    }
-    s_suf[t] = suf;  // min s_d[t+1..B]
-    __syncthreads();
-    {
-        // node k0+t is split t+1: shorter prefixes needed in s_d[0..t] and s_d[t+2..B]
-        const int dk = s_d[t + 1];
-        const int right = t + 1 < B ? s_suf[t + 1] : 64;
-        s_loc[t] = (dk >= 0 && pre < dk && right < dk) ? 1 : 0;
-    }
-    __syncthreads();
-
-    const uint32_t u = k0 + t;
-    if (u >= U || u >= n) return;
+// One leaf of k_emit: its records, then its climb while it is the second child to
+// arrive.  The nodes inside the block keep both child slots, their subtree size and
+// range in shared memory for k_emit's write-out; the others go as before.
+__device__ __forceinline__ void emit_climb(BvhHeader *hdr, const uint32_t *__restrict__ run,
+                                           const uint64_t *__restrict__ ukey, float4 *__restrict__ recs,
+                                           float4 *nodes, int32_t *other, int32_t *parent_of, uint32_t *subtree,
+                                           uint2 *range, EmitState *top, uint32_t *top_n, uint32_t top_cap,
+                                           unsigned int *err, const SortPlan *__restrict__ plan,
+                                           const float *__restrict__ verts, const float4 *__restrict__ sph,
+                                           uint32_t n_tri, uint32_t U, uint32_t k0, uint32_t u, const int *s_d,
+                                           int32_t *s_oth, float4 (*s_r0)[EMIT_THREADS],
+                                           float4 (*s_r1)[EMIT_THREADS], uint32_t *s_sub, uint2 *s_rng,
+                                           int32_t *s_par, const uint8_t *s_loc) {
+    constexpr int B = EMIT_THREADS;
     uint32_t first = run[u], last = run[u + 1];
     float3 lo, hi;
     const uint32_t *__restrict__ idx = plan->final_v;
@@ -911,8 +860,8 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
         float4 *nd = nodes + 4 * (size_t)p;
         const uint32_t q = p - k0;
         if (p >= k0 && q < (uint32_t)B && s_loc[q]) {
-            // both children are this block's: hand over through shared memory; the
-            // second child writes the whole node
+            // both children are this block's: each leaves its slot in shared memory (the
+            // block writes the node out); the second to arrive carries on
             s_r0[slot][q] = make_float4(lo.x, lo.y, lo.z, hi.x);
             s_r1[slot][q] = make_float4(hi.y, hi.z, __int_as_float(ref), __int_as_float(cnt));
             __threadfence_block();
@@ -922,20 +871,15 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
             const float4 a = lds_f4(&s_r0[slot ^ 1][q]), b = lds_f4(&s_r1[slot ^ 1][q]);
             const float3 slo = make_float3(a.x, a.y, a.z), shi = make_float3(a.w, b.x, b.y);
             const int32_t sref = __float_as_int(b.z), scnt = __float_as_int(b.w);
-            const float3 lo0 = left ? lo : slo, hi0 = left ? hi : shi, lo1 = left ? slo : lo, hi1 = left ? shi : hi;
-            nd[0] = make_float4(lo0.x, hi0.x, lo0.y, hi0.y);
-            nd[1] = make_float4(lo1.x, hi1.x, lo1.y, hi1.y);
-            nd[2] = make_float4(lo0.z, hi0.z, lo1.z, hi1.z);
-            reinterpret_cast<int4 *>(nd)[3] =
-                left ? make_int4(ref, cnt, sref, scnt) : make_int4(sref, scnt, ref, cnt);
-            if (cnt == 0) parent_of[ref] = (int32_t)p;
-            if (scnt == 0) parent_of[sref] = (int32_t)p;
+            // inner children of a node inside the block are inside it too
+            if (cnt == 0) s_par[ref - (int32_t)k0] = (int32_t)p;
+            if (scnt == 0) s_par[sref - (int32_t)k0] = (int32_t)p;
             lo = make_float3(fminf(lo.x, slo.x), fminf(lo.y, slo.y), fminf(lo.z, slo.z));
             hi = make_float3(fmaxf(hi.x, shi.x), fmaxf(hi.y, shi.y), fmaxf(hi.z, shi.z));
             if (left) r = (uint32_t)o;
             else l = (uint32_t)o;
-            subtree[p] = range_size(l, r);
-            range[p] = make_uint2(l, r);  // distinct-code range of inner node p
+            s_sub[q] = range_size(l, r);
+            s_rng[q] = make_uint2(l, r);  // distinct-code range of inner node p
             ref = (int32_t)p;
             cnt = 0;
             continue;
@@ -960,6 +904,98 @@ __global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_i
         top[k] = EmitState{{lo.x, lo.y, lo.z}, {hi.x, hi.y, hi.z}, l, r, p, 0u, {0u, 0u}};
         return;
     }
+}
+
+// Each leaf's primitive records are made here, from the sorted indices and the vertices,
+// and its box is taken from the values in registers (one pass over the records instead of
+// a gather launch that writes them and an emission that reads them back).
+__global__ void __launch_bounds__(EMIT_THREADS, 8) k_emit(const BvhHeader *hdr_in, BvhHeader *hdr,
+                                                       const uint32_t *__restrict__ run,
+                                                       const uint64_t *__restrict__ ukey,
+                                                       float4 *__restrict__ recs, float4 *nodes, int32_t *other,
+                                                       uint32_t *subtree, int32_t *parent_of, uint2 *range,
+                                                       uint32_t n, EmitState *top, uint32_t *top_n, uint32_t top_cap,
+                                                       unsigned int *err, const SortPlan *__restrict__ plan,
+                                                       const float *__restrict__ verts, const float4 *__restrict__ sph,
+                                                       uint32_t n_tri) {
+    gbt_pdl_wait();
+    gbt_pdl_trigger();
+    if (sort_failed(err)) return;
+    constexpr int B = EMIT_THREADS, NW = B / 32;
+    // s_d[i]: common prefix length at the split k0-1+i | k0+i (i = 0..B), -1 past
+    // either end of the codes.  s_loc[t]: inner node k0+t has its whole range in
+    // this block's leaves [k0, k0+B).  A node k covers the widest range around
+    // split k whose splits all share at least its prefix length, so its range
+    // stays inside iff a shorter prefix occurs among the block's splits on both
+    // sides of k (the splits k0-1 and k0+B-1 at the block's edges included).
+    __shared__ int s_d[B + 1];
+    __shared__ int s_suf[B];
+    __shared__ int s_wpre[NW], s_wsuf[NW];
+    __shared__ int32_t s_oth[B];
+    __shared__ float4 s_r0[2][B];  // per inner node, per child slot: lo.xyz, hi.x
+    __shared__ float4 s_r1[2][B];  //                                 hi.yz, ref, count
+    __shared__ uint32_t s_sub[B];  // per inner node: subtree size
+    __shared__ uint2 s_rng[B];     //                 distinct-code range
+    __shared__ int32_t s_par[B];   //                 parent when that is the block's too (-2: not)
+    __shared__ uint8_t s_loc[B];
+    const uint32_t U = hdr_in->n_unique;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint32_t k0 = blockIdx.x * B;
+    for (int i = t; i <= B; i += B) {
+        const long long j = (long long)k0 - 1 + i;  // split j | j+1
+        s_d[i] = (j >= 0 && j + 1 < (long long)U) ? prefix_len(ukey, (uint32_t)j, (uint32_t)j + 1) : -1;
+    }
+    s_oth[t] = -1;
+    s_par[t] = -2;
+    __syncthreads();
+    // pre = min s_d[0..t]; suf = min s_d[t+1..B-1+1] (inclusive scans, warp shuffles + warp totals)
+    int pre = s_d[t], suf = s_d[t + 1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int a = __shfl_up_sync(0xffffffffu, pre, o), b = __shfl_down_sync(0xffffffffu, suf, o);
+        if (lane >= o) pre = min(pre, a);
+        if (lane + o < 32) suf = min(suf, b);
+    }
+    if (lane == 31) s_wpre[w] = pre;
+    if (lane == 0) s_wsuf[w] = suf;
+    __syncthreads();
+    for (int k = 0; k < NW; k++) {
+        if (k < w) pre = min(pre, s_wpre[k]);
+        if (k > w) suf = min(suf, s_wsuf[k]);
+    }
+    s_suf[t] = suf;  // min s_d[t+1..B]
+    __syncthreads();
+    {
+        // node k0+t is split t+1: shorter prefixes needed in s_d[0..t] and s_d[t+2..B]
+        const int dk = s_d[t + 1];
+        const int right = t + 1 < B ? s_suf[t + 1] : 64;
+        s_loc[t] = (dk >= 0 && pre < dk && right < dk) ? 1 : 0;
+    }
+    __syncthreads();
+
+    const uint32_t u = k0 + t;
+    if (u < U && u < n) emit_climb(hdr, run, ukey, recs, nodes, other, parent_of, subtree, range, top, top_n,
+                                   top_cap, err, plan, verts, sph, n_tri, U, k0, u, s_d, s_oth, s_r0, s_r1, s_sub,
+                                   s_rng, s_par, s_loc);
+    // The block's inner nodes, whose two child slots the climb left in shared memory, are
+    // written out with consecutive threads on consecutive 16-byte words.
+    __syncthreads();
+    for (int j = t; j < 4 * B; j += B) {
+        const int q = j >> 2, part = j & 3;
+        if (!s_loc[q]) continue;
+        const float4 a0 = s_r0[0][q], a1 = s_r1[0][q], b0 = s_r0[1][q], b1 = s_r1[1][q];
+        float4 v;
+        if (part == 0) v = make_float4(a0.x, a0.w, a0.y, a1.x);       // left child: lo.x, hi.x, lo.y, hi.y
+        else if (part == 1) v = make_float4(b0.x, b0.w, b0.y, b1.x);  // right child
+        else if (part == 2) v = make_float4(a0.z, a1.y, b0.z, b1.y);  // lo.z, hi.z of both
+        else v = make_float4(a1.z, a1.w, b1.z, b1.w);                 // ref, count of both
+        nodes[4 * (size_t)(k0 + q) + part] = v;
+    }
+    if (s_loc[t]) {
+        subtree[k0 + t] = s_sub[t];
+        range[k0 + t] = s_rng[t];
+    }
+    if (s_par[t] != -2) parent_of[k0 + t] = s_par[t];
 }
 
 // The nodes that span blocks: one thread per node k_emit handed over, climbing
