@@ -826,7 +826,7 @@ def main():
 # over the build's 17 launches, one ncu capture of the second of four builds each):
 # terrain2048 3510.6 MB / 8,380,419 primitives; soup1M 366.3 MB / 1,000,000 (its keys largely
 # stay in the 129 MB L2, so the capture counts fewer bytes than the algorithm moves).
-LBVH_TRAFFIC_PER_TRI = {"terrain2048": 3510.6e6 / 8380419, "soup1M": 366.3e6 / 1e6}
+LBVH_TRAFFIC_PER_TRI = {"terrain2048": 3387.0e6 / 8380419, "soup1M": 343.3e6 / 1e6}
 
 # DRAM bytes of one headline frame's two traversal launches on the PHR tree
 # (dram__bytes_read.sum + dram__bytes_write.sum of one ncu --set full capture each:
