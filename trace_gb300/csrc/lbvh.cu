@@ -549,7 +549,8 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
             }
             if (publish) st_relaxed(&st[t], ST_PREFIX | (prefix + sum));
         }
-        s_gbase[t] = plan->digit_base[pass][t] + prefix;
+        // output position of tile slot j of digit t: j + (global start - tile start), mod 2^32
+        s_gbase[t] = plan->digit_base[pass][t] + prefix - tstart;
     }
     __syncthreads();
 #pragma unroll
@@ -570,13 +571,12 @@ __global__ void __launch_bounds__(T, MINB) k_onesweep(const SortPlan *__restrict
     for (uint32_t j = tid; j < valid; j += T) {
         uint64_t kk = s_keys[j];
         uint32_t d = (uint32_t)((kk >> shift) & 255u);
-        uint32_t g = s_gbase[d] + (j - s_tstart[d]);
+        uint32_t g = s_gbase[d] + j;
         kout[g] = kk;
         vout[g] = s_vals[j];
     }
 }
 
-// Launches the eight passes (a pass whose plan entry is inactive returns at once).
 // Launches the eight passes (a pass whose plan entry is inactive returns at once) with tiles
 // of 256 threads x 16 keys (threads 256) or 512 x 8 (threads 512, measured no faster).
 // 256-thread tiles take the 3-blocks-per-SM register budget once there are more than four
