@@ -337,7 +337,19 @@ __global__ void __launch_bounds__(256) k_hist(const uint64_t *__restrict__ keys,
     __shared__ uint32_t h[8 * 256];
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) h[i] = 0;
     __syncthreads();
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // eight keys' loads in flight per thread
+    for (; i + 7 * stride < n; i += 8 * stride) {
+        uint64_t k[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) k[u] = __ldcs(keys + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int p = 0; p < 8; p++) atomicAdd(&h[p * 256 + (uint32_t)((k[u] >> (8 * p)) & 255u)], 1u);
+    }
+    for (; i < n; i += stride) {
         uint64_t k = keys[i];
 #pragma unroll
         for (int p = 0; p < 8; p++) atomicAdd(&h[p * 256 + (uint32_t)((k >> (8 * p)) & 255u)], 1u);

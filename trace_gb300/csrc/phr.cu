@@ -2076,9 +2076,10 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, sizeof(PhrGlobals), st));
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0xff, offsetof(PhrGlobals, screen_bad), st));  // counters 0, root -1 below
     GBT_CUDA(ctx, cudaMemsetAsync(d_g, 0, offsetof(PhrGlobals, root), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(d_pn, 0, (size_t)pnode_cap * sizeof(PNode), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(d_aux, 0, (size_t)n_aux * sizeof(AuxNode), st));
-    GBT_CUDA(ctx, cudaMemsetAsync(d_auxc, 0, (size_t)n_aux * sizeof(AuxCold), st));
+    // The auxiliary nodes need no clearing: k_aux_build writes every field the
+    // refinement reads, of every node.  Neither do the output nodes: a level writes
+    // each node it allocates (children as their jobs attach them), and
+    // k_phr_finalize reads only allocated nodes and attached children.
     k_aux_build<<<(U + 255) / 256 + 1, 256, 0, st>>>(aux->d_hdr, aux->d_nodes, aux->d_size, aux->d_range, aux->d_run,
                                                      d_aux, d_auxc, U, N);
     k_phr_screen<<<ctx->num_sms * 4, 256, 0, st>>>(d_aux, n_aux, d_g);
