@@ -232,10 +232,10 @@ int gbt_lbvh_sorted(gbt_ctx *ctx, gbt_bvh *bvh, uint64_t *codes, int32_t *idx);
  * that every GPU loading the library holds until exit, so
  * n <= GBT_NOALLOC_MAX_PAIRS, else GBT_EINVAL.  No context is needed: work is
  * queued on `stream` (a cudaStream_t, NULL for the default stream) of the
- * current device, and the call returns after that stream has finished.  The
- * first call on a device looks up the array's device address, so make it
- * before any stream capture.  All calls share the one array: calls whose work
- * overlaps on the GPU race and corrupt each other's results. */
+ * current device, and the call returns after that stream has finished: it
+ * synchronises the stream to read the sort's error word back, so it cannot be
+ * made while the stream is capturing a graph.  All calls share the one array:
+ * calls whose work overlaps on the GPU race and corrupt each other's results. */
 #define GBT_NOALLOC_MAX_PAIRS 262144u
 int gbt_sort_morton_pairs_noalloc(void *stream, const uint64_t *d_codes_in, uint64_t *d_codes_out,
                                   uint32_t *d_idx_out, uint32_t n);

@@ -73,6 +73,31 @@ def test_phr_workspace_kept_or_released_gives_the_same_tree(ctx):
         ctx.set_option("keep_workspace", 1)
 
 
+def test_reused_tree_blocks_give_the_same_tree_and_hits(ctx):
+    """A destroyed tree's device blocks (its arrays and its 4-wide view) stay on
+    the context for the next trees: a tree built into the blocks of a larger
+    one, with that tree's contents still in them, exports the oracle's tree and
+    gives the same hits as the same tree built into fresh blocks."""
+    small_s = scenes.soup(30_000, seed=9)
+    small, big = small_s["verts"], scenes.soup(50_000, seed=5)["verts"]
+    aux_small = pt.DefaultLBVH(pt.DeviceScene(ctx, small))
+    aux_big = pt.DefaultLBVH(pt.DeviceScene(ctx, big))
+    rays = scenes.camera_rays(small_s["camera"], 96, 64, jitter_seed=3)
+    ref = O.lbvh(small).phr(0.5, 6.0, 2).export()
+    fresh = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(aux_small)  # kept: its blocks stay in use
+    want = fresh.trace(rays)
+    other = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(aux_big)
+    other.trace(rays)
+    other.close()  # its blocks go to the context's cache, the only ones there of these sizes
+    g = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(aux_small)
+    ge = g.export()
+    assert canonical_equal(ge, ref), first_mismatch(ge, ref)
+    got = g.trace(rays)
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    fresh.close()
+
+
 @pytest.mark.parametrize("alpha,delta,bf", [(0.5, 6.0, 2), (0.55, 9.0, 2), (0.5, 6.0, 4)])
 def test_phr_1m_soup(ctx, alpha, delta, bf):
     s = scenes.soup(1_000_000, seed=1)
