@@ -73,6 +73,21 @@ def test_phr_workspace_kept_or_released_gives_the_same_tree(ctx):
         ctx.set_option("keep_workspace", 1)
 
 
+@pytest.mark.parametrize("coord", [1e-12, 3e9])
+def test_phr_outside_the_screening_range_matches_oracle(ctx, coord):
+    """A box coordinate outside [2^-30, 2^30] in magnitude (other than 0) turns
+    the float32 screening off for the whole refinement, which then decides every
+    comparison in float64: the tree is still the oracle's."""
+    verts = np.array(scenes.soup(3000, seed=11)["verts"], np.float32)
+    verts[0, 0] = coord
+    aux = pt.DefaultLBVH(pt.DeviceScene(ctx, verts))
+    g = pt.NewPHRBuilder(0.5, 6.0, 2).BuildFromAuxilary(aux)
+    o = O.lbvh(verts).phr(0.5, 6.0, 2)
+    ge, oe = g.export(), o.export()
+    assert canonical_equal(ge, oe), first_mismatch(ge, oe)
+    assert g.Cost() == o.cost()
+
+
 def test_reused_tree_blocks_give_the_same_tree_and_hits(ctx):
     """A destroyed tree's device blocks (its arrays and its 4-wide view) stay on
     the context for the next trees: a tree built into the blocks of a larger

@@ -1,9 +1,9 @@
 // PHR refinement on the device: pkg/pt/phr.go:47-459 (BuildFromAuxilary).
 //
 //   k_aux_build      unified view of the LBVH (inner nodes and leaves) with
-//                    boxes, subtree sizes (bvh.go:159-167) and primitive ranges
-//   k_phr_screen     whether every box coordinate lies in the range where the
-//                    float32 screening of phr_exact.cuh holds
+//                    boxes, subtree sizes (bvh.go:159-167) and primitive ranges,
+//                    and whether every box coordinate lies in the range where
+//                    the float32 screening of phr_exact.cuh holds
 //   k_initial_cut    findInitialCut (phr.go:257-311), breadth-first in FIFO
 //                    order with the MAX_CUT_SIZE cap, one block
 //   k_phr_level      buildSubTree (phr.go:92-152), one launch per tree level:
@@ -215,27 +215,12 @@ __device__ uint32_t block_scan_u32(uint32_t v, uint32_t *s_tmp, uint32_t *total)
 // ---------------------------------------------------------------------------
 // auxiliary tree
 // ---------------------------------------------------------------------------
-__global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
-                            const uint32_t *__restrict__ subtree, const uint2 *__restrict__ range,
-                            const uint32_t *__restrict__ run, AuxNode *aux, AuxCold *auxc, uint32_t U,
-                            uint32_t n_prim) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k == 0) {  // the root's own box lives in the header
-        uint32_t rid = hdr->root_cnt > 0 ? 0u : (uint32_t)hdr->root_ref;
-        AuxNode &a = aux[rid];
-        for (int c = 0; c < 3; c++) {
-            a.lo[c] = hdr->root_lo[c];
-            a.hi[c] = hdr->root_hi[c];
-        }
-        if (hdr->root_cnt > 0) {
-            a.size = 1;
-            a.c0 = -1;
-            auxc[rid].first = 0;
-            auxc[rid].count = n_prim;
-            auxc[rid].c1 = -1;
-        }
-    }
-    if (U < 2 || k >= U - 1) return;
+// Inner node k of the LBVH: its children's boxes (and a leaf child's records),
+// its first child, subtree size and record range; ok is cleared when a child's
+// box leaves the float32 screening range.
+__device__ __forceinline__ void aux_build_node(const float4 *__restrict__ nodes, const uint32_t *__restrict__ subtree,
+                                               const uint2 *__restrict__ range, const uint32_t *__restrict__ run,
+                                               AuxNode *aux, AuxCold *auxc, uint32_t U, uint32_t k, bool &ok) {
     const float4 *nd = nodes + 4 * (size_t)k;
     float4 n0 = nd[0], n1 = nd[1], n2 = nd[2];
     int4 n3 = *reinterpret_cast<const int4 *>(nd + 3);
@@ -248,6 +233,8 @@ __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__r
         ids[c] = id;
         AuxNode &a = aux[id];
         a.lo[0] = xy.x; a.hi[0] = xy.y; a.lo[1] = xy.z; a.hi[1] = xy.w; a.lo[2] = zl; a.hi[2] = zh;
+        const float cs[6] = {xy.x, xy.y, xy.z, xy.w, zl, zh};
+        for (int q = 0; q < 6; q++) ok = ok && gbt_phr::phr_screen_ok(cs[q]);
         if (cnt > 0) {
             a.size = 1;
             a.c0 = -1;
@@ -265,14 +252,34 @@ __global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__r
     auxc[k].count = run[lr.y + 1] - run[lr.x];
 }
 
-// Whether every box coordinate lies in the float32 screening range (phr_exact.cuh);
-// the boxes of every cut and of every union of cut nodes are made of these.
-__global__ void k_phr_screen(const AuxNode *__restrict__ aux, uint32_t n_aux, PhrGlobals *g) {
+// Every box it writes is checked against the float32 screening range
+// (phr_exact.cuh); g->screen_bad is set when some coordinate is outside.
+__global__ void k_aux_build(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
+                            const uint32_t *__restrict__ subtree, const uint2 *__restrict__ range,
+                            const uint32_t *__restrict__ run, AuxNode *aux, AuxCold *auxc, uint32_t U,
+                            uint32_t n_prim, PhrGlobals *g) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     bool ok = true;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_aux; i += gridDim.x * blockDim.x) {
-        const AuxNode &a = aux[i];
-        for (int k = 0; k < 3; k++) ok = ok && gbt_phr::phr_screen_ok(a.lo[k]) && gbt_phr::phr_screen_ok(a.hi[k]);
+    auto screen = [&](const AuxNode &a) {
+        for (int c = 0; c < 3; c++) ok = ok && gbt_phr::phr_screen_ok(a.lo[c]) && gbt_phr::phr_screen_ok(a.hi[c]);
+    };
+    if (k == 0) {  // the root's own box lives in the header
+        uint32_t rid = hdr->root_cnt > 0 ? 0u : (uint32_t)hdr->root_ref;
+        AuxNode &a = aux[rid];
+        for (int c = 0; c < 3; c++) {
+            a.lo[c] = hdr->root_lo[c];
+            a.hi[c] = hdr->root_hi[c];
+        }
+        screen(a);
+        if (hdr->root_cnt > 0) {
+            a.size = 1;
+            a.c0 = -1;
+            auxc[rid].first = 0;
+            auxc[rid].count = n_prim;
+            auxc[rid].c1 = -1;
+        }
     }
+    if (U >= 2 && k < U - 1) aux_build_node(nodes, subtree, range, run, aux, auxc, U, k, ok);
     if (__any_sync(0xffffffffu, !ok) && (threadIdx.x & 31) == 0) atomicOr(&g->screen_bad, 1u);
 }
 
@@ -2081,8 +2088,7 @@ int gbt_phr_run(gbt_ctx *ctx, gbt_bvh *aux, double alpha, double delta, int bf, 
     // each node it allocates (children as their jobs attach them), and
     // k_phr_finalize reads only allocated nodes and attached children.
     k_aux_build<<<(U + 255) / 256 + 1, 256, 0, st>>>(aux->d_hdr, aux->d_nodes, aux->d_size, aux->d_range, aux->d_run,
-                                                     d_aux, d_auxc, U, N);
-    k_phr_screen<<<ctx->num_sms * 4, 256, 0, st>>>(d_aux, n_aux, d_g);
+                                                     d_aux, d_auxc, U, N, d_g);
     const int32_t root = h.root_cnt > 0 ? 0 : h.root_ref;
     k_initial_cut<<<1, 1024, 0, st>>>(d_aux, d_auxc, root, thr[0], d_front[0], d_front[1], d_pool[0], d_jobs[0], d_g, 2 * n_aux + 2);
     GBT_CUDA(ctx, cudaGetLastError());
