@@ -121,8 +121,10 @@ int gbt_ctx_set_profiling(gbt_ctx *ctx, int32_t level);
  *                          them with both kernels and synchronises once)
  *   GBT_OPT_KEEP_WORKSPACE 1 (default): a PHR refinement leaves its device
  *                          workspace (about 600 bytes per auxiliary-tree
- *                          triangle) on the context for the next one; 0 frees
- *                          it now and after every refinement
+ *                          triangle) on the context for the next one, and a
+ *                          destroyed tree's device blocks (a PHR tree's arrays,
+ *                          a 4-wide view; up to four) stay on the context for
+ *                          the next trees; 0 frees both now and from then on
  *   GBT_OPT_PHR_SMALL_CUT  1..256 (default 256): PHR levels whose cuts are all
  *                          at most this many nodes run with one-warp blocks in
  *                          batches of launches; a launch that meets a larger
