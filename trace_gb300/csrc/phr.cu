@@ -397,6 +397,103 @@ __device__ Scratch carve(unsigned char *base, uint32_t nmax) {
     return s;
 }
 
+// One compare-exchange of the bitonic network on pair (i, i + j) of the shared
+// arrays, ascending when (i & k) == 0.
+__device__ __forceinline__ void bitonic_cx_shared(unsigned long long *skey, uint32_t *sval, uint32_t i, uint32_t j,
+                                                  uint32_t k) {
+    const uint32_t l = i + j;
+    const unsigned long long ki = skey[i], kl = skey[l];
+    const uint32_t vi = sval[i], vl = sval[l];
+    const bool gt = ki > kl || (ki == kl && vi > vl);
+    if (((i & k) == 0) == gt) {
+        skey[i] = kl;
+        skey[l] = ki;
+        sval[i] = vl;
+        sval[l] = vi;
+    }
+}
+
+// The bitonic network over P = E * blockDim.x (key, position) pairs of the
+// shared arrays, E consecutive ones held in each thread's registers: partners
+// within a thread (stride below E) swap in registers, partners in other lanes
+// of the warp (stride below 32 E) are read through shuffles, and only wider
+// strides go through the shared arrays, with a barrier per stage.  The pairs
+// (key, position) are distinct, so the order is the one any sort gives.
+template <int E>
+__device__ void bitonic_regs(unsigned long long *skey, uint32_t *sval, uint32_t P) {
+    const uint32_t t = threadIdx.x, base = t * E;
+    unsigned long long k[E];
+    uint32_t v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        k[e] = skey[base + e];
+        v[e] = sval[base + e];
+    }
+    for (uint32_t kk = 2; kk <= P; kk <<= 1) {
+        uint32_t j = kk >> 1;
+        if (j >= 32u * E) {
+            __syncthreads();  // every thread has read the arrays it wrote before
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                skey[base + e] = k[e];
+                sval[base + e] = v[e];
+            }
+            __syncthreads();
+            for (; j >= 32u * E; j >>= 1) {
+                for (uint32_t q = t; q < P / 2; q += blockDim.x)
+                    bitonic_cx_shared(skey, sval, ((q & ~(j - 1)) << 1) | (q & (j - 1)), j, kk);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                k[e] = skey[base + e];
+                v[e] = sval[base + e];
+            }
+        }
+        for (; j >= (uint32_t)E; j >>= 1) {  // the partner: same slot, lane ^ (j / E)
+            const uint32_t lx = j / E;
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                const unsigned long long pk = __shfl_xor_sync(0xffffffffu, k[e], lx);
+                const uint32_t pv = __shfl_xor_sync(0xffffffffu, v[e], lx);
+                const uint32_t i = base + e;
+                const bool p_less = pk < k[e] || (pk == k[e] && pv < v[e]);
+                // the lower position of an ascending pair (or the upper of a descending one) keeps the smaller
+                if ((((i & j) == 0) == ((i & kk) == 0)) ? p_less : !p_less) {
+                    k[e] = pk;
+                    v[e] = pv;
+                }
+            }
+        }
+#pragma unroll
+        for (int jj = E / 2; jj > 0; jj >>= 1) {  // the partner in this thread's registers
+            if ((uint32_t)jj > (kk >> 1)) continue;
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                if ((e & jj) == 0) {
+                    const int f = e | jj;
+                    const bool gt = k[e] > k[f] || (k[e] == k[f] && v[e] > v[f]);
+                    if ((((base + e) & kk) == 0) == gt) {
+                        const unsigned long long tk = k[e];
+                        k[e] = k[f];
+                        k[f] = tk;
+                        const uint32_t tv = v[e];
+                        v[e] = v[f];
+                        v[f] = tv;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+        skey[base + e] = k[e];
+        sval[base + e] = v[e];
+    }
+    __syncthreads();
+}
+
 // sort.SliceStable by barycenter component: bitonic sort of (key, input
 // position), so equal keys keep their input order.
 __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t *in, uint32_t n, int axis,
@@ -413,6 +510,17 @@ __device__ void stable_sort_axis(const AuxNode *__restrict__ aux, const uint32_t
         sval[i] = i;
     }
     __syncthreads();
+    // blocks of whole warps sorting 1 to 8 pairs a thread: the network in registers
+    const uint32_t E = P / blockDim.x;
+    if (blockDim.x >= 64 && P >= blockDim.x && P % blockDim.x == 0 && E <= 8) {
+        if (E == 1) bitonic_regs<1>(skey, sval, P);
+        else if (E == 2) bitonic_regs<2>(skey, sval, P);
+        else if (E == 4) bitonic_regs<4>(skey, sval, P);
+        else bitonic_regs<8>(skey, sval, P);
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = in[sval[i]];
+        __syncthreads();
+        return;
+    }
     for (uint32_t k = 2; k <= P; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
             for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
