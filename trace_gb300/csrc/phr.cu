@@ -354,6 +354,7 @@ struct Scratch {
     uint32_t *sval;
     float *lb[6], *rb[6];
     uint32_t *lc, *rc, *flag;
+    float *c32;  // float32 cost of each split position of the sweep in progress
 };
 
 __host__ __device__ inline uint32_t pow2_at_least(uint32_t n) {
@@ -364,7 +365,7 @@ __host__ __device__ inline uint32_t pow2_at_least(uint32_t n) {
 
 __host__ __device__ inline size_t scratch_bytes_for(uint32_t nmax) {
     size_t P = pow2_at_least(nmax > 0 ? nmax : 1);
-    return (size_t)nmax * 4 * 4 + P * 12 + (size_t)nmax * 12 * 4 + (size_t)nmax * 3 * 4 + 256 * 4;
+    return (size_t)nmax * 4 * 4 + P * 12 + (size_t)nmax * 12 * 4 + (size_t)nmax * 4 * 4 + 256 * 4;
 }
 
 __device__ Scratch carve(unsigned char *base, uint32_t nmax) {
@@ -394,6 +395,8 @@ __device__ Scratch carve(unsigned char *base, uint32_t nmax) {
     s.rc = reinterpret_cast<uint32_t *>(p);
     p += (size_t)nmax * 4;
     s.flag = reinterpret_cast<uint32_t *>(p);
+    p += (size_t)nmax * 4;
+    s.c32 = reinterpret_cast<float *>(p);
     return s;
 }
 
@@ -724,8 +727,12 @@ __device__ __forceinline__ void min_cost(const AuxNode *__restrict__ aux, const 
         e.c = x.size;
         run = agg_join(run, e);
     }
-    // backward: inclusive suffix from position i to the end -> right box/count
+    // backward: inclusive suffix from position i to the end -> right box/count, and
+    // the float32 cost of splitting before position i (>= 1) with the left box and
+    // count this thread wrote in the forward pass
     BoxAgg suf = block_scan_agg(loc, (int)blockDim.x - 1 - t, s_tmp, s_rank);
+    float m = INFINITY;  // least float32 cost of this thread's positions, first position
+    uint32_t mi = 0xffffffffu;
     for (uint32_t i = b; i > a; i--) {
         const AuxNode &x = aux[ord[i - 1]];
         BoxAgg e;
@@ -734,25 +741,21 @@ __device__ __forceinline__ void min_cost(const AuxNode *__restrict__ aux, const 
         suf = agg_join(suf, e);
         for (int k = 0; k < 3; k++) { s.rb[k][i - 1] = suf.lo[k]; s.rb[3 + k][i - 1] = suf.hi[k]; }
         s.rc[i - 1] = suf.c;
-    }
-    __syncthreads();
-    auto cost32 = [&](uint32_t i) {
-        const float rl[3] = {s.rb[0][i], s.rb[1][i], s.rb[2][i]}, rh[3] = {s.rb[3][i], s.rb[4][i], s.rb[5][i]};
-        const float ll[3] = {s.lb[0][i], s.lb[1][i], s.lb[2][i]}, lh[3] = {s.lb[3][i], s.lb[4][i], s.lb[5][i]};
-        return __fadd_rn(__fmul_rn(gbt_phr::surface32(rl, rh), gbt_phr::count_f32(s.rc[i])),
-                         __fmul_rn(gbt_phr::surface32(ll, lh), gbt_phr::count_f32(s.lc[i])));
-    };
-    float *s_f = reinterpret_cast<float *>(s_cost);
-    // least float32 cost, first position
-    float m = INFINITY;
-    uint32_t mi = 0xffffffffu;
-    for (uint32_t i = 1 + t; i < n; i += blockDim.x) {
-        const float c = cost32(i);
-        if (c < m) {
-            m = c;
-            mi = i;
+        if (i - 1 >= 1) {
+            const float ll[3] = {s.lb[0][i - 1], s.lb[1][i - 1], s.lb[2][i - 1]};
+            const float lh[3] = {s.lb[3][i - 1], s.lb[4][i - 1], s.lb[5][i - 1]};
+            const float c = __fadd_rn(__fmul_rn(gbt_phr::surface32(suf.lo, suf.hi), gbt_phr::count_f32(suf.c)),
+                                      __fmul_rn(gbt_phr::surface32(ll, lh), gbt_phr::count_f32(s.lc[i - 1])));
+            s.c32[i - 1] = c;
+            if (c <= m) {  // going backwards: an equal cost at a lower position wins
+                m = c;
+                mi = i - 1;
+            }
         }
     }
+    __syncthreads();
+    auto cost32 = [&](uint32_t i) { return s.c32[i]; };
+    float *s_f = reinterpret_cast<float *>(s_cost);
     block_argmin_f32(m, mi, s_f, s_idx);
     const float lim = __fmul_rn(m, gbt_phr::SCREEN_SLACK);
     uint32_t cand = 0;
