@@ -93,6 +93,9 @@ typedef struct {
 } gbt_render_stats;
 
 /* ---- context -------------------------------------------------------- */
+/* Scenes, BVHs, buffers and batches belong to the context they were made on:
+ * destroy them before it (gbt_bvh_destroy hands a tree's device blocks back to
+ * its context). */
 int gbt_ctx_create(int device, gbt_ctx **out);
 int gbt_ctx_destroy(gbt_ctx *ctx);
 const char *gbt_last_error(const gbt_ctx *ctx);
