@@ -363,6 +363,13 @@ __device__ __forceinline__ uint32_t lane_lt() {
 #ifndef GBT_PT_SH
 #define GBT_PT_SH 12
 #endif
+// The same two settings for the any-hit queries past MaxDepth (their own instantiation).
+#ifndef GBT_PT_DYN_ANY
+#define GBT_PT_DYN_ANY GBT_PT_DYN
+#endif
+#ifndef GBT_PT_SH_ANY
+#define GBT_PT_SH_ANY GBT_PT_SH
+#endif
 
 
 // AM 0: closest hit.  AM 1: stop at the first hit found (for rays whose shading only
@@ -374,7 +381,7 @@ __global__ void __launch_bounds__(128, GBT_PT_MINB) k_trace_pt(const BvhHeader *
                                                   const uint32_t *__restrict__ d_count, int out_mode, unsigned int *err,
                                                   unsigned long long *counters, uint32_t *fetch) {
     constexpr int STACK = W == 2 ? 64 : 96;
-    constexpr int SH = GBT_PT_SH;
+    constexpr int SH = AM > 0 ? GBT_PT_SH_ANY : GBT_PT_SH;
     constexpr bool ANY = AM > 0;
     const uint32_t total = d_count ? *d_count : n;
     const uint32_t lane = threadIdx.x & 31;
@@ -594,9 +601,10 @@ template <int W, int DYN>
 void launch_pt_any(gbt_ctx *ctx, const BvhHeader *hdr, const float4 *nodes, const float4 *recs, const float4 *rays,
                    float4 *hits, uint32_t n, const uint32_t *d_count, int out_mode, unsigned long long *counters,
                    cudaStream_t s, bool any) {
+    constexpr int DYN_ANY = DYN > 0 ? GBT_PT_DYN_ANY : 0;
     if (any) {
-        if (counters) launch_pt<W, true, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
-        else launch_pt<W, false, DYN, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
+        if (counters) launch_pt<W, true, DYN_ANY, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
+        else launch_pt<W, false, DYN_ANY, 1>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
     } else {
         if (counters) launch_pt<W, true, DYN, 0>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, counters, s);
         else launch_pt<W, false, DYN, 0>(ctx, hdr, nodes, recs, rays, hits, n, d_count, out_mode, nullptr, s);
