@@ -276,15 +276,21 @@ __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, 
             c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
             c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
             c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
+            // the children any lane hits (warp-uniform): none -> pop, one -> take it unsorted
+            const int nh = (c0.t != MISS) + (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
+            if (nh == 0) {
+                node = pop();
+                continue;
+            }
+            if (nh == 1) {
+                node = c0.t != MISS ? c0.e : c1.t != MISS ? c1.e : c2.t != MISS ? c2.e : c3.e;
+                continue;
+            }
             gbt_dev::cx(c0, c1);
             gbt_dev::cx(c2, c3);
             gbt_dev::cx(c0, c2);
             gbt_dev::cx(c1, c3);
             gbt_dev::cx(c1, c2);
-            if (c0.t == MISS) {
-                node = pop();
-                continue;
-            }
             const int np = (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
             if (sp + np > PSTACK) {
                 if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
