@@ -113,6 +113,20 @@ __device__ __forceinline__ void packet4_loop(int2 node, const float4 *__restrict
             const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab_sel<OCT>(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
             const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab_sel<OCT>(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
             const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab_sel<OCT>(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
+            // the children any lane hits, as one warp-wide mask: none -> pop, one -> take it;
+            // only two or more need the warp's entry distances and the sorting network
+            const uint32_t hm = __reduce_or_sync(FULL, (t0 != MISS ? 1u : 0u) | (t1 != MISS ? 2u : 0u) |
+                                                           (t2 != MISS ? 4u : 0u) | (t3 != MISS ? 8u : 0u));
+            if (hm == 0) {
+                node = pop();
+                continue;
+            }
+            if ((hm & (hm - 1)) == 0) {
+                const int k = __ffs(hm) - 1;
+                node = make_int2(__float_as_int(k == 0 ? rff.x : k == 1 ? rff.y : k == 2 ? rff.z : rff.w),
+                                 __float_as_int(k == 0 ? cnf.x : k == 1 ? cnf.y : k == 2 ? cnf.z : cnf.w));
+                continue;
+            }
             gbt_dev::Cand c0, c1, c2, c3;
             c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
             c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
@@ -122,16 +136,6 @@ __device__ __forceinline__ void packet4_loop(int2 node, const float4 *__restrict
             c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
             c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
             c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
-            // the children any lane hits (warp-uniform): none -> pop, one -> take it unsorted
-            const int nh = (c0.t != MISS) + (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
-            if (nh == 0) {
-                node = pop();
-                continue;
-            }
-            if (nh == 1) {
-                node = c0.t != MISS ? c0.e : c1.t != MISS ? c1.e : c2.t != MISS ? c2.e : c3.e;
-                continue;
-            }
             gbt_dev::cx(c0, c1);
             gbt_dev::cx(c2, c3);
             gbt_dev::cx(c0, c2);
@@ -267,6 +271,20 @@ __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, 
             const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
             const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
             const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
+            // the children any lane hits, as one warp-wide mask: none -> pop, one -> take it;
+            // only two or more need the warp's entry distances and the sorting network
+            const uint32_t hm = __reduce_or_sync(FULL, (t0 != MISS ? 1u : 0u) | (t1 != MISS ? 2u : 0u) |
+                                                           (t2 != MISS ? 4u : 0u) | (t3 != MISS ? 8u : 0u));
+            if (hm == 0) {
+                node = pop();
+                continue;
+            }
+            if ((hm & (hm - 1)) == 0) {
+                const int k = __ffs(hm) - 1;
+                node = make_int2(__float_as_int(k == 0 ? rff.x : k == 1 ? rff.y : k == 2 ? rff.z : rff.w),
+                                 __float_as_int(k == 0 ? cnf.x : k == 1 ? cnf.y : k == 2 ? cnf.z : cnf.w));
+                continue;
+            }
             gbt_dev::Cand c0, c1, c2, c3;
             c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
             c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
@@ -276,16 +294,6 @@ __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, 
             c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
             c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
             c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
-            // the children any lane hits (warp-uniform): none -> pop, one -> take it unsorted
-            const int nh = (c0.t != MISS) + (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
-            if (nh == 0) {
-                node = pop();
-                continue;
-            }
-            if (nh == 1) {
-                node = c0.t != MISS ? c0.e : c1.t != MISS ? c1.e : c2.t != MISS ? c2.e : c3.e;
-                continue;
-            }
             gbt_dev::cx(c0, c1);
             gbt_dev::cx(c2, c3);
             gbt_dev::cx(c0, c2);
