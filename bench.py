@@ -741,10 +741,10 @@ def main():
             # kernels on the PHR(0.5,6,2) tree of the 1M soup (not measured by this run).
             "cache_profile": {
                 "source": "profiles/traversal_kernels_soup1M_phr.md (ncu --set full)",
-                "l2_throughput_pct": {"camera_packets": 1.6, "anyhit_bounce": 16.4},
-                "l1_hit_pct": {"camera_packets": 54.5, "anyhit_bounce": 17.1},
-                "l2_hit_pct": {"camera_packets": 52.7, "anyhit_bounce": 93.5},
-                "warp_efficiency": {"camera_packets": 0.92, "anyhit_bounce": 0.28}}}
+                "l2_throughput_pct": {"camera_packets": 1.8, "anyhit_bounce": 16.4},
+                "l1_hit_pct": {"camera_packets": 54.7, "anyhit_bounce": 17.1},
+                "l2_hit_pct": {"camera_packets": 52.5, "anyhit_bounce": 93.5},
+                "warp_efficiency": {"camera_packets": 0.94, "anyhit_bounce": 0.28}}}
     ctx.check(L.gbt_ctx_set_profiling(h, 0))
 
     # e2e: the C-ABI call with a pinned host image, device->host copy inside the timed region
