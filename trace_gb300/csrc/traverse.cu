@@ -127,6 +127,30 @@ __device__ __forceinline__ void packet4_loop(int2 node, const float4 *__restrict
                                  __float_as_int(k == 0 ? cnf.x : k == 1 ? cnf.y : k == 2 ? cnf.z : cnf.w));
                 continue;
             }
+            if (__popc(hm) == 2) {  // two: the nearer taken, the farther pushed
+                const int ka = __ffs(hm) - 1, kb = __ffs(hm & (hm - 1)) - 1;
+                const float ta = __uint_as_float(__reduce_min_sync(
+                    FULL, __float_as_uint(ka == 0 ? t0 : ka == 1 ? t1 : ka == 2 ? t2 : t3)));
+                const float tb = __uint_as_float(__reduce_min_sync(
+                    FULL, __float_as_uint(kb == 1 ? t1 : kb == 2 ? t2 : t3)));
+                const int2 ea = make_int2(__float_as_int(ka == 0 ? rff.x : ka == 1 ? rff.y : rff.z),
+                                          __float_as_int(ka == 0 ? cnf.x : ka == 1 ? cnf.y : cnf.z));
+                const int2 eb = make_int2(__float_as_int(kb == 1 ? rff.y : kb == 2 ? rff.z : rff.w),
+                                          __float_as_int(kb == 1 ? cnf.y : kb == 2 ? cnf.z : cnf.w));
+                const bool a_first = !(tb < ta);
+                if (sp + 1 > PSTACK) {
+                    if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
+                } else {
+                    if (lane == 0) {
+                        se[sp] = a_first ? eb : ea;
+                        st[sp] = a_first ? tb : ta;
+                    }
+                    sp += 1;
+                    __syncwarp();
+                }
+                node = a_first ? ea : eb;
+                continue;
+            }
             gbt_dev::Cand c0, c1, c2, c3;
             c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
             c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
@@ -283,6 +307,30 @@ __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, 
                 const int k = __ffs(hm) - 1;
                 node = make_int2(__float_as_int(k == 0 ? rff.x : k == 1 ? rff.y : k == 2 ? rff.z : rff.w),
                                  __float_as_int(k == 0 ? cnf.x : k == 1 ? cnf.y : k == 2 ? cnf.z : cnf.w));
+                continue;
+            }
+            if (__popc(hm) == 2) {  // two: the nearer taken, the farther pushed
+                const int ka = __ffs(hm) - 1, kb = __ffs(hm & (hm - 1)) - 1;
+                const float ta = __uint_as_float(__reduce_min_sync(
+                    FULL, __float_as_uint(ka == 0 ? t0 : ka == 1 ? t1 : ka == 2 ? t2 : t3)));
+                const float tb = __uint_as_float(__reduce_min_sync(
+                    FULL, __float_as_uint(kb == 1 ? t1 : kb == 2 ? t2 : t3)));
+                const int2 ea = make_int2(__float_as_int(ka == 0 ? rff.x : ka == 1 ? rff.y : rff.z),
+                                          __float_as_int(ka == 0 ? cnf.x : ka == 1 ? cnf.y : cnf.z));
+                const int2 eb = make_int2(__float_as_int(kb == 1 ? rff.y : kb == 2 ? rff.z : rff.w),
+                                          __float_as_int(kb == 1 ? cnf.y : kb == 2 ? cnf.z : cnf.w));
+                const bool a_first = !(tb < ta);
+                if (sp + 1 > PSTACK) {
+                    if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
+                } else {
+                    if (lane == 0) {
+                        s_e[wp][sp] = a_first ? eb : ea;
+                        s_t[wp][sp] = a_first ? tb : ta;
+                    }
+                    sp += 1;
+                    __syncwarp();
+                }
+                node = a_first ? ea : eb;
                 continue;
             }
             gbt_dev::Cand c0, c1, c2, c3;
