@@ -253,9 +253,8 @@ __global__ void __launch_bounds__(128) k_trace_packet4(const BvhHeader *__restri
 
 // One packet walk over a 4-wide tree by a warp of a 128-thread block: every
 // lane takes part (a lane without a ray carries one that misses everything).
-// The warp's stack lives in shared memory.  The walk is k_trace_packet4's
-// (above); that kernel keeps its own inline copy, which ptxas allocates
-// without spills (as a call of this function it spills 20 bytes).
+// The warp's stack lives in shared memory; the node loop is k_trace_packet4's
+// general one (instantiated per octant as well, it left this kernel spilling).
 template <bool COUNT>
 __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, const float4 *__restrict__ nodes,
                                              const float4 *__restrict__ recs, const gbt_dev::Ray &r, gbt_dev::Hit &h,
@@ -265,110 +264,11 @@ __device__ __forceinline__ void packet_walk4(const BvhHeader *__restrict__ hdr, 
     __shared__ int2 s_e[4][PSTACK];
     __shared__ float s_t[4][PSTACK];
     const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float MISS = __int_as_float(0x7f800000);
     float te;
     const bool root_hit = gbt_dev::slab(hdr->root_lo[0], hdr->root_lo[1], hdr->root_lo[2], hdr->root_hi[0],
                                         hdr->root_hi[1], hdr->root_hi[2], r, h.t, te);
-    int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
-    int sp = 0;
-    auto pop = [&]() -> int2 {
-        while (sp > 0) {
-            --sp;
-            const float t = s_t[wp][sp];
-            const int2 e = s_e[wp][sp];
-            if (__any_sync(FULL, t <= h.t * 1.0000005f)) return e;
-        }
-        return make_int2(0, -1);
-    };
-    for (;;) {
-        if (node.y == 0) {
-            if (COUNT && lane == 0) w.nodes++;
-            const float4 *nd = nodes + 8 * (size_t)node.x;
-            float4 lx, hx, ly, hy, lz, hz, rff, cnf;
-            gbt_dev::ldg256(nd, lx, hx);
-            gbt_dev::ldg256(nd + 2, ly, hy);
-            gbt_dev::ldg256(nd + 4, lz, hz);
-            gbt_dev::ldg256(nd + 6, rff, cnf);
-            float t;
-            // per lane entry distance (+0 for -0, so that unsigned min orders them), MISS if missed
-            const float t0 = (__float_as_int(cnf.x) >= 0 && gbt_dev::slab(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, r, h.t, t)) ? t + 0.f : MISS;
-            const float t1 = (__float_as_int(cnf.y) >= 0 && gbt_dev::slab(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, r, h.t, t)) ? t + 0.f : MISS;
-            const float t2 = (__float_as_int(cnf.z) >= 0 && gbt_dev::slab(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, r, h.t, t)) ? t + 0.f : MISS;
-            const float t3 = (__float_as_int(cnf.w) >= 0 && gbt_dev::slab(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, r, h.t, t)) ? t + 0.f : MISS;
-            // the children any lane hits, as one warp-wide mask: none -> pop, one -> take it;
-            // only two or more need the warp's entry distances and the sorting network
-            const uint32_t hm = __reduce_or_sync(FULL, (t0 != MISS ? 1u : 0u) | (t1 != MISS ? 2u : 0u) |
-                                                           (t2 != MISS ? 4u : 0u) | (t3 != MISS ? 8u : 0u));
-            if (hm == 0) {
-                node = pop();
-                continue;
-            }
-            if ((hm & (hm - 1)) == 0) {
-                const int k = __ffs(hm) - 1;
-                node = make_int2(__float_as_int(k == 0 ? rff.x : k == 1 ? rff.y : k == 2 ? rff.z : rff.w),
-                                 __float_as_int(k == 0 ? cnf.x : k == 1 ? cnf.y : k == 2 ? cnf.z : cnf.w));
-                continue;
-            }
-            if (__popc(hm) == 2) {  // two: the nearer taken, the farther pushed
-                const int ka = __ffs(hm) - 1, kb = __ffs(hm & (hm - 1)) - 1;
-                const float ta = __uint_as_float(__reduce_min_sync(
-                    FULL, __float_as_uint(ka == 0 ? t0 : ka == 1 ? t1 : ka == 2 ? t2 : t3)));
-                const float tb = __uint_as_float(__reduce_min_sync(
-                    FULL, __float_as_uint(kb == 1 ? t1 : kb == 2 ? t2 : t3)));
-                const int2 ea = make_int2(__float_as_int(ka == 0 ? rff.x : ka == 1 ? rff.y : rff.z),
-                                          __float_as_int(ka == 0 ? cnf.x : ka == 1 ? cnf.y : cnf.z));
-                const int2 eb = make_int2(__float_as_int(kb == 1 ? rff.y : kb == 2 ? rff.z : rff.w),
-                                          __float_as_int(kb == 1 ? cnf.y : kb == 2 ? cnf.z : cnf.w));
-                const bool a_first = !(tb < ta);
-                if (sp + 1 > PSTACK) {
-                    if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
-                } else {
-                    if (lane == 0) {
-                        s_e[wp][sp] = a_first ? eb : ea;
-                        s_t[wp][sp] = a_first ? tb : ta;
-                    }
-                    sp += 1;
-                    __syncwarp();
-                }
-                node = a_first ? ea : eb;
-                continue;
-            }
-            gbt_dev::Cand c0, c1, c2, c3;
-            c0.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t0)));
-            c1.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t1)));
-            c2.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t2)));
-            c3.t = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(t3)));
-            c0.e = make_int2(__float_as_int(rff.x), __float_as_int(cnf.x));
-            c1.e = make_int2(__float_as_int(rff.y), __float_as_int(cnf.y));
-            c2.e = make_int2(__float_as_int(rff.z), __float_as_int(cnf.z));
-            c3.e = make_int2(__float_as_int(rff.w), __float_as_int(cnf.w));
-            gbt_dev::cx(c0, c1);
-            gbt_dev::cx(c2, c3);
-            gbt_dev::cx(c0, c2);
-            gbt_dev::cx(c1, c3);
-            gbt_dev::cx(c1, c2);
-            const int np = (c1.t != MISS) + (c2.t != MISS) + (c3.t != MISS);
-            if (sp + np > PSTACK) {
-                if (lane == 0) atomicOr(err, GBT_DEVERR_STACK);
-            } else {
-                if (lane == 0) {
-                    int q = sp;
-                    if (c3.t != MISS) { s_e[wp][q] = c3.e; s_t[wp][q] = c3.t; ++q; }
-                    if (c2.t != MISS) { s_e[wp][q] = c2.e; s_t[wp][q] = c2.t; ++q; }
-                    if (c1.t != MISS) { s_e[wp][q] = c1.e; s_t[wp][q] = c1.t; ++q; }
-                }
-                sp += np;
-                __syncwarp();
-            }
-            node = c0.e;
-        } else if (node.y > 0) {
-            if (COUNT && lane == 0) w.prims += (uint32_t)node.y;
-            gbt_dev::leaf(recs, node.x, node.y, r, h);
-            node = pop();
-        } else {
-            break;
-        }
-    }
+    const int2 node = __any_sync(FULL, root_hit) ? make_int2(hdr->root_ref, hdr->root_cnt) : make_int2(0, -1);
+    packet4_loop<COUNT, -1>(node, nodes, recs, r, h, s_e[wp], s_t[wp], lane, err, w);
     __syncwarp();  // the stack is free for the warp's next walk
 }
 
